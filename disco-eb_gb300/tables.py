@@ -1,0 +1,106 @@
+"""Pack a cosmology ``param`` dict into the flat FP64 blob the GPU receives.
+
+Layout (one blob per cosmology, all cosmologies of a batch the same length;
+the C side of the layout is ``include/discoeb_gb300.h``):
+
+* ``HDR_LEN`` = 32 header doubles: the scalars the reference reads from
+  ``param`` (``perturbations.py:113-371``, ``background.py:100-122``), the
+  momentum-bin count, the seven spline sizes, the blob length and a magic
+  number;
+* seven natural cubic splines, each stored as ``x[n], y[n], S[n]``
+  (``spline_interpolation.py:112-113`` fields ``_x_``, ``_y_``, ``_S_full_``)
+  in the order of :data:`SPLINE_KEYS`;
+* the ``nq`` momentum nodes q and kernel weights w of
+  ``get_neutrino_momentum_bins`` (``background.py:13-44``).
+
+Splines are read duck-typed through ``_x_``, ``_y_``, ``_S_full_`` so a
+``param`` produced by the reference's own ``evolve_background`` packs the
+same way as one produced by :func:`background.evolve_background`.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .background import get_neutrino_momentum_bins
+
+HDR_LEN = 32
+MAGIC = 20231103.0
+SCALAR_KEYS = ("Omegam", "Omegab", "OmegaDE", "Omegak", "grhom", "grhog", "grhor", "Neff", "Nmnu",
+               "amnu", "w_DE_0", "w_DE_a", "cs2_DE", "YHe", "H0", "taumin", "A_s", "n_s", "k_p")
+H_NQ = 19
+H_NSPL0 = 20
+H_BLOBLEN = 27
+H_MAGIC = 28
+SPLINE_KEYS = ("xe_of_loga_spline", "cs2a_of_loga_spline", "logrhonu_of_loga_spline",
+               "logpnu_of_loga_spline", "a_of_tau_spline", "tau_of_a_spline", "xe_of_tau_spline")
+SP_TAU_OF_A = 5
+
+
+def _arr(x):
+    if hasattr(x, "__array__"):
+        return np.asarray(x, dtype=np.float64)
+    return np.asarray(x, dtype=np.float64)
+
+
+def blob_length(spline_sizes, nq: int) -> int:
+    return HDR_LEN + 3 * int(sum(spline_sizes)) + 2 * nq
+
+
+def pack_cosmology(param: dict, nqmax: int) -> np.ndarray:
+    """One cosmology's FP64 table blob."""
+    scal = []
+    for key in SCALAR_KEYS:
+        if key == "k_p":
+            scal.append(float(param.get("k_p", 0.05)))
+        elif key == "Omegak":
+            scal.append(float(param.get("Omegak", 0.0)))
+        else:
+            if key not in param:
+                raise KeyError(f"param is missing '{key}' (run evolve_background first)")
+            scal.append(float(np.asarray(param[key])))
+    splines = []
+    for key in SPLINE_KEYS:
+        sp = param[key]
+        x, y, S = _arr(sp._x_), _arr(sp._y_), _arr(sp._S_full_)
+        if not (x.shape == y.shape == S.shape) or x.ndim != 1 or x.shape[0] < 2:
+            raise ValueError(f"spline '{key}' has inconsistent arrays")
+        splines.append((x, y, S))
+    q, w = get_neutrino_momentum_bins(nqmax)
+    sizes = [s[0].shape[0] for s in splines]
+    L = blob_length(sizes, nqmax)
+    b = np.zeros(L, dtype=np.float64)
+    b[: len(scal)] = scal
+    b[H_NQ] = nqmax
+    b[H_NSPL0:H_NSPL0 + 7] = sizes
+    b[H_BLOBLEN] = L
+    b[H_MAGIC] = MAGIC
+    p = HDR_LEN
+    for (x, y, S) in splines:
+        n = x.shape[0]
+        b[p:p + n] = x
+        b[p + n:p + 2 * n] = y
+        b[p + 2 * n:p + 3 * n] = S
+        p += 3 * n
+    b[p:p + nqmax] = q
+    b[p + nqmax:p + 2 * nqmax] = w
+    return b
+
+
+def pack_batch(params, nqmax: int) -> np.ndarray:
+    """[ncosmo, blob_len] table array; all cosmologies must share spline sizes."""
+    blobs = [pack_cosmology(p, nqmax) for p in params]
+    L = blobs[0].shape[0]
+    for bb in blobs:
+        if bb.shape[0] != L or not np.array_equal(bb[H_NSPL0:H_NSPL0 + 7], blobs[0][H_NSPL0:H_NSPL0 + 7]):
+            raise ValueError("all cosmologies of one batch need identical table sizes")
+    return np.ascontiguousarray(np.stack(blobs))
+
+
+def tau_of_a(param: dict, aexp) -> np.ndarray:
+    """Conformal times of the output scale factors (``perturbations.py:975``)."""
+    from .spline import SplineInterpolation
+
+    sp = param["tau_of_a_spline"]
+    s = SplineInterpolation.__new__(SplineInterpolation)
+    s._x_, s._y_, s._S_full_ = _arr(sp._x_), _arr(sp._y_), _arr(sp._S_full_)
+    return s.evaluate(np.atleast_1d(np.asarray(aexp, dtype=np.float64)))

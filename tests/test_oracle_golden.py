@@ -1,0 +1,88 @@
+"""The oracle pinned against the reference's own golden vectors (CPU only)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import discoeb_gb300.tables as tb
+from discoeb_gb300.spline import SplineInterpolation
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_class_pkbc_at_a0p01(test_cosmology):
+    """P_bc(k) at a=0.01 vs CLASS within 5e-3, the reference's own bar
+    (tests/test_perturbations.py:128-142: lmax 31, nqmax 5, rtol=atol=1e-5)."""
+    g = json.load(open(os.path.join(GOLD, "class_pkbc_a0p01.json")))
+    kc, Pc = np.array(g["k"]), np.array(g["Pkbc"])
+    sel = np.arange(0, kc.shape[0], 20)
+    p = test_cosmology
+    blob = tb.pack_cosmology(p, 5)
+    tau_out = tb.tau_of_a(p, [0.01])
+    y, st = oracle.solve(blob, kc[sel], tau_out, lmaxg=31, lmaxgp=31, lmaxr=31, lmaxnu=31, nqmax=5,
+                         rtol=1e-5, atol=1e-5, max_steps=2048)
+    assert (st[:, 0] == 0).all()
+    k = kc[sel]
+    P = 2 * np.pi**2 * p["A_s"] * (k / 0.05) ** (p["n_s"] - 1) * k**-3 * y[:, 0, 6] ** 2
+    np.testing.assert_allclose(P, Pc[sel], rtol=5e-3)
+
+
+def test_recfast_xe_vs_v010_baseline(test_cosmology):
+    """x_e(a) vs the DISCO-EB v0.1.0 RECFAST fixture.
+
+    Before and after recombination the tables follow the fixture to 0.1%;
+    through recombination the reference's GRK4A (all stages at t0,
+    ode_integrators_stiff.py:192-200) differs from that older baseline by
+    several per cent, so the bar there is 10%.
+    """
+    g = json.load(open(os.path.join(GOLD, "recfast_xe_v010.json")))
+    a, xr = np.array(g["a"]), np.array(g["xe"])
+    p = test_cosmology
+    m = a <= 1.0
+    xe = p["xe_of_tau_spline"].evaluate(p["tau_of_a_spline"].evaluate(a[m]))
+    rel = np.abs(xe / xr[m] - 1)
+    early = a[m] < 1.0 / 20001.0
+    assert rel[early].max() < 1e-3
+    assert rel.max() < 0.1
+
+
+def test_oracle_jacobian_matches_finite_differences(test_cosmology):
+    dims = (12, 12, 17, 17, 15)
+    blob = tb.pack_cosmology(test_cosmology, 15)
+    k = 0.3
+    tau0, y0 = oracle.initial(blob, dims, k, 1e4)
+    rng = np.random.default_rng(0)
+    y = y0 * (1 + 0.1 * rng.standard_normal(y0.shape)) + 1e-3 * rng.standard_normal(y0.shape)
+    y[0] = y0[0] * 3.0
+    tau = tau0 * 3.0
+    J, dT = oracle.jacobian(blob, dims, k, tau, y)
+    n = y.shape[0]
+    for j in list(range(0, 12)) + [n - 2, n - 1]:
+        h = 1e-6 * max(abs(y[j]), 1e-8)
+        yp, ym = y.copy(), y.copy()
+        yp[j] += h
+        ym[j] -= h
+        fd = (oracle.rhs(blob, dims, k, tau, yp) - oracle.rhs(blob, dims, k, tau, ym)) / (2 * h)
+        scale = np.abs(J[:, j]).max() + 1e-300
+        assert np.abs(fd - J[:, j]).max() <= 1e-4 * scale, j
+    ht = 1e-6 * tau
+    fdt = (oracle.rhs(blob, dims, k, tau + ht, y) - oracle.rhs(blob, dims, k, tau - ht, y)) / (2 * ht)
+    np.testing.assert_allclose(dT, fdt, rtol=1e-5, atol=1e-12 * np.abs(fdt).max())
+
+
+def test_oracle_spline_matches_host_spline(test_cosmology):
+    p = test_cosmology
+    blob = tb.pack_cosmology(p, 3)
+    for which, key in enumerate(tb.SPLINE_KEYS):
+        sp = p[key]
+        x = np.sort(np.concatenate([sp._x_[:-1] + 0.37 * np.diff(sp._x_), sp._x_]))
+        np.testing.assert_allclose(oracle.spline_eval(blob, which, x), sp.evaluate(x), rtol=1e-13, atol=1e-300)
+
+
+def test_natural_spline_reproduces_cubic_interior():
+    x = np.linspace(0.0, 2.0, 41)
+    s = SplineInterpolation(x, np.sin(x))
+    xx = np.linspace(0.3, 1.7, 57)
+    np.testing.assert_allclose(s.evaluate(xx), np.sin(xx), atol=2e-6)
