@@ -1,0 +1,296 @@
+"""Benchmark of the perturbation hot path on GB300.
+
+Workload (default): 64 cosmologies drawn uniformly over Omegam [.25,.35],
+Omegab [.04,.055], h [.6,.75], n_s [.92,1], ln(1e10 A_s) [2.9,3.2],
+m_nu [.06,.3] eV, w0 [-1.2,-.8], wa [-.3,.3] (w(a) = -1 crossings redrawn),
+each with 512 log-spaced k in [1e-4, 10] /Mpc, lmaxg=lmaxgp=12, lmaxr=17,
+lmaxnu=17, nqmax=15 (nvar 323), output at a=1, rtol=atol=1e-5: 32768 modes
+in one persistent launch.  A "step" is one full solve of that batch plus the
+P(k) assembly.  ``value`` is cosmologies (full k-grids) per second with the
+inputs resident on the device; ``e2e`` is the same through the public call
+with host inputs (tables, k-grid, output times copied in, all 20 output
+fields copied out, every step).
+
+``--impl reference`` times the CPU restatement of the reference algorithm
+(``oracle/``: Rodas5 + PID + dense forward-mode Jacobian + dense LU, FP64,
+OpenMP over modes) on the host cores on a bounded sample of the same
+workload: the reference's own JAX code is not installable here.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (ncosmo, num_k, kmin, kmax, dims, rtol, atol)
+    "batched_64cosmo_512k_n323_rtol1e-5": (64, 512, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
+    "batched_8cosmo_512k_n323_rtol1e-5": (8, 512, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
+    "single_1cosmo_256k_n323_rtol1e-5": (1, 256, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
+}
+DEFAULT_WORKLOAD = "batched_64cosmo_512k_n323_rtol1e-5"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_inputs(name, rank=0, world=1, seed=1234):
+    from discoeb_gb300 import background, tables
+    from discoeb_gb300.workloads import sample_cosmologies
+
+    ncosmo, num_k, kmin, kmax, dims, rtol, atol = WORKLOADS[name]
+    params, rejected = sample_cosmologies(ncosmo * world, seed=seed)
+    mine = params[rank * ncosmo:(rank + 1) * ncosmo]
+    ps = [background.evolve_background(param=p) for p in mine]
+    tabs = tables.pack_batch(ps, dims["nqmax"])
+    tau = np.stack([tables.tau_of_a(p, [1.0]) for p in ps])
+    k = np.geomspace(kmin, kmax, num_k)
+    kk = np.tile(k, ncosmo)
+    com = np.repeat(np.arange(ncosmo, dtype=np.int32), num_k)
+    return dict(ps=ps, tables=tabs, tau=tau, k=kk, cosmo=com, dims=dims, rtol=rtol, atol=atol, ncosmo=ncosmo,
+                num_k=num_k, rejected=rejected)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.samples = []
+        self._p = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                        "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self._p = None
+        return self
+
+    def _read(self):
+        for line in self._p.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self._p is not None:
+            self._p.terminate()
+            try:
+                self._p.wait(timeout=5)
+            except Exception:
+                self._p.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_baseline(inp, seconds=20.0, threads=0):
+    """Oracle (CPU port, FP64, OpenMP over modes) on a bounded sample of the
+    workload; returns cosmology solves/s scaled from the sampled modes."""
+    import oracle
+
+    threads = threads or os.cpu_count() or 1
+    num_k = inp["num_k"]
+    # sample: every s-th k of cosmology 0, growing until the time budget is used
+    stride = 64
+    done_modes, t_used = 0, 0.0
+    while True:
+        sel = np.arange(0, num_k, stride)
+        t = time.perf_counter()
+        oracle.solve(inp["tables"][0], inp["k"][sel], inp["tau"][0], rtol=inp["rtol"], atol=inp["atol"],
+                     nthreads=threads, **inp["dims"])
+        dt = time.perf_counter() - t
+        done_modes += sel.size
+        t_used += dt
+        if t_used >= seconds or stride == 1:
+            break
+        stride = max(1, stride // 2)
+    per_mode = t_used / done_modes
+    return {"value": 1.0 / (per_mode * num_k), "unit": "cosmology solves/s", "cores": threads, "kind": "port",
+            "sample": f"{done_modes} modes of cosmology 0 (k strided over the 512-point grid), {t_used:.1f} s"}
+
+
+def algorithmic_flops_per_step(dims, nq):
+    """FP64 flops of one attempted step of the structured Rodas5 solve."""
+    from discoeb_gb300.perturbations import nvar
+
+    n = nvar(dims["lmaxg"], dims["lmaxgp"], dims["lmaxr"], dims["lmaxnu"], dims["nqmax"])
+    rhs = 12 * n + 60 * nq + 220          # one RHS evaluation
+    rhs_dual = 2 * rhs                    # f and d f / d a
+    stage_sums = 2 * n * (1 + 2 + 3 + 4 + 5 + 1 + 1)   # u_i
+    stage_rhs = 2 * n * (0 + 1 + 2 + 3 + 4 + 5 + 6 + 7) + 4 * n   # C_ij k_j and d_i dT
+    factor = 10 * n + 600 + 2 * 13 * n    # chain pivots, 8x8 LU, Z_h, Z_e
+    solves = 8 * 13 * n                   # per-stage structured solve
+    ctrl = 2 * n + 80
+    return rhs_dual + 7 * rhs + stage_sums + stage_rhs + factor + solves + ctrl
+
+
+def run_ours(args):
+    import torch
+
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    import discoeb_gb300 as deb
+    from discoeb_gb300 import _native, perturbations as pt
+
+    inp = make_inputs(args.workload, rank, world)
+    dims = inp["dims"]
+    prob = deb.DeviceProblem(inp["tables"], inp["k"], inp["tau"], inp["cosmo"], **dims)
+    cfg = pt._cfg(inp["rtol"], inp["atol"], 0.25, 0.80, 0.0, 20.0, 0.3, args.max_steps)
+    stream = torch.cuda.current_stream()
+
+    def one_step():
+        prob.launch(cfg, stream)
+        return prob.power(4, stream)
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    st = prob.status.cpu().numpy()
+    steps = prob.steps.cpu().numpy()
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            ev0[i].record(stream)
+            prob.launch(cfg, stream)
+            ev1[i].record(stream)
+            prob.power(4, stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if world > 1:
+        torch.distributed.barrier()
+    kern_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+    t_step = wall / args.steps
+    if world > 1:
+        tt = torch.tensor([t_step], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(tt.item())
+    total_cosmo = inp["ncosmo"] * world
+    value = total_cosmo / t_step
+
+    # end to end through the public call with host buffers
+    e2e_steps = max(1, min(args.steps, 3))
+    host_tabs, host_k, host_tau, host_com = (np.ascontiguousarray(inp["tables"]), np.ascontiguousarray(inp["k"]),
+                                             np.ascontiguousarray(inp["tau"]), np.ascontiguousarray(inp["cosmo"]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        y = deb.solve(host_tabs, host_k, host_tau, host_com, rtol=inp["rtol"], atol=inp["atol"], max_steps=args.max_steps,
+                      throw=False, **dims)
+    torch.cuda.synchronize()
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    h2d = host_tabs.nbytes + host_k.nbytes + host_tau.nbytes + host_com.nbytes
+    d2h = int(y.nbytes) + prob.status.numel() * 4
+
+    peak = _native.measure_fp64_peak(stream.cuda_stream)
+    nsteps_attempted = int(steps.sum())
+    flops = algorithmic_flops_per_step(dims, dims["nqmax"]) * nsteps_attempted
+    kern_s = statistics.median(kern_ms) * 1e-3
+    achieved = flops / kern_s
+    out = {
+        "metric": "P(k) forward solves/s on 1 GB300, batched FP64 structured Rodas5 (gradient not included)",
+        "value": value, "unit": "cosmology solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded cosmology sample, host RECFAST tables)",
+        "config": {"workload": args.workload, "ncosmo_per_gpu": inp["ncosmo"], "num_k": inp["num_k"],
+                   "modes_per_step": int(inp["k"].shape[0]), "nvar": prob.n, "rtol": inp["rtol"],
+                   "linear_solver": "structured", "l2": "working set > L2 (workspace %.2f GB)" % (prob.plan.workspace_bytes() / 1e9),
+                   "redrawn_cosmologies": inp["rejected"]},
+        "e2e": {"value": total_cosmo / t_e2e if world == 1 else None, "unit": "cosmology solves/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "note": "FP64-pipe bound; peak = FP64 FMA microkernel measured in this run"},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk.summary(),
+        "kernel_ms_median": statistics.median(kern_ms),
+        "attempted_steps_per_launch": nsteps_attempted,
+        "mode_status_nonzero": int((st != 0).sum()),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(inp, seconds=args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    world, rank, local = _dist()
+    if rank != 0:
+        return
+    inp = make_inputs(args.workload, 0, 1)
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(inp, seconds=args.cpu_seconds / 2, threads=threads)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = statistics.median(vals)
+    out = {"impl": "reference", "metric": "P(k) forward solves/s on 1 GB300, batched FP64 structured Rodas5 (gradient not included)",
+           "value": v * 1.0, "unit": "cosmology solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded cosmology sample, host RECFAST tables)",
+           "config": {"workload": args.workload, "ncosmo_per_gpu": inp["ncosmo"], "num_k": inp["num_k"]},
+           "cpu_baseline": {"value": v, "unit": "cosmology solves/s", "cores": threads, "kind": "port",
+                            "sample": cb["sample"]},
+           "e2e": {"value": v, "unit": "cosmology solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "reference JAX path not installable offline; CPU restatement of its algorithm timed instead"}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--max-steps", type=int, default=4096)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,95 @@
+"""ctypes binding of the C ABI in ``include/discoeb_gb300.h``.
+
+The CUDA library is the only compute path: if it is missing or no CUDA
+device is present, every call raises.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libdiscoeb_gb300.so")
+
+DEB_SOLVE_STRUCTURED = 0
+DEB_SOLVE_DENSE = 1
+MODE_STATUS = {0: "OK", 1: "MAX_STEPS", 2: "DT_UNDERFLOW", 3: "NONFINITE", 4: "BAD_INPUT"}
+
+
+class DebDims(ctypes.Structure):
+    _fields_ = [("lmaxg", ctypes.c_int), ("lmaxgp", ctypes.c_int), ("lmaxr", ctypes.c_int), ("lmaxnu", ctypes.c_int),
+                ("nqmax", ctypes.c_int), ("nout", ctypes.c_int), ("return_full", ctypes.c_int),
+                ("linear_solver", ctypes.c_int)]
+
+
+class DebSolverCfg(ctypes.Structure):
+    _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double), ("pcoeff", ctypes.c_double),
+                ("icoeff", ctypes.c_double), ("dcoeff", ctypes.c_double), ("factormax", ctypes.c_double),
+                ("factormin", ctypes.c_double), ("safety", ctypes.c_double), ("error_order", ctypes.c_double),
+                ("max_steps", ctypes.c_int), ("hist_on_reject", ctypes.c_int)]
+
+
+_lib = None
+EXPORTS = ("deb_nvar", "deb_plan_create", "deb_plan_workspace_bytes", "deb_forward", "deb_get_power",
+           "deb_plan_destroy", "deb_measure_fp64_peak", "deb_error_string", "deb_version")
+
+
+def load(path: str | None = None):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"CUDA library not built: {p} is missing (run __graft_entry__.build() "
+                           f"or python disco-eb_gb300/build.py)")
+    L = ctypes.CDLL(p)
+    vp = ctypes.c_void_p
+    L.deb_nvar.argtypes = [ctypes.POINTER(DebDims)]
+    L.deb_plan_create.argtypes = [ctypes.POINTER(DebDims), ctypes.c_int, ctypes.POINTER(vp)]
+    L.deb_plan_workspace_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
+    L.deb_forward.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp,
+                              ctypes.POINTER(DebSolverCfg), vp, vp, vp, vp]
+    L.deb_get_power.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
+                                ctypes.c_int, vp, vp]
+    L.deb_plan_destroy.argtypes = [vp]
+    L.deb_plan_destroy.restype = None
+    L.deb_measure_fp64_peak.argtypes = [ctypes.POINTER(ctypes.c_double), vp]
+    L.deb_error_string.argtypes = [ctypes.c_int]
+    L.deb_error_string.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def check(rc: int, what: str):
+    if rc != 0:
+        msg = load().deb_error_string(rc).decode()
+        raise RuntimeError(f"{what} failed: {msg} ({rc})")
+
+
+class Plan:
+    """Owns one deb_plan (device workspace sized for max_modes)."""
+
+    def __init__(self, dims: DebDims, max_modes: int):
+        self.dims = dims
+        self.max_modes = max_modes
+        self.ptr = ctypes.c_void_p()
+        check(load().deb_plan_create(ctypes.byref(dims), int(max_modes), ctypes.byref(self.ptr)), "deb_plan_create")
+
+    def workspace_bytes(self) -> int:
+        b = ctypes.c_size_t()
+        check(load().deb_plan_workspace_bytes(self.ptr, ctypes.byref(b)), "deb_plan_workspace_bytes")
+        return int(b.value)
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                load().deb_plan_destroy(self.ptr)
+        except Exception:
+            pass
+
+
+def measure_fp64_peak(stream: int = 0) -> float:
+    v = ctypes.c_double()
+    check(load().deb_measure_fp64_peak(ctypes.byref(v), ctypes.c_void_p(stream)), "deb_measure_fp64_peak")
+    return float(v.value)

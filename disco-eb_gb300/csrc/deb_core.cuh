@@ -1,0 +1,1060 @@
+// deb_core.cuh -- per-mode perturbation solver: physics, structured linear
+// algebra, Rodas5 step and PID control.  Written once as host/device code:
+// the CUDA kernel (deb_solver.cu) runs it with one thread per k-mode; the
+// test suite also compiles it for the host to check the exact kernel logic
+// against the oracle without a GPU.
+//
+// Reference correspondence (file:line of DISCO-EB):
+//   spline evaluate            src/discoeb/spline_interpolation.py:130-153
+//   conformal Hubble rate      src/discoeb/background.py:100-122
+//   synchronous-gauge RHS      src/discoeb/perturbations.py:84-371 (nu_perturb :22-50)
+//   output conversion          src/discoeb/perturbations.py:374-523
+//   adiabatic ICs              src/discoeb/perturbations.py:526-627
+//   start time                 src/discoeb/perturbations.py:630-681, util.py:365-396
+//   Rodas5 transformed step    src/discoeb/ode_integrators_stiff.py:622-834
+//   PID control + error norm   src/discoeb/perturbations.py:701-724, 756-771
+//
+// Linear algebra.  The reference factors W = I/(gamma h) - J densely (LU
+// with partial pivoting).  Here W is factored exactly through its structure:
+//   * row 0 (a' depends only on a) is solved first and column 0 moved to the
+//     right-hand side; variable 1 (a h', never read by the RHS) is solved last;
+//   * the remaining J is  B + u_h g_h^T + u_e g_e^T : B holds the local
+//     couplings (tridiagonal multipole chains, an 8x8 photon-baryon core,
+//     2x2 CDM and DE blocks) and the two rank-1 terms are the metric
+//     functionals h' and eta' that every species reads;
+//   * M = I/(gamma h) - B is factored block by block (chain tails eliminated
+//     from lmax downwards, 8x8 core with partial pivoting) and the rank-2
+//     term is applied exactly with the Woodbury identity.
+// The result equals the dense solution to rounding; the work is O(n).
+#pragma once
+
+#ifdef __CUDACC__
+#define HD __host__ __device__ __forceinline__
+#ifdef __CUDA_ARCH__
+#define LDG(p) __ldg(p)
+#else
+#define LDG(p) (*(p))
+#endif
+#else
+#include <cmath>
+#include <algorithm>
+#define HD inline
+#define LDG(p) (*(p))
+#endif
+
+namespace deb {
+
+#ifndef __CUDACC__
+using std::exp; using std::log; using std::sqrt; using std::fabs; using std::pow;
+using std::min; using std::max;
+HD bool isfinite_(double x) { return std::isfinite(x); }
+#else
+HD bool isfinite_(double x) { return isfinite(x); }
+#endif
+
+// ------------------------------------------------------------------ blob layout
+enum { H_OMEGAM = 0, H_OMEGAB, H_OMEGADE, H_OMEGAK, H_GRHOM, H_GRHOG, H_GRHOR, H_NEFF, H_NMNU,
+       H_AMNU, H_W0, H_WA, H_CS2DE, H_YHE, H_H0, H_TAUMIN, H_AS, H_NS, H_KP, H_NQ,
+       H_NSPL0 = 20, H_BLOBLEN = 27, H_MAGIC = 28, HDR_LEN = 32 };
+enum { SP_XE_LOGA = 0, SP_CS2A_LOGA, SP_LRHONU_LOGA, SP_LPNU_LOGA, SP_A_TAU, SP_TAU_A, SP_XE_TAU, NSPL };
+constexpr double TABLE_MAGIC = 20231103.0;
+
+enum { ST_OK = 0, ST_MAX_STEPS = 1, ST_DT_UNDERFLOW = 2, ST_NONFINITE = 3, ST_BAD_INPUT = 4 };
+
+constexpr int LMAX_TABLE = 128;
+
+// ------------------------------------------------------------------ dual numbers
+// Forward-mode scalar for the a-column of the Jacobian (d f / d a).
+struct Dual {
+  double v, d;
+  HD Dual() : v(0), d(0) {}
+  HD Dual(double x) : v(x), d(0) {}
+  HD Dual(double x, double dx) : v(x), d(dx) {}
+};
+HD Dual operator+(Dual a, Dual b) { return Dual(a.v + b.v, a.d + b.d); }
+HD Dual operator-(Dual a, Dual b) { return Dual(a.v - b.v, a.d - b.d); }
+HD Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
+HD Dual operator*(Dual a, Dual b) { return Dual(a.v * b.v, a.d * b.v + a.v * b.d); }
+HD Dual operator/(Dual a, Dual b) { double r = 1.0 / b.v; double q = a.v * r; return Dual(a.v / b.v, (a.d - q * b.d) * r); }
+HD Dual operator+(Dual a, double b) { return Dual(a.v + b, a.d); }
+HD Dual operator+(double a, Dual b) { return Dual(a + b.v, b.d); }
+HD Dual operator-(Dual a, double b) { return Dual(a.v - b, a.d); }
+HD Dual operator-(double a, Dual b) { return Dual(a - b.v, -b.d); }
+HD Dual operator*(Dual a, double b) { return Dual(a.v * b, a.d * b); }
+HD Dual operator*(double a, Dual b) { return Dual(a * b.v, a * b.d); }
+HD Dual operator/(Dual a, double b) { return Dual(a.v / b, a.d / b); }
+HD Dual operator/(double a, Dual b) { double r = 1.0 / b.v; return Dual(a / b.v, -a * b.d * r * r); }
+HD Dual dexp(Dual a) { double e = exp(a.v); return Dual(e, e * a.d); }
+HD Dual dlog(Dual a) { return Dual(log(a.v), a.d / a.v); }
+HD Dual dsqrt(Dual a) { double s = sqrt(a.v); return Dual(s, 0.5 * a.d / s); }
+HD double dexp(double a) { return exp(a); }
+HD double dlog(double a) { return log(a); }
+HD double dsqrt(double a) { return sqrt(a); }
+HD double val(double x) { return x; }
+HD double val(Dual x) { return x.v; }
+HD double der(double) { return 0.0; }
+HD double der(Dual x) { return x.d; }
+template <class S> HD S make_var(double v);
+template <> HD double make_var<double>(double v) { return v; }
+template <> HD Dual make_var<Dual>(double v) { return Dual(v, 1.0); }
+template <class S> HD S mk(double v, double d);
+template <> HD double mk<double>(double v, double) { return v; }
+template <> HD Dual mk<Dual>(double v, double d) { return Dual(v, d); }
+
+// ------------------------------------------------------------------ tables
+struct Spl { const double *x, *y, *S; int n; };
+
+struct Cosmo {
+  const double* b;
+  Spl sp[NSPL];
+  const double *q, *w;
+  int nq;
+};
+
+HD bool load_cosmo(const double* b, int blob_len, Cosmo& c) {
+  if (LDG(b + H_MAGIC) != TABLE_MAGIC) return false;
+  c.b = b;
+  c.nq = (int)LDG(b + H_NQ);
+  const double* p = b + HDR_LEN;
+  long tot = HDR_LEN;
+  for (int s = 0; s < NSPL; ++s) {
+    int n = (int)LDG(b + H_NSPL0 + s);
+    if (n < 2) return false;
+    c.sp[s].n = n; c.sp[s].x = p; c.sp[s].y = p + n; c.sp[s].S = p + 2 * n;
+    p += 3 * n; tot += 3 * n;
+  }
+  c.q = p; c.w = p + c.nq;
+  tot += 2 * c.nq;
+  return tot <= blob_len && (int)LDG(b + H_BLOBLEN) == blob_len;
+}
+
+HD double hdr(const Cosmo& c, int i) { return LDG(c.b + i); }
+
+// left searchsorted clipped to [0, n-2] (spline_interpolation.py:143)
+HD int spl_locate(const Spl& s, double x) {
+  int lo = 0, hi = s.n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (LDG(s.x + mid) < x) lo = mid + 1; else hi = mid;
+  }
+  int i = lo - 1;
+  i = i < 0 ? 0 : i;
+  i = i > s.n - 2 ? s.n - 2 : i;
+  return i;
+}
+
+template <class S> HD S spl_eval(const Spl& s, S x) {
+  int i = spl_locate(s, val(x));
+  double x0 = LDG(s.x + i), x1 = LDG(s.x + i + 1);
+  double h = x1 - x0;
+  S t = (x - x0) / h;
+  S A = 1.0 - t;
+  S B = t;
+  return A * LDG(s.y + i) + B * LDG(s.y + i + 1) +
+         ((A * A * A - A) * LDG(s.S + i) + (B * B * B - B) * LDG(s.S + i + 1)) * (h * h) / 6.0;
+}
+
+// ------------------------------------------------------------------ dimensions
+struct Dims {
+  int lg, lgp, lr, lnu, nq, n;
+  int igp, ir, iq0;
+};
+
+HD Dims make_dims(int lg, int lgp, int lr, int lnu, int nq) {
+  Dims d;
+  d.lg = lg; d.lgp = lgp; d.lr = lr; d.lnu = lnu; d.nq = nq;
+  d.n = 7 + (lg + 1) + (lgp + 1) + (lr + 1) + nq * (lnu + 1) + 2;
+  d.igp = 8 + lg; d.ir = 9 + lg + lgp; d.iq0 = 10 + lg + lgp + lr;
+  return d;
+}
+
+// ------------------------------------------------------------------ workspace
+// Per-mode scratch: NV vectors of length n plus a MISC block.  Element e of a
+// mode's scratch lives at p[e * stride] (stride 32 interleaves the 32 modes
+// of a warp so that every access of the warp is one coalesced transaction).
+enum { V_Y = 0, V_Y1, V_U, V_F, V_JC0, V_LO, V_UP, V_PI, V_ZH, V_ZE, V_K0, NV = V_K0 + 8 };
+// MISC block offsets
+enum { M_CORE = 0,          // 8x8 core LU (row-major)           64
+       M_CPIV = 64,         // core pivots                         8
+       M_DE = 72,           // DE 2x2 LU + pivot flag              5
+       M_CINV = 77,         // Woodbury capacitance inverse        4
+       M_SCAL = 81,         // cached per-step scalars            24
+       M_Q = 105 };         // per-q arrays: v, dv/da, dlfdlq, ghq, geq, r1q, dTq  (7 nq)
+enum { Q_V = 0, Q_DV, Q_DLF, Q_GH, Q_GE, Q_R1, Q_DT, NQARR };
+enum { S_D = 0, S_W00I, S_ID, S_IDAH, S_GH2, S_GH3, S_GH5, S_GH7, S_GHR0, S_GHQE, S_GE4, S_GE6, S_GE8,
+       S_GER1, S_GEQE, S_R13, S_R15, S_R17, S_R1R0, S_R1QE, S_R1QT, S_DTT, S_DTP, S_DTR };
+HD int misc_len(int nq) { return M_Q + NQARR * nq; }
+HD long slot_len(const Dims& D, bool dense) {
+  long L = (long)NV * D.n + misc_len(D.nq);
+  if (dense) L += (long)D.n * D.n + D.n;
+  return L;
+}
+
+struct WS {
+  double* p;
+  int stride;
+  long n;
+  long misc0;
+  HD double& v(int vec, int j) const { return p[((long)vec * n + j) * stride]; }
+  HD double& m(int off) const { return p[(misc0 + off) * stride]; }
+  HD double& e(long off) const { return p[off * stride]; }
+};
+
+// ------------------------------------------------------------------ constants
+struct Tab { double lo[LMAX_TABLE + 2], up[LMAX_TABLE + 2]; };  // l/(2l+1), (l+1)/(2l+1)
+
+// Published transformed Rodas5 tableau (Hairer & Wanner), as listed in
+// ode_integrators_stiff.py:622-687: identical coefficients are required for
+// the reference's step sequence.
+struct Rodas {
+  double gamma;
+  double a[8][8];
+  double C[8][8];
+  double c[8];
+  double d[8];
+};
+
+// ------------------------------------------------------------------ scalars of the RHS at a given a
+template <class S> struct Bg {
+  S a, ia, ia2, a2, la, cs2, xe, rhonu, rhoQ, aH, iaH, wQ, ca2, opac, pb43;
+};
+
+struct ModeConst {
+  double k, k2, ik, ik2;
+  double Om, Ob, Oc, ODE, Ok, grhom, grhog, grhor, Neff, Nmnu, amnu, w0, wa, cs2Q, YHe, H0;
+  double akthom, pQ, photbar0;
+};
+
+HD void mode_const(const Cosmo& c, double k, ModeConst& m) {
+  m.k = k; m.k2 = k * k; m.ik = 1.0 / k; m.ik2 = 1.0 / (k * k);
+  m.Om = hdr(c, H_OMEGAM); m.Ob = hdr(c, H_OMEGAB); m.Oc = m.Om - m.Ob; m.ODE = hdr(c, H_OMEGADE);
+  m.Ok = hdr(c, H_OMEGAK); m.grhom = hdr(c, H_GRHOM); m.grhog = hdr(c, H_GRHOG); m.grhor = hdr(c, H_GRHOR);
+  m.Neff = hdr(c, H_NEFF); m.Nmnu = hdr(c, H_NMNU); m.amnu = hdr(c, H_AMNU); m.w0 = hdr(c, H_W0);
+  m.wa = hdr(c, H_WA); m.cs2Q = hdr(c, H_CS2DE); m.YHe = hdr(c, H_YHE); m.H0 = hdr(c, H_H0);
+  m.akthom = 2.3038921003709498e-9 * (1.0 - m.YHe) * m.Ob * m.H0 * m.H0;
+  m.pQ = -3.0 * (1.0 + m.w0 + m.wa);
+  m.photbar0 = m.grhog / (m.grhom * m.Ob);
+}
+
+template <class S>
+HD void background(const Cosmo& c, const ModeConst& m, S a, Bg<S>& g) {
+  g.a = a;
+  g.ia = 1.0 / a;
+  g.ia2 = g.ia * g.ia;
+  g.a2 = a * a;
+  g.la = dlog(a);
+  g.cs2 = spl_eval(c.sp[SP_CS2A_LOGA], g.la) * g.ia;
+  g.xe = spl_eval(c.sp[SP_XE_LOGA], g.la);
+  g.rhonu = dexp(spl_eval(c.sp[SP_LRHONU_LOGA], g.la));
+  // a^(-3(1+w0+wa)) exp(3(a-1) wa), background.py:111
+  g.rhoQ = dexp(m.pQ * g.la + 3.0 * (a - 1.0) * m.wa);
+  S grho = m.grhom * m.Om * g.ia + (m.grhog + m.grhor * (m.Neff + m.Nmnu * g.rhonu)) * g.ia2 +
+           m.grhom * m.ODE * g.rhoQ * g.a2 + m.grhom * m.Ok;
+  g.aH = dsqrt(grho / 3.0);
+  g.iaH = 1.0 / g.aH;
+  g.wQ = m.w0 + m.wa * (1.0 - a);
+  S wQp = -m.wa * g.aH * a;
+  g.ca2 = g.wQ - wQp / 3.0 / ((1.0 + g.wQ) + 1e-6) * g.iaH;
+  g.opac = g.xe * m.akthom * g.ia2;
+  g.pb43 = (4.0 / 3.0) * m.photbar0 * g.ia;
+}
+
+// conformal Hubble rate only (start time)
+HD double aprimeoa(const Cosmo& c, const ModeConst& m, double a) {
+  double la = log(a);
+  double rhonu = exp(spl_eval(c.sp[SP_LRHONU_LOGA], la));
+  double rhoQ = exp(m.pQ * la + 3.0 * (a - 1.0) * m.wa);
+  double grho = m.grhom * m.Om / a + (m.grhog + m.grhor * (m.Neff + m.Nmnu * rhonu)) / (a * a) +
+                m.grhom * m.ODE * rhoQ * a * a + m.grhom * m.Ok;
+  return sqrt(grho / 3.0);
+}
+
+// ------------------------------------------------------------------ RHS
+// f = model_synchronous(tau, y) (perturbations.py:84-371).  With S = Dual the
+// a-dependence is differentiated: vout receives f, vjc receives d f / d a.
+template <class S>
+HD void rhs(const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, double tau, const WS& w, int vin,
+            int vout, int vjc) {
+  const int n = D.n, nq = D.nq, iq0 = D.iq0, iq1 = iq0 + nq, iq2 = iq1 + nq, iq3 = iq2 + nq;
+  const int igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
+  const double k = m.k, k2 = m.k2;
+  const double itau = 1.0 / tau;
+  Bg<S> g;
+  background<S>(c, m, make_var<S>(w.v(vin, 0)), g);
+  auto Y = [&](int j) -> double { return w.v(vin, j); };
+  auto put = [&](int j, S f) {
+    w.v(vout, j) = val(f);
+    if (vjc >= 0) w.v(vjc, j) = der(f);
+  };
+  const double eta = Y(2), dc = Y(3), tc = Y(4), db = Y(5), tb = Y(6), dg = Y(7), tg = Y(8), y9 = Y(9);
+  const double dr = Y(ir), tr = Y(ir + 1), y_r2 = Y(ir + 2);
+  const double dq = Y(n - 2), tq = Y(n - 1);
+  // massive neutrino momentum sums (nu_perturb, perturbations.py:22-50)
+  S drhonu = 0.0, dpnu = 0.0, fnu = 0.0;
+  for (int i = 0; i < nq; ++i) {
+    const double amq = m.amnu / LDG(c.q + i);
+    S aq = g.a * amq;
+    S v = 1.0 / dsqrt(1.0 + aq * aq);
+    const double wq = LDG(c.w + i);
+    const double p0 = Y(iq0 + i);
+    drhonu = drhonu + wq * p0 / v;
+    dpnu = dpnu + wq * p0 * v;
+    fnu = fnu + wq * Y(iq1 + i);
+    w.m(M_Q + i) = val(v);                 // v_q and d v_q / d a for the element loop
+    if (vjc >= 0) w.m(M_Q + nq + i) = der(v);
+  }
+  dpnu = dpnu / 3.0;
+  S rptQ = (1.0 + g.wQ) * g.rhoQ * m.grhom * m.ODE * tq * g.a2;
+  S dgrho = m.grhom * (m.Oc * dc + m.Ob * db) * g.ia + (m.grhog * dg + m.grhor * (m.Neff * dr + m.Nmnu * drhonu)) * g.ia2 +
+            m.grhom * m.ODE * dq * g.rhoQ * g.a2;
+  S dgpres = (m.grhog * dg + m.grhor * m.Neff * dr) * g.ia2 / 3.0 + m.grhor * m.Nmnu * dpnu * g.ia2 +
+             (m.cs2Q * m.grhom * m.ODE * dq * g.rhoQ * g.a2 + (m.cs2Q - g.ca2) * (3.0 * g.aH * rptQ * m.ik2));
+  S dgtheta = m.grhom * (m.Oc * tc + m.Ob * tb) * g.ia + (4.0 / 3.0) * (m.grhog * tg + m.Neff * m.grhor * tr) * g.ia2 +
+              m.Nmnu * m.grhor * k * fnu * g.ia2 + rptQ;
+  S hp = (2.0 * k2 * eta + dgrho) * g.iaH;
+  S etap = 0.5 * dgtheta * m.ik2;
+  S alpha = (hp + 6.0 * etap) * 0.5 * m.ik2;
+  put(0, g.aH * g.a);
+  put(1, -(dgrho + 3.0 * dgpres) * g.a);
+  put(2, etap);
+  put(3, -tc - 0.5 * hp);
+  put(4, -g.aH * tc);
+  put(5, -tb - 0.5 * hp);
+  put(6, -g.aH * tb + k2 * g.cs2 * db + g.pb43 * g.opac * (tg - tb));
+  // photons, temperature (BLT11 2.4)
+  const double polter = y9 + Y(igp) + Y(igp + 2);
+  put(7, (4.0 / 3.0) * (-tg - 0.5 * hp));
+  put(8, k2 * (0.25 * dg - 0.5 * y9) - g.opac * (tg - tb));
+  put(9, (8.0 / 15.0) * (tg + k2 * alpha) - 0.6 * k * Y(10) - g.opac * (y9 - 0.1 * polter));
+  for (int l = 3; l < lg; ++l)
+    put(7 + l, k * (T.lo[l] * Y(6 + l) - T.up[l] * Y(8 + l)) - g.opac * Y(7 + l));
+  put(7 + lg, k * Y(6 + lg) - (lg + 1.0) * itau * Y(7 + lg) - g.opac * Y(7 + lg));
+  // photons, polarisation
+  put(igp, -k * Y(igp + 1) - g.opac * Y(igp) + g.opac * polter * 0.5);
+  put(igp + 1, k * (T.lo[1] * Y(igp) - T.up[1] * Y(igp + 2)) - g.opac * Y(igp + 1));
+  put(igp + 2, k * (T.lo[2] * Y(igp + 1) - T.up[2] * Y(igp + 3)) - g.opac * Y(igp + 2) + g.opac * polter * 0.1);
+  for (int l = 3; l < lgp; ++l)
+    put(igp + l, k * (T.lo[l] * Y(igp + l - 1) - T.up[l] * Y(igp + l + 1)) - g.opac * Y(igp + l));
+  put(igp + lgp, k * Y(igp + lgp - 1) - (lgp + 1.0) * itau * Y(igp + lgp) - g.opac * Y(igp + lgp));
+  // massless neutrinos
+  put(ir, (4.0 / 3.0) * (-tr - 0.5 * hp));
+  put(ir + 1, k2 * (0.25 * dr - 0.5 * y_r2));
+  put(ir + 2, (8.0 / 15.0) * (tr + k2 * alpha) - 0.6 * k * Y(ir + 3));
+  for (int l = 3; l < lr; ++l) w.v(vout, ir + l) = k * (T.lo[l] * Y(ir + l - 1) - T.up[l] * Y(ir + l + 1));
+  if (vjc >= 0) for (int l = 3; l < lr; ++l) w.v(vjc, ir + l) = 0.0;
+  put(ir + lr, S(k * Y(ir + lr - 1) - (lr + 1.0) * itau * Y(ir + lr)));
+  // massive neutrinos, l-major [l][q]
+  for (int i = 0; i < nq; ++i) {
+    S v = mk<S>(w.m(M_Q + i), vjc >= 0 ? w.m(M_Q + nq + i) : 0.0);
+    const double dlf = w.m(M_Q + 2 * nq + i);
+    S kv = k * v;
+    put(iq0 + i, -kv * Y(iq1 + i) + hp * dlf / 6.0);
+    put(iq1 + i, kv * (Y(iq0 + i) - 2.0 * Y(iq2 + i)) / 3.0);
+    put(iq2 + i, kv * (2.0 * Y(iq1 + i) - 3.0 * Y(iq3 + i)) / 5.0 - (hp / 15.0 + 0.4 * etap) * dlf);
+    for (int l = 3; l < lnu; ++l)
+      put(iq0 + l * nq + i, kv * (T.lo[l] * Y(iq0 + (l - 1) * nq + i) - T.up[l] * Y(iq0 + (l + 1) * nq + i)));
+    put(iq0 + lnu * nq + i, kv * Y(iq0 + (lnu - 1) * nq + i) - (lnu + 1.0) * itau * Y(iq0 + lnu * nq + i));
+  }
+  // dark-energy fluid (BL10 3.5, 3.6)
+  put(n - 2, -(1.0 + g.wQ) * (tq + 0.5 * hp) - 3.0 * (m.cs2Q - g.wQ) * g.aH * dq -
+                 9.0 * (1.0 + g.wQ) * (m.cs2Q - g.ca2) * g.aH * g.aH * m.ik2 * tq);
+  put(n - 1, -(1.0 - 3.0 * m.cs2Q) * g.aH * tq + m.cs2Q / (1.0 + g.wQ) * k2 * dq);
+}
+
+
+// ------------------------------------------------------------------ outputs
+// convert_to_output_variables (perturbations.py:374-523) of the state held in
+// vector vin; Friedmann aH from the tables, 20 fields to out[0..19*ostride].
+HD void outputs(const Cosmo& c, const ModeConst& m, const Dims& D, const WS& w, int vin, double* out, long ostride) {
+  const int nq = D.nq, iq0 = D.iq0, iq1 = iq0 + nq, n = D.n;
+  const double k = m.k, k2 = m.k2;
+  auto Y = [&](int j) -> double { return w.v(vin, j); };
+  const double a = Y(0), eta = Y(2), dc = Y(3), tc = Y(4), db = Y(5), tb = Y(6), dg = Y(7), tg = Y(8);
+  const double dr = Y(D.ir), tr = Y(D.ir + 1);
+  const double la = log(a);
+  const double rhonu = exp(spl_eval(c.sp[SP_LRHONU_LOGA], la));
+  const double pnu = exp(spl_eval(c.sp[SP_LPNU_LOGA], la));
+  double drhonu = 0.0, fnu = 0.0;
+  for (int i = 0; i < nq; ++i) {
+    const double aq = a * m.amnu / LDG(c.q + i);
+    const double v = 1.0 / sqrt(1.0 + aq * aq);
+    drhonu += LDG(c.w + i) * Y(iq0 + i) / v;
+    fnu += LDG(c.w + i) * Y(iq1 + i);
+  }
+  const double dnu = drhonu / rhonu, tnu = k * fnu / (rhonu + pnu);
+  const double dq = Y(n - 2), tq = Y(n - 1);
+  const double wQ = m.w0 + m.wa * (1.0 - a);
+  const double rhoQ = exp(m.pQ * la + 3.0 * (a - 1.0) * m.wa);
+  const double a2 = a * a;
+  const double rptQ = (1.0 + wQ) * rhoQ * m.grhom * m.ODE * tq * a2;
+  const double grho = m.grhom * m.Om / a + (m.grhog + m.grhor * (m.Neff + m.Nmnu * rhonu)) / a2 +
+                      m.grhom * m.ODE * rhoQ * a2 + m.grhom * m.Ok;
+  const double aH = sqrt(grho / 3.0);
+  const double dgrho = m.grhom * (m.Oc * dc + m.Ob * db) / a +
+                       (m.grhog * dg + m.grhor * (m.Neff * dr + m.Nmnu * drhonu)) / a2 + m.grhom * m.ODE * dq * rhoQ * a2;
+  const double dgtheta = m.grhom * (m.Oc * tc + m.Ob * tb) / a + 4.0 / 3.0 * (m.grhog * tg + m.Neff * m.grhor * tr) / a2 +
+                         m.Nmnu * m.grhor * k * fnu / a2 + rptQ;
+  const double hp = (2.0 * k2 * eta + dgrho) / aH;
+  const double etap = 0.5 * dgtheta / k2;
+  const double alpha = (hp + 6.0 * etap) / 2.0 / k2;
+  const double dm = (m.grhom * (m.Oc * dc + m.Ob * db) / a + (m.grhor * m.Nmnu * drhonu) / a2) /
+                    (m.grhom * m.Om / a + (m.grhor * m.Nmnu * rhonu) / a2);
+  double tm = (m.grhom * (m.Oc * tc + m.Ob * tb) / a + m.Nmnu * m.grhor * k * fnu / a2) /
+              (3.0 * (m.grhom * m.Om / a + m.grhor * m.Nmnu * rhonu / a2));
+  const double dbc = (m.grhom * (m.Oc * dc + m.Ob * db) / a) / (m.grhom * m.Om / a);
+  double tbc = (m.grhom * (m.Oc * tc + m.Ob * tb) / a) / (3.0 * (m.grhom * m.Om / a) / a2);
+  tm += alpha * k2;
+  tbc += alpha * k2;
+  const double r[20] = {eta, etap, hp, alpha, dm, tm / aH, dbc, tbc / aH, dc, tc / aH, db, tb / aH,
+                        dg, tg / aH, dr, tr / aH, dnu, tnu / aH, dq, tq / aH};
+  for (int i = 0; i < 20; ++i) out[i * ostride] = r[i];
+}
+
+// ------------------------------------------------------------------ initial conditions
+// adiabatic_ics_one_mode (perturbations.py:526-627), written into vector vout.
+HD void initial_conditions(const Cosmo& c, const ModeConst& m, const Dims& D, double tau, const WS& w, int vout) {
+  const int n = D.n, nq = D.nq, iq0 = D.iq0, iq1 = iq0 + nq, iq2 = iq1 + nq;
+  const double k = m.k;
+  for (int j = 0; j < n; ++j) w.v(vout, j) = 0.0;
+  const double a = spl_eval(c.sp[SP_A_TAU], tau);
+  const double rn = exp(spl_eval(c.sp[SP_LRHONU_LOGA], log(a)));
+  const double a4 = a * a * a * a;
+  const double rhom = m.grhom * m.Om / (a * a * a);
+  const double rhor = (m.grhog + m.grhor * (m.Neff + m.Nmnu * rn)) / a4;
+  const double rhonu = m.grhor * (m.Neff + m.Nmnu * rn) / a4;
+  const double fracb = m.Ob / m.Om, fracnu = rhonu / rhor;
+  const double om = a * rhom / sqrt(rhor);
+  const double ci = -1.0, s2 = 1.0;
+  const double kt = k * tau;
+  const double dg = -(kt * kt) / 3.0 * (1.0 - om * tau / 5.0) * ci * s2;
+  const double tg = -(kt * kt * kt) / tau / 36.0 *
+                    (1.0 - 3.0 * (1.0 + 5.0 * fracb - fracnu) / 20.0 / (1.0 - fracnu) * om * tau) * ci * s2;
+  const double dr = dg;
+  const double tr = -(kt * kt * kt * kt) / tau / 36.0 / (4.0 * fracnu + 15.0) *
+                    (4.0 * fracnu + 11.0 + 12.0 -
+                     3.0 * (8.0 * fracnu * fracnu + 50.0 * fracnu + 275.0) / 20.0 / (2.0 * fracnu + 15.0) * tau * om) * ci;
+  const double sr = (kt * kt) / (45.0 + 12.0 * fracnu) * (3.0 * s2 - 1.0) *
+                    (1.0 + (4.0 * fracnu - 5.0) / 4.0 / (2.0 * fracnu + 15.0) * tau * om) * ci;
+  const double wQ = m.w0 + m.wa * (1.0 - a);
+  const double dq = (kt * kt) / 4.0 * (1.0 + wQ) * (4.0 - 3.0 * m.cs2Q) / (4.0 - 6.0 * wQ + 3.0 * m.cs2Q) * ci * s2;
+  const double tq = (kt * kt * kt * kt) / tau / 4.0 * m.cs2Q / (4.0 - 6.0 * wQ + 3.0 * m.cs2Q) * ci * s2;
+  const double eta = ci * (1.0 - (kt * kt) / 12.0 / (15.0 + 4.0 * fracnu) *
+                                     (5.0 + 4.0 * s2 * fracnu -
+                                      (16.0 * fracnu * fracnu + 280.0 * fracnu + 325.0) / 10.0 / (2.0 * fracnu + 15.0) * tau * om));
+  w.v(vout, 0) = a; w.v(vout, 2) = eta; w.v(vout, 3) = 0.75 * dg;
+  w.v(vout, 5) = 0.75 * dg; w.v(vout, 6) = tg; w.v(vout, 7) = dg; w.v(vout, 8) = tg;
+  w.v(vout, D.ir) = dr; w.v(vout, D.ir + 1) = tr; w.v(vout, D.ir + 2) = sr * 2.0;
+  for (int i = 0; i < nq; ++i) {
+    const double q = LDG(c.q + i);
+    const double aq = a * m.amnu / q;
+    const double v = 1.0 / sqrt(1.0 + aq * aq);
+    const double dlf = -q / (1.0 + exp(-q));
+    w.v(vout, iq0 + i) = -0.25 * dlf * dr;
+    w.v(vout, iq1 + i) = -dlf * tr / v / k / 3.0;
+    w.v(vout, iq2 + i) = -0.5 * dlf * sr;
+    w.m(M_Q + Q_DLF * nq + i) = dlf;
+  }
+  w.v(vout, n - 2) = dq; w.v(vout, n - 1) = tq;
+}
+
+// determine_starting_time (perturbations.py:630-681) with root_find_bisect (util.py:365-396)
+HD double start_time(const Cosmo& c, const ModeConst& m) {
+  const double small_k = 0.0004, large_k = 0.07;
+  const double tau0 = hdr(c, H_TAUMIN);
+  const double tau1 = spl_eval(c.sp[SP_TAU_A], 0.1);
+  const double tau_k = 1.0 / m.k;
+  const double akthom_st = 2.3048e-9 * (1.0 - m.YHe) * m.Ob * m.H0 * m.H0;  // as perturbations.py:648
+  double lt[2];
+  for (int which = 0; which < 2; ++which) {
+    double xl = log(tau0), xr = log(tau1);
+    for (int it = 0; it < 7; ++it) {
+      const double xm = 0.5 * (xl + xr);
+      double fv[2];
+      for (int e = 0; e < 2; ++e) {
+        const double tau = exp(e == 0 ? xm : xl);
+        const double a = spl_eval(c.sp[SP_A_TAU], tau);
+        const double aH = aprimeoa(c, m, a);
+        if (which == 0) {
+          fv[e] = (1.0 / aH) / tau_k / large_k - 1.0;
+        } else {
+          const double xe = spl_eval(c.sp[SP_XE_TAU], tau);
+          const double opac = xe * akthom_st / (a * a);
+          fv[e] = (1.0 / opac) / (1.0 / aH) / small_k - 1.0;
+        }
+      }
+      if (fv[0] * fv[1] > 0.0) xl = xm; else xr = xm;
+    }
+    lt[which] = 0.5 * (xl + xr);
+  }
+  return exp(lt[1] < lt[0] ? lt[1] : lt[0]);
+}
+
+// ------------------------------------------------------------------ structured factorization
+// Chain coefficients of M = d I - B (see file header).  A chain is the list
+// of indices start, start+stride, ... ; LO[i] = M[i, prev], UP[i] = M[i, next].
+// Bottom-up elimination: p_last = M_ii, p_i = M_ii - UP_i LO_next / p_next,
+// PI = 1/p.  All chain pivots are >= d > 0: the products UP_i LO_next are
+// negative for every free-streaming hierarchy and the diagonal damping
+// (opacity, truncation (l+1)/tau) is non-negative.
+struct StepScal {
+  double d, dt, t0;
+};
+
+HD void chain_pivots(const WS& w, int start, int stride, int cnt, double d_last, double d_rest) {
+  int i = start + (cnt - 1) * stride;
+  double pinv = 1.0 / d_last;
+  w.v(V_PI, i) = pinv;
+  for (int j = cnt - 2; j >= 0; --j) {
+    const int ii = start + j * stride;
+    const double p = d_rest - w.v(V_UP, ii) * w.v(V_LO, ii + stride) * pinv;
+    pinv = 1.0 / p;
+    w.v(V_PI, ii) = pinv;
+  }
+}
+
+// small dense LU with partial pivoting in the MISC block (row-major, N <= 8)
+template <int N>
+HD void small_lu(const WS& w, int off, int pivoff) {
+  for (int kk = 0; kk < N; ++kk) {
+    int p = kk;
+    double mx = fabs(w.m(off + kk * N + kk));
+    for (int i = kk + 1; i < N; ++i) {
+      const double v = fabs(w.m(off + i * N + kk));
+      if (v > mx) { mx = v; p = i; }
+    }
+    w.m(pivoff + kk) = (double)p;
+    if (p != kk)
+      for (int j = 0; j < N; ++j) { double t = w.m(off + kk * N + j); w.m(off + kk * N + j) = w.m(off + p * N + j); w.m(off + p * N + j) = t; }
+    const double inv = 1.0 / w.m(off + kk * N + kk);
+    for (int i = kk + 1; i < N; ++i) {
+      const double l = w.m(off + i * N + kk) * inv;
+      w.m(off + i * N + kk) = l;
+      if (l != 0.0)
+        for (int j = kk + 1; j < N; ++j) w.m(off + i * N + j) -= l * w.m(off + kk * N + j);
+    }
+  }
+}
+
+template <int N>
+HD void small_solve(const WS& w, int off, int pivoff, double* r) {
+  for (int kk = 0; kk < N; ++kk) {
+    const int p = (int)w.m(pivoff + kk);
+    if (p != kk) { double t = r[kk]; r[kk] = r[p]; r[p] = t; }
+  }
+  for (int i = 1; i < N; ++i) { double s = r[i]; for (int j = 0; j < i; ++j) s -= w.m(off + i * N + j) * r[j]; r[i] = s; }
+  for (int i = N - 1; i >= 0; --i) { double s = r[i]; for (int j = i + 1; j < N; ++j) s -= w.m(off + i * N + j) * r[j]; r[i] = s / w.m(off + i * N + i); }
+}
+
+// Fill LO/UP for all chains, the core and DE blocks, and factor M.  Uses the
+// background at (t0, y0) in g; vq (v_q values) must be in MISC.
+HD void factor_M(const ModeConst& m, const Dims& D, const Tab& T, const WS& w, double d, double tau, const Bg<double>& g) {
+  const int nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
+  const double k = m.k, k2 = m.k2, itau = 1.0 / tau, op = g.opac;
+  // massless neutrinos r0..r_lr
+  w.v(V_UP, ir) = 4.0 / 3.0;
+  w.v(V_LO, ir + 1) = -0.25 * k2; w.v(V_UP, ir + 1) = 0.5 * k2;
+  w.v(V_LO, ir + 2) = -8.0 / 15.0; w.v(V_UP, ir + 2) = 0.6 * k;
+  for (int l = 3; l < lr; ++l) { w.v(V_LO, ir + l) = -k * T.lo[l]; w.v(V_UP, ir + l) = k * T.up[l]; }
+  w.v(V_LO, ir + lr) = -k;
+  chain_pivots(w, ir, 1, lr + 1, d + (lr + 1.0) * itau, d);
+  // massive neutrinos, chain q: iq0 + l*nq + q
+  for (int i = 0; i < nq; ++i) {
+    const double kv = k * w.m(M_Q + Q_V * nq + i);
+    for (int l = 0; l < lnu; ++l) {
+      const int e = iq0 + l * nq + i;
+      if (l > 0) w.v(V_LO, e) = -kv * T.lo[l];
+      w.v(V_UP, e) = kv * T.up[l];
+    }
+    w.v(V_LO, iq0 + lnu * nq + i) = -kv;
+    chain_pivots(w, iq0 + i, nq, lnu + 1, d + (lnu + 1.0) * itau, d);
+  }
+  // photon temperature tail T3..T_lg attached to T2 (index 9)
+  w.v(V_UP, 9) = 0.6 * k;
+  for (int l = 3; l < lg; ++l) { w.v(V_LO, 7 + l) = -k * T.lo[l]; w.v(V_UP, 7 + l) = k * T.up[l]; }
+  w.v(V_LO, 7 + lg) = -k;
+  chain_pivots(w, 10, 1, lg - 2, d + op + (lg + 1.0) * itau, d + op);
+  // photon polarisation tail P3..P_lgp attached to P2
+  w.v(V_UP, igp + 2) = 0.6 * k;
+  for (int l = 3; l < lgp; ++l) { w.v(V_LO, igp + l) = -k * T.lo[l]; w.v(V_UP, igp + l) = k * T.up[l]; }
+  w.v(V_LO, igp + lgp) = -k;
+  chain_pivots(w, igp + 3, 1, lgp - 2, d + op + (lgp + 1.0) * itau, d + op);
+  // 8x8 photon-baryon core: db, tb, dg, tg, T2, P0, P1, P2
+  for (int i = 0; i < 64; ++i) w.m(M_CORE + i) = 0.0;
+#define CM(r, c_) w.m(M_CORE + (r) * 8 + (c_))
+  CM(0, 0) = d; CM(0, 1) = 1.0;
+  CM(1, 0) = -k2 * g.cs2; CM(1, 1) = d + g.aH + g.pb43 * op; CM(1, 3) = -g.pb43 * op;
+  CM(2, 2) = d; CM(2, 3) = 4.0 / 3.0;
+  CM(3, 1) = -op; CM(3, 2) = -0.25 * k2; CM(3, 3) = d + op; CM(3, 4) = 0.5 * k2;
+  CM(4, 3) = -8.0 / 15.0; CM(4, 4) = d + 0.9 * op - w.v(V_UP, 9) * w.v(V_LO, 10) * w.v(V_PI, 10);
+  CM(4, 5) = -0.1 * op; CM(4, 7) = -0.1 * op;
+  CM(5, 4) = -0.5 * op; CM(5, 5) = d + 0.5 * op; CM(5, 6) = k; CM(5, 7) = -0.5 * op;
+  CM(6, 5) = -k * T.lo[1]; CM(6, 6) = d + op; CM(6, 7) = k * T.up[1];
+  CM(7, 4) = -0.1 * op; CM(7, 5) = -0.1 * op; CM(7, 6) = -k * T.lo[2];
+  CM(7, 7) = d + 0.9 * op - w.v(V_UP, igp + 2) * w.v(V_LO, igp + 3) * w.v(V_PI, igp + 3);
+#undef CM
+  small_lu<8>(w, M_CORE, M_CPIV);
+  // dark energy 2x2 (rows n-2, n-1)
+  const double wQ = g.wQ, cs2Q = m.cs2Q;
+  w.m(M_DE + 0) = d + 3.0 * (cs2Q - wQ) * g.aH;
+  w.m(M_DE + 1) = (1.0 + wQ) + 9.0 * (1.0 + wQ) * (cs2Q - g.ca2) * g.aH * g.aH * m.ik2;
+  w.m(M_DE + 2) = -cs2Q / (1.0 + wQ) * k2;
+  w.m(M_DE + 3) = d + (1.0 - 3.0 * cs2Q) * g.aH;
+  {
+    // LU with partial pivoting; M_DE+4 = 1 if rows swapped
+    double a00 = w.m(M_DE + 0), a01 = w.m(M_DE + 1), a10 = w.m(M_DE + 2), a11 = w.m(M_DE + 3);
+    double sw = 0.0;
+    if (fabs(a10) > fabs(a00)) { double t0_ = a00, t1_ = a01; a00 = a10; a01 = a11; a10 = t0_; a11 = t1_; sw = 1.0; }
+    const double l = a10 / a00;
+    w.m(M_DE + 0) = a00; w.m(M_DE + 1) = a01; w.m(M_DE + 2) = l; w.m(M_DE + 3) = a11 - l * a01; w.m(M_DE + 4) = sw;
+  }
+}
+
+// z = M^{-1} r on indices >= 2, in place on vector vr.
+HD void solve_M(const ModeConst& m, const Dims& D, const WS& w, double d, double aH, int vr) {
+  const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
+  const double id = 1.0 / d;
+  // eta
+  w.v(vr, 2) = w.v(vr, 2) * id;
+  // CDM: [[d, 1], [0, d + aH]]
+  {
+    const double z4 = w.v(vr, 4) / (d + aH);
+    w.v(vr, 4) = z4;
+    w.v(vr, 3) = (w.v(vr, 3) - z4) * id;
+  }
+  // DE
+  {
+    double r0 = w.v(vr, n - 2), r1 = w.v(vr, n - 1);
+    if (w.m(M_DE + 4) != 0.0) { double t = r0; r0 = r1; r1 = t; }
+    r1 -= w.m(M_DE + 2) * r0;
+    const double z1 = r1 / w.m(M_DE + 3);
+    const double z0 = (r0 - w.m(M_DE + 1) * z1) / w.m(M_DE + 0);
+    w.v(vr, n - 2) = z0; w.v(vr, n - 1) = z1;
+  }
+  // full chains: massless, massive
+  auto full_chain = [&](int start, int stride, int cnt) {
+    for (int j = cnt - 2; j >= 0; --j) {
+      const int i = start + j * stride;
+      w.v(vr, i) -= w.v(V_UP, i) * w.v(vr, i + stride) * w.v(V_PI, i + stride);
+    }
+    double z = w.v(vr, start) * w.v(V_PI, start);
+    w.v(vr, start) = z;
+    for (int j = 1; j < cnt; ++j) {
+      const int i = start + j * stride;
+      z = (w.v(vr, i) - w.v(V_LO, i) * z) * w.v(V_PI, i);
+      w.v(vr, i) = z;
+    }
+  };
+  full_chain(ir, 1, lr + 1);
+  for (int i = 0; i < nq; ++i) full_chain(iq0 + i, nq, lnu + 1);
+  // tails: forward sweep up to the attach point
+  auto tail_fwd = [&](int start, int cnt, int attach) {
+    for (int j = cnt - 2; j >= 0; --j) {
+      const int i = start + j;
+      w.v(vr, i) -= w.v(V_UP, i) * w.v(vr, i + 1) * w.v(V_PI, i + 1);
+    }
+    w.v(vr, attach) -= w.v(V_UP, attach) * w.v(vr, start) * w.v(V_PI, start);
+  };
+  auto tail_back = [&](int start, int cnt, int attach) {
+    double z = w.v(vr, attach);
+    for (int j = 0; j < cnt; ++j) {
+      const int i = start + j;
+      z = (w.v(vr, i) - w.v(V_LO, i) * z) * w.v(V_PI, i);
+      w.v(vr, i) = z;
+    }
+  };
+  tail_fwd(10, lg - 2, 9);
+  tail_fwd(igp + 3, lgp - 2, igp + 2);
+  double r[8] = {w.v(vr, 5), w.v(vr, 6), w.v(vr, 7), w.v(vr, 8), w.v(vr, 9), w.v(vr, igp), w.v(vr, igp + 1), w.v(vr, igp + 2)};
+  small_solve<8>(w, M_CORE, M_CPIV, r);
+  w.v(vr, 5) = r[0]; w.v(vr, 6) = r[1]; w.v(vr, 7) = r[2]; w.v(vr, 8) = r[3]; w.v(vr, 9) = r[4];
+  w.v(vr, igp) = r[5]; w.v(vr, igp + 1) = r[6]; w.v(vr, igp + 2) = r[7];
+  tail_back(10, lg - 2, 9);
+  tail_back(igp + 3, lgp - 2, igp + 2);
+}
+
+// g_h . v and g_e . v (the metric functionals h', eta' as rows)
+HD void functionals(const Dims& D, const WS& w, int vr, double& sh, double& se) {
+  const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
+  double h = w.m(M_SCAL + S_GH2) * w.v(vr, 2) + w.m(M_SCAL + S_GH3) * w.v(vr, 3) + w.m(M_SCAL + S_GH5) * w.v(vr, 5) +
+             w.m(M_SCAL + S_GH7) * w.v(vr, 7) + w.m(M_SCAL + S_GHR0) * w.v(vr, ir) + w.m(M_SCAL + S_GHQE) * w.v(vr, n - 2);
+  double e = w.m(M_SCAL + S_GE4) * w.v(vr, 4) + w.m(M_SCAL + S_GE6) * w.v(vr, 6) + w.m(M_SCAL + S_GE8) * w.v(vr, 8) +
+             w.m(M_SCAL + S_GER1) * w.v(vr, ir + 1) + w.m(M_SCAL + S_GEQE) * w.v(vr, n - 1);
+  for (int i = 0; i < nq; ++i) {
+    h += w.m(M_Q + Q_GH * nq + i) * w.v(vr, iq0 + i);
+    e += w.m(M_Q + Q_GE * nq + i) * w.v(vr, iq0 + nq + i);
+  }
+  sh = h; se = e;
+}
+
+// Per-step factorization of W = d I - J at (t0, y0).  Needs: JC0 (d f/d a),
+// background g at a0, v_q in MISC.  Writes LO/UP/PI, core/DE LU, ZH, ZE,
+// capacitance inverse and the sparse row-1 / functional coefficients.
+HD void factor_W(const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, const WS& w, double d, double tau, const Bg<double>& g) {
+  const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
+  const double a = g.a;
+  w.m(M_SCAL + S_D) = d;
+  w.m(M_SCAL + S_W00I) = 1.0 / (d - w.v(V_JC0, 0));
+  factor_M(m, D, T, w, d, tau, g);
+  // functional coefficients (d h'/d y and d eta'/d y)
+  const double iaH = g.iaH;
+  w.m(M_SCAL + S_GH2) = 2.0 * m.k2 * iaH;
+  w.m(M_SCAL + S_GH3) = m.grhom * m.Oc * g.ia * iaH;
+  w.m(M_SCAL + S_GH5) = m.grhom * m.Ob * g.ia * iaH;
+  w.m(M_SCAL + S_GH7) = m.grhog * g.ia2 * iaH;
+  w.m(M_SCAL + S_GHR0) = m.grhor * m.Neff * g.ia2 * iaH;
+  w.m(M_SCAL + S_GHQE) = m.grhom * m.ODE * g.rhoQ * g.a2 * iaH;
+  const double h2 = 0.5 * m.ik2;
+  w.m(M_SCAL + S_GE4) = m.grhom * m.Oc * g.ia * h2;
+  w.m(M_SCAL + S_GE6) = m.grhom * m.Ob * g.ia * h2;
+  w.m(M_SCAL + S_GE8) = (4.0 / 3.0) * m.grhog * g.ia2 * h2;
+  w.m(M_SCAL + S_GER1) = (4.0 / 3.0) * m.Neff * m.grhor * g.ia2 * h2;
+  w.m(M_SCAL + S_GEQE) = (1.0 + g.wQ) * g.rhoQ * m.grhom * m.ODE * g.a2 * h2;
+  // row 1: J[1, j] = -a (d dgrho/d y_j + 3 d dgpres/d y_j)
+  w.m(M_SCAL + S_R13) = -m.grhom * m.Oc;
+  w.m(M_SCAL + S_R15) = -m.grhom * m.Ob;
+  w.m(M_SCAL + S_R17) = -2.0 * m.grhog * g.ia;
+  w.m(M_SCAL + S_R1R0) = -2.0 * m.grhor * m.Neff * g.ia;
+  w.m(M_SCAL + S_R1QE) = -m.grhom * m.ODE * g.rhoQ * g.a2 * a * (1.0 + 3.0 * m.cs2Q);
+  w.m(M_SCAL + S_R1QT) = -9.0 * (m.cs2Q - g.ca2) * g.aH * (1.0 + g.wQ) * g.rhoQ * m.grhom * m.ODE * g.a2 * a * m.ik2;
+  for (int i = 0; i < nq; ++i) {
+    const double v = w.m(M_Q + Q_V * nq + i);
+    const double wq = LDG(c.w + i);
+    w.m(M_Q + Q_GH * nq + i) = m.grhor * m.Nmnu * wq / v * g.ia2 * iaH;
+    w.m(M_Q + Q_GE * nq + i) = m.Nmnu * m.grhor * m.k * wq * g.ia2 * h2;
+    w.m(M_Q + Q_R1 * nq + i) = -m.grhor * m.Nmnu * wq * (1.0 / v + v) * g.ia;
+  }
+  // u_h into ZH, u_e into ZE (sparse), then M^{-1}
+  for (int j = 0; j < n; ++j) { w.v(V_ZH, j) = 0.0; w.v(V_ZE, j) = 0.0; }
+  w.v(V_ZH, 3) = -0.5; w.v(V_ZH, 5) = -0.5; w.v(V_ZH, 7) = -2.0 / 3.0; w.v(V_ZH, 9) = 4.0 / 15.0;
+  w.v(V_ZH, ir) = -2.0 / 3.0; w.v(V_ZH, ir + 2) = 4.0 / 15.0; w.v(V_ZH, n - 2) = -0.5 * (1.0 + g.wQ);
+  w.v(V_ZE, 2) = 1.0; w.v(V_ZE, 9) = 1.6; w.v(V_ZE, ir + 2) = 1.6;
+  for (int i = 0; i < nq; ++i) {
+    const double dlf = w.m(M_Q + Q_DLF * nq + i);
+    w.v(V_ZH, iq0 + i) = dlf / 6.0;
+    w.v(V_ZH, iq0 + 2 * nq + i) = -dlf / 15.0;
+    w.v(V_ZE, iq0 + 2 * nq + i) = -0.4 * dlf;
+  }
+  solve_M(m, D, w, d, g.aH, V_ZH);
+  solve_M(m, D, w, d, g.aH, V_ZE);
+  double hh, eh, he, ee;
+  functionals(D, w, V_ZH, hh, eh);
+  functionals(D, w, V_ZE, he, ee);
+  // C = I - G^T Z = [[1 - hh, -he], [-eh, 1 - ee]]
+  const double c00 = 1.0 - hh, c01 = -he, c10 = -eh, c11 = 1.0 - ee;
+  const double idet = 1.0 / (c00 * c11 - c01 * c10);
+  w.m(M_CINV + 0) = c11 * idet; w.m(M_CINV + 1) = -c01 * idet;
+  w.m(M_CINV + 2) = -c10 * idet; w.m(M_CINV + 3) = c00 * idet;
+}
+
+// x = W^{-1} b in place on vector vb.
+HD void solve_W(const ModeConst& m, const Dims& D, const WS& w, double aH, int vb) {
+  const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
+  const double d = w.m(M_SCAL + S_D);
+  const double x0 = w.v(vb, 0) * w.m(M_SCAL + S_W00I);
+  w.v(vb, 0) = x0;
+  for (int j = 1; j < n; ++j) w.v(vb, j) += w.v(V_JC0, j) * x0;
+  solve_M(m, D, w, d, aH, vb);
+  double sh, se;
+  functionals(D, w, vb, sh, se);
+  const double th = w.m(M_CINV + 0) * sh + w.m(M_CINV + 1) * se;
+  const double te = w.m(M_CINV + 2) * sh + w.m(M_CINV + 3) * se;
+  for (int j = 2; j < n; ++j) w.v(vb, j) += w.v(V_ZH, j) * th + w.v(V_ZE, j) * te;
+  double s1 = w.v(vb, 1) + w.m(M_SCAL + S_R13) * w.v(vb, 3) + w.m(M_SCAL + S_R15) * w.v(vb, 5) +
+              w.m(M_SCAL + S_R17) * w.v(vb, 7) + w.m(M_SCAL + S_R1R0) * w.v(vb, ir) +
+              w.m(M_SCAL + S_R1QE) * w.v(vb, n - 2) + w.m(M_SCAL + S_R1QT) * w.v(vb, n - 1);
+  for (int i = 0; i < nq; ++i) s1 += w.m(M_Q + Q_R1 * nq + i) * w.v(vb, iq0 + i);
+  w.v(vb, 1) = s1 / d;
+}
+
+// ------------------------------------------------------------------ dense reference-method path
+// W = d I - J assembled densely from the same pieces and factored by LU with
+// partial pivoting, like the reference's lu_factor / lu_solve
+// (ode_integrators_stiff.py:774-776, 783).  Kept for validation and as the
+// "plain" method; O(n^3) per step.
+HD long dense_off(const Dims& D) { return (long)NV * D.n + misc_len(D.nq); }
+
+template <class F>
+HD void visit_u(const Dims& D, const WS& w, double wQ, F f) {
+  const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
+  f(3, -0.5, 0.0); f(5, -0.5, 0.0); f(7, -2.0 / 3.0, 0.0); f(9, 4.0 / 15.0, 1.6);
+  f(ir, -2.0 / 3.0, 0.0); f(ir + 2, 4.0 / 15.0, 1.6); f(n - 2, -0.5 * (1.0 + wQ), 0.0); f(2, 0.0, 1.0);
+  for (int i = 0; i < nq; ++i) {
+    const double dlf = w.m(M_Q + Q_DLF * nq + i);
+    f(iq0 + i, dlf / 6.0, 0.0);
+    f(iq0 + 2 * nq + i, -dlf / 15.0, -0.4 * dlf);
+  }
+}
+
+template <class F>
+HD void visit_g(const Dims& D, const WS& w, F f) {
+  const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
+  f(2, w.m(M_SCAL + S_GH2), 0.0); f(3, w.m(M_SCAL + S_GH3), 0.0); f(5, w.m(M_SCAL + S_GH5), 0.0);
+  f(7, w.m(M_SCAL + S_GH7), 0.0); f(ir, w.m(M_SCAL + S_GHR0), 0.0); f(n - 2, w.m(M_SCAL + S_GHQE), 0.0);
+  f(4, 0.0, w.m(M_SCAL + S_GE4)); f(6, 0.0, w.m(M_SCAL + S_GE6)); f(8, 0.0, w.m(M_SCAL + S_GE8));
+  f(ir + 1, 0.0, w.m(M_SCAL + S_GER1)); f(n - 1, 0.0, w.m(M_SCAL + S_GEQE));
+  for (int i = 0; i < nq; ++i) {
+    f(iq0 + i, w.m(M_Q + Q_GH * nq + i), 0.0);
+    f(iq0 + nq + i, 0.0, w.m(M_Q + Q_GE * nq + i));
+  }
+}
+
+// Assemble and factor the dense W.  Must run after factor_W (which fills the
+// chain coefficients and functional/row-1 coefficients) and before the core /
+// DE LU overwrite -- so factor_W calls it between factor_M's fills and LU.
+HD void dense_assemble(const ModeConst& m, const Dims& D, const Tab& T, const WS& w, double d, double tau,
+                       const Bg<double>& g, const double* core, const double* de) {
+  const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
+  const long A0 = dense_off(D);
+  auto A = [&](int i, int j) -> double& { return w.e(A0 + (long)i * n + j); };
+  const double itau = 1.0 / tau, op = g.opac;
+  for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) A(i, j) = (i == j) ? d : 0.0;
+  for (int i = 0; i < n; ++i) A(i, 0) -= w.v(V_JC0, i);
+  // CDM, eta
+  A(3, 4) = 1.0; A(4, 4) = d + g.aH;
+  // chains: off-diagonals from LO/UP (M entries), diagonal damping
+  auto chain = [&](int start, int stride, int cnt, double damp, double damp_last, bool attach) {
+    for (int j = 0; j < cnt; ++j) {
+      const int i = start + j * stride;
+      if (j > 0 || attach) A(i, i - stride) = w.v(V_LO, i);
+      if (j < cnt - 1) A(i, i + stride) = w.v(V_UP, i);
+      A(i, i) = d + (j == cnt - 1 ? damp_last : damp);
+    }
+  };
+  chain(ir, 1, lr + 1, 0.0, (lr + 1.0) * itau, false);
+  for (int i = 0; i < nq; ++i) chain(iq0 + i, nq, lnu + 1, 0.0, (lnu + 1.0) * itau, false);
+  chain(10, 1, lg - 2, op, op + (lg + 1.0) * itau, true);
+  chain(igp + 3, 1, lgp - 2, op, op + (lgp + 1.0) * itau, true);
+  A(9, 10) = w.v(V_UP, 9);
+  A(igp + 2, igp + 3) = w.v(V_UP, igp + 2);
+  const int cidx[8] = {5, 6, 7, 8, 9, igp, igp + 1, igp + 2};
+  for (int r = 0; r < 8; ++r) for (int cc = 0; cc < 8; ++cc) A(cidx[r], cidx[cc]) = core[r * 8 + cc];
+  A(n - 2, n - 2) = de[0]; A(n - 2, n - 1) = de[1]; A(n - 1, n - 2) = de[2]; A(n - 1, n - 1) = de[3];
+  // rank-2 metric coupling
+  visit_u(D, w, g.wQ, [&](int i, double uh, double ue) {
+    visit_g(D, w, [&](int j, double gh, double ge) { A(i, j) -= uh * gh + ue * ge; });
+  });
+  // row 1
+  for (int j = 1; j < n; ++j) A(1, j) = (j == 1) ? d : 0.0;
+  A(1, 0) = -w.v(V_JC0, 1);
+  A(1, 3) = -w.m(M_SCAL + S_R13); A(1, 5) = -w.m(M_SCAL + S_R15); A(1, 7) = -w.m(M_SCAL + S_R17);
+  A(1, ir) = -w.m(M_SCAL + S_R1R0); A(1, n - 2) = -w.m(M_SCAL + S_R1QE); A(1, n - 1) = -w.m(M_SCAL + S_R1QT);
+  for (int i = 0; i < nq; ++i) A(1, iq0 + i) = -w.m(M_Q + Q_R1 * nq + i);
+  // LU with partial pivoting (first maximal |pivot|)
+  const long P0 = A0 + (long)n * n;
+  for (int kk = 0; kk < n; ++kk) {
+    int p = kk;
+    double mx = fabs(A(kk, kk));
+    for (int i = kk + 1; i < n; ++i) { const double v = fabs(A(i, kk)); if (v > mx) { mx = v; p = i; } }
+    w.e(P0 + kk) = (double)p;
+    if (p != kk) for (int j = 0; j < n; ++j) { const double t = A(kk, j); A(kk, j) = A(p, j); A(p, j) = t; }
+    const double inv = 1.0 / A(kk, kk);
+    for (int i = kk + 1; i < n; ++i) {
+      const double l = A(i, kk) * inv;
+      A(i, kk) = l;
+      if (l != 0.0) for (int j = kk + 1; j < n; ++j) A(i, j) -= l * A(kk, j);
+    }
+  }
+}
+
+HD void dense_solve(const Dims& D, const WS& w, int vb) {
+  const int n = D.n;
+  const long A0 = dense_off(D), P0 = A0 + (long)n * n;
+  auto A = [&](int i, int j) -> double { return w.e(A0 + (long)i * n + j); };
+  for (int kk = 0; kk < n; ++kk) {
+    const int p = (int)w.e(P0 + kk);
+    if (p != kk) { const double t = w.v(vb, kk); w.v(vb, kk) = w.v(vb, p); w.v(vb, p) = t; }
+  }
+  for (int i = 1; i < n; ++i) { double s = w.v(vb, i); for (int j = 0; j < i; ++j) s -= A(i, j) * w.v(vb, j); w.v(vb, i) = s; }
+  for (int i = n - 1; i >= 0; --i) { double s = w.v(vb, i); for (int j = i + 1; j < n; ++j) s -= A(i, j) * w.v(vb, j); w.v(vb, i) = s / A(i, i); }
+}
+
+// ------------------------------------------------------------------ controller + step
+struct Ctl {
+  double rtol, atol, b1, b2, b3, safety, fmin, fmax;
+  int max_steps, hist_on_reject, dense, return_full, nout;
+};
+
+struct Run {
+  double t0, t1, T1, prev_inv, prev_prev_inv;
+  int vy, vy1, steps, acc, rej, status;
+};
+
+// start a mode: start time, ICs, first step size (perturbations.py:742-756)
+HD void mode_begin(const Cosmo& c, const ModeConst& m, const Dims& D, const Ctl& ctl, const WS& w, const double* tau_out,
+                   Run& r) {
+  double tmax = LDG(tau_out), tmin = tmax;
+  for (int o = 1; o < ctl.nout; ++o) { const double t = LDG(tau_out + o); tmax = t > tmax ? t : tmax; tmin = t < tmin ? t : tmin; }
+  const double ts = start_time(c, m);
+  const double t0 = 0.99 * (tmin < ts ? tmin : ts);
+  initial_conditions(c, m, D, t0, w, V_Y);
+  r.t0 = t0; r.T1 = tmax;
+  const double dt0 = (t0 / 4.0 < 0.5 * (tmax - t0)) ? t0 / 4.0 : 0.5 * (tmax - t0);
+  r.t1 = t0 + dt0 < tmax ? t0 + dt0 : tmax;
+  r.prev_inv = 1.0; r.prev_prev_inv = 1.0;
+  r.vy = V_Y; r.vy1 = V_Y1; r.steps = 0; r.acc = 0; r.rej = 0; r.status = ST_OK;
+}
+
+// One attempted Rodas5 step (ode_integrators_stiff.py:718-834) plus the PID
+// decision.  Returns true while the mode still needs steps.
+HD bool mode_step(const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, const Rodas& R, const Ctl& ctl,
+                  const WS& w, const double* tau_out, double* yout, long ostride, Run& r) {
+  if (!(r.t0 < r.T1)) return false;
+  if (r.steps >= ctl.max_steps) { r.status = ST_MAX_STEPS; return false; }
+  const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
+  const double t0 = r.t0, dt = r.t1 - r.t0;
+  const int vy = r.vy;
+  // f(t0, y0) and d f / d a in one forward-mode pass
+  rhs<Dual>(c, m, D, T, t0, w, vy, V_F, V_JC0);
+  Bg<double> g;
+  background<double>(c, m, w.v(vy, 0), g);
+  const double d = 1.0 / (dt * R.gamma);
+  factor_W(c, m, D, T, w, d, t0, g);
+  if (ctl.dense) {
+    // rebuild the core and DE blocks of M (factor_W overwrote them with LU factors)
+    double core[64], de[4];
+    {
+      const double k = m.k, k2 = m.k2, op = g.opac;
+      for (int i = 0; i < 64; ++i) core[i] = 0.0;
+      core[0] = d; core[1] = 1.0;
+      core[8] = -k2 * g.cs2; core[9] = d + g.aH + g.pb43 * op; core[11] = -g.pb43 * op;
+      core[18] = d; core[19] = 4.0 / 3.0;
+      core[25] = -op; core[26] = -0.25 * k2; core[27] = d + op; core[28] = 0.5 * k2;
+      core[35] = -8.0 / 15.0; core[36] = d + 0.9 * op; core[37] = -0.1 * op; core[39] = -0.1 * op;
+      core[44] = -0.5 * op; core[45] = d + 0.5 * op; core[46] = k; core[47] = -0.5 * op;
+      core[53] = -k * T.lo[1]; core[54] = d + op; core[55] = k * T.up[1];
+      core[60] = -0.1 * op; core[61] = -0.1 * op; core[62] = -k * T.lo[2]; core[63] = d + 0.9 * op;
+      de[0] = d + 3.0 * (m.cs2Q - g.wQ) * g.aH;
+      de[1] = (1.0 + g.wQ) + 9.0 * (1.0 + g.wQ) * (m.cs2Q - g.ca2) * g.aH * g.aH * m.ik2;
+      de[2] = -m.cs2Q / (1.0 + g.wQ) * k2;
+      de[3] = d + (1.0 - 3.0 * m.cs2Q) * g.aH;
+    }
+    dense_assemble(m, D, T, w, d, t0, g, core, de);
+  }
+  // d f / d tau: only the (l+1)/tau truncation terms
+  const double it2 = 1.0 / (t0 * t0);
+  const double dTT = (lg + 1.0) * it2 * w.v(vy, 7 + lg);
+  const double dTP = (lgp + 1.0) * it2 * w.v(vy, igp + lgp);
+  const double dTR = (lr + 1.0) * it2 * w.v(vy, ir + lr);
+  for (int i = 0; i < nq; ++i) w.m(M_Q + Q_DT * nq + i) = (lnu + 1.0) * it2 * w.v(vy, iq0 + lnu * nq + i);
+  const double idt = 1.0 / dt;
+  for (int s = 0; s < 8; ++s) {
+    const int vk = V_K0 + s;
+    if (s > 0) {
+      if (s <= 5) {
+        for (int j = 0; j < n; ++j) {
+          double acc = w.v(vy, j);
+          for (int q = 0; q < s; ++q) acc += R.a[s][q] * w.v(V_K0 + q, j);
+          w.v(V_U, j) = acc;
+        }
+      } else {
+        for (int j = 0; j < n; ++j) w.v(V_U, j) += w.v(V_K0 + s - 1, j);
+      }
+      rhs<double>(c, m, D, T, t0 + R.c[s] * dt, w, V_U, V_F, -1);
+    }
+    for (int j = 0; j < n; ++j) {
+      double acc = w.v(V_F, j);
+      for (int q = 0; q < s; ++q) acc += (R.C[s][q] * idt) * w.v(V_K0 + q, j);
+      w.v(vk, j) = acc;
+    }
+    if (s <= 4) {
+      const double dd = dt * R.d[s];
+      w.v(vk, 7 + lg) += dd * dTT;
+      w.v(vk, igp + lgp) += dd * dTP;
+      w.v(vk, ir + lr) += dd * dTR;
+      for (int i = 0; i < nq; ++i) w.v(vk, iq0 + lnu * nq + i) += dd * w.m(M_Q + Q_DT * nq + i);
+    }
+    if (ctl.dense) dense_solve(D, w, vk);
+    else solve_W(m, D, w, g.aH, vk);
+  }
+  // y1 = u + k8 ; error estimate k8
+  const int vy1 = r.vy1, vk8 = V_K0 + 7;
+  bool bad = false;
+  for (int j = 0; j < n; ++j) {
+    const double v = w.v(V_U, j) + w.v(vk8, j);
+    w.v(vy1, j) = v;
+    bad = bad || !isfinite_(v);
+  }
+  const int eidx[6] = {0, 2, 3, 5, 6, 7};
+  const double ew[6] = {1.0, m.k2, 1.0, 1.0, m.ik2, 1.0};
+  double ss = 0.0;
+  for (int q = 0; q < 6; ++q) {
+    const int j = eidx[q];
+    const double y0 = fabs(w.v(vy, j));
+    const double y1 = bad ? y0 : fabs(w.v(vy1, j));
+    const double sc = w.v(vk8, j) / (ctl.atol + (y0 > y1 ? y0 : y1) * ctl.rtol) * ew[q];
+    ss += sc * sc;
+  }
+  const double err = sqrt(ss / 6.0);
+  ++r.steps;
+  if (!isfinite_(err)) { r.status = ST_NONFINITE; return false; }
+  const bool keep = err < 1.0;
+  double inv = 1.0 / err;
+  const double f1 = ctl.b1 == 0.0 ? 1.0 : pow(inv, ctl.b1);
+  const double f2 = ctl.b2 == 0.0 ? 1.0 : pow(r.prev_inv, ctl.b2);
+  const double f3 = ctl.b3 == 0.0 ? 1.0 : pow(r.prev_prev_inv, ctl.b3);
+  double factor = ctl.safety * f1 * f2 * f3;
+  const double fmin = keep ? 1.0 : ctl.fmin;
+  factor = factor < fmin ? fmin : factor;
+  factor = factor > ctl.fmax ? ctl.fmax : factor;
+  const double dtn = dt * factor;
+  if (inv == 0.0 || !isfinite_(inv)) inv = 1.0;
+  if (keep) {
+    ++r.acc;
+    // SaveAt(ts) with LocalLinearInterpolation between (t0, y0) and (t1, y1)
+    for (int o = 0; o < ctl.nout; ++o) {
+      const double tt = LDG(tau_out + o);
+      if (tt > r.t0 && tt <= r.t1) {
+        const double cf = (tt - r.t0) / (r.t1 - r.t0);
+        double* dst = yout + (long)o * (ctl.return_full ? n : 20) * ostride;
+        if (ctl.return_full) {
+          for (int j = 0; j < n; ++j) { const double y0 = w.v(vy, j); dst[(long)j * ostride] = y0 + cf * (w.v(vy1, j) - y0); }
+        } else {
+          for (int j = 0; j < n; ++j) { const double y0 = w.v(vy, j); w.v(V_U, j) = y0 + cf * (w.v(vy1, j) - y0); }
+          outputs(c, m, D, w, V_U, dst, ostride);
+        }
+      }
+    }
+    r.vy = vy1; r.vy1 = vy;
+    r.t0 = r.t1;
+    r.prev_prev_inv = r.prev_inv;
+    r.prev_inv = inv;
+  } else {
+    ++r.rej;
+    if (ctl.hist_on_reject) { r.prev_prev_inv = r.prev_inv; r.prev_inv = inv; }
+  }
+  double tn = r.t0 + dtn;
+  if (tn > r.T1 - 1e-10) tn = r.T1;
+  if (!(tn > r.t0) && r.t0 < r.T1) { r.status = ST_DT_UNDERFLOW; return false; }
+  r.t1 = tn;
+  return r.t0 < r.T1;
+}
+
+HD void fill_tables(Tab& T) {
+  for (int l = 0; l < LMAX_TABLE + 2; ++l) { T.lo[l] = (double)l / (2.0 * l + 1.0); T.up[l] = (l + 1.0) / (2.0 * l + 1.0); }
+}
+
+HD void fill_rodas(Rodas& R) {
+  for (int i = 0; i < 8; ++i) for (int j = 0; j < 8; ++j) { R.a[i][j] = 0.0; R.C[i][j] = 0.0; }
+  R.gamma = 0.19;
+  R.a[1][0] = 2.0;
+  R.a[2][0] = 3.040894194418781; R.a[2][1] = 1.041747909077569;
+  R.a[3][0] = 2.576417536461461; R.a[3][1] = 1.622083060776640; R.a[3][2] = -0.9089668560264532;
+  R.a[4][0] = 2.760842080225597; R.a[4][1] = 1.446624659844071; R.a[4][2] = -0.3036980084553738; R.a[4][3] = 0.2877498600325443;
+  R.a[5][0] = -14.09640773051259; R.a[5][1] = 6.925207756232704; R.a[5][2] = -41.47510893210728;
+  R.a[5][3] = 2.343771018586405; R.a[5][4] = 24.13215229196062;
+  R.C[1][0] = -10.31323885133993;
+  R.C[2][0] = -21.04823117650003; R.C[2][1] = -7.234992135176716;
+  R.C[3][0] = 32.22751541853323; R.C[3][1] = -4.943732386540191; R.C[3][2] = 19.44922031041879;
+  R.C[4][0] = -20.69865579590063; R.C[4][1] = -8.816374604402768; R.C[4][2] = 1.260436877740897; R.C[4][3] = -0.7495647613787146;
+  R.C[5][0] = -46.22004352711257; R.C[5][1] = -17.49534862857472; R.C[5][2] = -289.6389582892057;
+  R.C[5][3] = 93.60855400400906; R.C[5][4] = 318.3822534212147;
+  R.C[6][0] = 34.20013733472935; R.C[6][1] = -14.15535402717690; R.C[6][2] = 57.82335640988400;
+  R.C[6][3] = 25.83362985412365; R.C[6][4] = 1.408950972071624; R.C[6][5] = -6.551835421242162;
+  R.C[7][0] = 42.57076742291101; R.C[7][1] = -13.80770672017997; R.C[7][2] = 93.98938432427124;
+  R.C[7][3] = 18.77919633714503; R.C[7][4] = -31.58359187223370; R.C[7][5] = -6.685968952921985; R.C[7][6] = -5.810979938412932;
+  const double c_[8] = {0.0, 0.38, 0.3878509998321533, 0.4839718937873840, 0.4570477008819580, 1.0, 1.0, 1.0};
+  const double d_[8] = {0.19, -0.1823079225333714636, -0.319231832186874912, 0.3449828624725343, -0.377417564392089818, 0, 0, 0};
+  for (int i = 0; i < 8; ++i) { R.c[i] = c_[i]; R.d[i] = d_[i]; }
+}
+
+}  // namespace deb

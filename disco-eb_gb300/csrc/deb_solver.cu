@@ -1,0 +1,297 @@
+// deb_solver.cu -- CUDA kernels and the C ABI of include/discoeb_gb300.h.
+//
+// Execution model: one persistent grid sized to the device (blocks of 128
+// threads, a few blocks per SM); every thread owns one workspace slot and
+// pulls k-modes from a device-side queue (one atomicAdd per mode).  A mode is
+// integrated to completion by its thread, then the thread takes the next
+// queued mode, so modes with very different step counts (and modes of
+// different cosmologies) share the launch without lock-step waste.  Each
+// warp keeps its 32 slots interleaved in global memory (element e of lane l
+// at base + 32 e + l), so every vector access of the warp is one coalesced
+// 256-byte transaction.
+//
+// Replaces jax.vmap(evolve_one_mode) of perturbations.py:980-987 (and the
+// lock-step while_loop it compiles to) for one GPU.
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+
+#include "deb_core.cuh"
+#include "discoeb_gb300.h"
+
+namespace {
+
+constexpr int kBlock = 128;
+
+__constant__ deb::Tab c_tab;
+__constant__ deb::Rodas c_rodas;
+
+struct KParams {
+  const double* tables;
+  int ncosmo, blob_len;
+  const double* k;
+  const int* cosmo;
+  int nmode;
+  const double* tau_out;
+  double* y_out;
+  int* status;
+  int* steps;
+  double* ws;
+  long slot_len;
+  int* queue;
+  deb::Ctl ctl;
+  deb::Dims D;
+};
+
+__global__ void __launch_bounds__(kBlock) forward_kernel(KParams P) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const long warp = tid >> 5;
+  deb::WS w;
+  w.p = P.ws + warp * 32 * P.slot_len + lane;
+  w.stride = 32;
+  w.n = P.D.n;
+  w.misc0 = (long)deb::NV * P.D.n;
+  const int osz = P.ctl.return_full ? P.D.n : DEB_NOUT_FIELDS;
+  int mode = -1;
+  deb::Cosmo c;
+  deb::ModeConst mc;
+  deb::Run run;
+  const double* tau_out = nullptr;
+  double* yout = nullptr;
+
+  auto fetch = [&]() -> bool {
+    for (;;) {
+      const int m = atomicAdd(P.queue, 1);
+      if (m >= P.nmode) return false;
+      mode = m;
+      const int ci = P.cosmo ? P.cosmo[m] : 0;
+      const double k = P.k[m];
+      double* dst = P.y_out + (long)m * P.ctl.nout * osz;
+      for (int i = 0; i < P.ctl.nout * osz; ++i) dst[i] = __longlong_as_double(0x7ff8000000000000LL);
+      bool ok = ci >= 0 && ci < P.ncosmo && k > 0.0 && isfinite(k);
+      if (ok) ok = deb::load_cosmo(P.tables + (long)ci * P.blob_len, P.blob_len, c) && c.nq == P.D.nq;
+      if (!ok) {
+        P.status[m] = deb::ST_BAD_INPUT;
+        if (P.steps) { P.steps[2 * m] = 0; P.steps[2 * m + 1] = 0; }
+        continue;
+      }
+      deb::mode_const(c, k, mc);
+      tau_out = P.tau_out + (long)ci * P.ctl.nout;
+      yout = dst;
+      deb::mode_begin(c, mc, P.D, P.ctl, w, tau_out, run);
+      return true;
+    }
+  };
+
+  bool active = fetch();
+  while (__any_sync(0xffffffffu, active)) {
+    if (active) {
+      const bool more = deb::mode_step(c, mc, P.D, c_tab, c_rodas, P.ctl, w, tau_out, yout, 1, run);
+      if (!more) {
+        P.status[mode] = run.status;
+        if (P.steps) { P.steps[2 * mode] = run.acc; P.steps[2 * mode + 1] = run.rej; }
+        active = fetch();
+      }
+    }
+  }
+}
+
+__global__ void power_kernel(const double* tables, int ncosmo, int blob_len, const double* k, const int* cosmo, int nmode,
+                             int nout, const double* y, int stride, int idx, double* P) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)nmode * nout) return;
+  const int m = (int)(t / nout);
+  const int ci = cosmo ? cosmo[m] : 0;
+  if (ci < 0 || ci >= ncosmo) { P[t] = __longlong_as_double(0x7ff8000000000000LL); return; }
+  const double* b = tables + (long)ci * blob_len;
+  const double As = b[deb::H_AS], ns = b[deb::H_NS], kp = b[deb::H_KP];
+  const double km = k[m];
+  const double v = y[t * stride + idx];
+  // get_power, perturbations.py:1123
+  P[t] = 2.0 * M_PI * M_PI * As * pow(km / kp, ns - 1.0) * pow(km, -3.0) * v * v;
+}
+
+// Independent FMA chains: 8 per thread, long enough to be issue-bound.
+__global__ void fp64_peak_kernel(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  const double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+
+bool g_consts_ready[64] = {false};
+
+int upload_constants() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return DEB_ERR_CUDA;
+  if (dev >= 0 && dev < 64 && g_consts_ready[dev]) return DEB_OK;
+  deb::Tab T;
+  deb::Rodas R;
+  deb::fill_tables(T);
+  deb::fill_rodas(R);
+  if (cudaMemcpyToSymbol(c_tab, &T, sizeof(T)) != cudaSuccess) return DEB_ERR_CUDA;
+  if (cudaMemcpyToSymbol(c_rodas, &R, sizeof(R)) != cudaSuccess) return DEB_ERR_CUDA;
+  if (dev >= 0 && dev < 64) g_consts_ready[dev] = true;
+  return DEB_OK;
+}
+
+}  // namespace
+
+struct deb_plan {
+  deb::Dims D;
+  int dense, return_full, nout;
+  int max_modes, nslots, nblocks;
+  long slot_len;
+  double* ws;
+  int* queue;
+  size_t ws_bytes;
+};
+
+extern "C" {
+
+int deb_version(void) { return 1; }
+
+const char* deb_error_string(int code) {
+  switch (code) {
+    case DEB_OK: return "ok";
+    case DEB_ERR_INVALID: return "invalid argument";
+    case DEB_ERR_TABLES: return "inconsistent table blob";
+    case DEB_ERR_CUDA: return "CUDA runtime error";
+    case DEB_ERR_NOMEM: return "device allocation failed";
+    case DEB_ERR_CAPACITY: return "plan capacity exceeded";
+    default: return "unknown error";
+  }
+}
+
+int deb_nvar(const deb_dims* d) {
+  if (!d) return DEB_ERR_INVALID;
+  return deb::make_dims(d->lmaxg, d->lmaxgp, d->lmaxr, d->lmaxnu, d->nqmax).n;
+}
+
+int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
+  if (!dims || !out || max_modes <= 0) return DEB_ERR_INVALID;
+  *out = nullptr;
+  if (dims->lmaxg < 3 || dims->lmaxgp < 3 || dims->lmaxr < 3 || dims->lmaxnu < 3 || dims->nqmax < 1 || dims->nout < 1)
+    return DEB_ERR_INVALID;
+  if (dims->lmaxg > deb::LMAX_TABLE || dims->lmaxgp > deb::LMAX_TABLE || dims->lmaxr > deb::LMAX_TABLE ||
+      dims->lmaxnu > deb::LMAX_TABLE)
+    return DEB_ERR_INVALID;
+  if (dims->linear_solver != DEB_SOLVE_STRUCTURED && dims->linear_solver != DEB_SOLVE_DENSE) return DEB_ERR_INVALID;
+  int rc = upload_constants();
+  if (rc) return rc;
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return DEB_ERR_CUDA;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return DEB_ERR_CUDA;
+  deb_plan* p = new deb_plan();
+  p->D = deb::make_dims(dims->lmaxg, dims->lmaxgp, dims->lmaxr, dims->lmaxnu, dims->nqmax);
+  p->dense = dims->linear_solver == DEB_SOLVE_DENSE;
+  p->return_full = dims->return_full;
+  p->nout = dims->nout;
+  p->max_modes = max_modes;
+  p->slot_len = deb::slot_len(p->D, p->dense);
+  // slots: enough for every mode, at most 4 blocks per SM, and at most
+  // 16 GiB of workspace
+  long cap = (long)nsm * 4 * kBlock;
+  const long mem_cap = (16L << 30) / (p->slot_len * 8);
+  if (cap > mem_cap) cap = (mem_cap / 32) * 32;
+  if (cap < 32) cap = 32;
+  long want = ((long)max_modes + 31) / 32 * 32;
+  long ns = want < cap ? want : cap;
+  p->nblocks = (int)((ns + kBlock - 1) / kBlock);
+  p->nslots = p->nblocks * kBlock;
+  p->ws_bytes = (size_t)p->nslots * p->slot_len * sizeof(double);
+  if (cudaMalloc(&p->ws, p->ws_bytes) != cudaSuccess) { delete p; return DEB_ERR_NOMEM; }
+  if (cudaMalloc(&p->queue, sizeof(int) * 4) != cudaSuccess) { cudaFree(p->ws); delete p; return DEB_ERR_NOMEM; }
+  *out = p;
+  return DEB_OK;
+}
+
+int deb_plan_workspace_bytes(const deb_plan* p, size_t* bytes) {
+  if (!p || !bytes) return DEB_ERR_INVALID;
+  *bytes = p->ws_bytes;
+  return DEB_OK;
+}
+
+void deb_plan_destroy(deb_plan* p) {
+  if (!p) return;
+  cudaFree(p->ws);
+  cudaFree(p->queue);
+  delete p;
+}
+
+int deb_forward(deb_plan* p, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
+                const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+                double* d_y_out, int* d_status, int* d_steps, void* stream) {
+  if (!p || !cfg || ncosmo <= 0 || nmode < 0 || blob_len <= deb::HDR_LEN) return DEB_ERR_INVALID;
+  if (nmode == 0) return DEB_OK;
+  if (!d_tables || !d_k || !d_tau_out || !d_y_out || !d_status) return DEB_ERR_INVALID;
+  if (nmode > p->max_modes) return DEB_ERR_CAPACITY;
+  if (!(cfg->rtol >= 0.0) || !(cfg->atol >= 0.0) || cfg->max_steps <= 0 || !(cfg->error_order > 0.0)) return DEB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  KParams P;
+  P.tables = d_tables; P.ncosmo = ncosmo; P.blob_len = blob_len; P.k = d_k; P.cosmo = d_cosmo_of_mode;
+  P.nmode = nmode; P.tau_out = d_tau_out; P.y_out = d_y_out; P.status = d_status; P.steps = d_steps;
+  P.ws = p->ws; P.slot_len = p->slot_len; P.queue = p->queue; P.D = p->D;
+  P.ctl.rtol = cfg->rtol; P.ctl.atol = cfg->atol;
+  P.ctl.b1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / cfg->error_order;
+  P.ctl.b2 = -(cfg->pcoeff + 2.0 * cfg->dcoeff) / cfg->error_order;
+  P.ctl.b3 = cfg->dcoeff / cfg->error_order;
+  P.ctl.safety = cfg->safety; P.ctl.fmin = cfg->factormin; P.ctl.fmax = cfg->factormax;
+  P.ctl.max_steps = cfg->max_steps; P.ctl.hist_on_reject = cfg->hist_on_reject;
+  P.ctl.dense = p->dense; P.ctl.return_full = p->return_full; P.ctl.nout = p->nout;
+  if (cudaMemsetAsync(p->queue, 0, sizeof(int), s) != cudaSuccess) return DEB_ERR_CUDA;
+  long need = ((long)nmode + kBlock - 1) / kBlock;
+  const int blocks = (int)(need < p->nblocks ? need : p->nblocks);
+  forward_kernel<<<blocks, kBlock, 0, s>>>(P);
+  if (cudaGetLastError() != cudaSuccess) return DEB_ERR_CUDA;
+  return DEB_OK;
+}
+
+int deb_get_power(const double* d_tables, int ncosmo, int blob_len, const double* d_k, const int* d_cosmo_of_mode,
+                  int nmode, int nout, const double* d_y, int stride, int idx, double* d_P, void* stream) {
+  if (!d_tables || !d_k || !d_y || !d_P || ncosmo <= 0 || nmode < 0 || nout <= 0 || idx < 0 || idx >= stride)
+    return DEB_ERR_INVALID;
+  if (nmode == 0) return DEB_OK;
+  const long tot = (long)nmode * nout;
+  const int threads = 256;
+  power_kernel<<<(unsigned)((tot + threads - 1) / threads), threads, 0, (cudaStream_t)stream>>>(
+      d_tables, ncosmo, blob_len, d_k, d_cosmo_of_mode, nmode, nout, d_y, stride, idx, d_P);
+  return cudaGetLastError() == cudaSuccess ? DEB_OK : DEB_ERR_CUDA;
+}
+
+int deb_measure_fp64_peak(double* flops_per_s, void* stream) {
+  if (!flops_per_s) return DEB_ERR_INVALID;
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return DEB_ERR_CUDA;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return DEB_ERR_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
+  double* out = nullptr;
+  if (cudaMalloc(&out, sizeof(double)) != cudaSuccess) return DEB_ERR_NOMEM;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = nsm * 8, threads = 256, iters = 1 << 14;
+  fp64_peak_kernel<<<blocks, threads, 0, s>>>(out, 256, 1.0000001, 1e-9);  // warm-up
+  cudaEventRecord(e0, s);
+  fp64_peak_kernel<<<blocks, threads, 0, s>>>(out, iters, 1.0000001, 1e-9);
+  cudaEventRecord(e1, s);
+  cudaError_t err = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (err != cudaSuccess || ms <= 0.f) return DEB_ERR_CUDA;
+  *flops_per_s = 2.0 * 8.0 * (double)iters * blocks * threads / (ms * 1e-3);
+  return DEB_OK;
+}
+
+}  // extern "C"

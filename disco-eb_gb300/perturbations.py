@@ -1,0 +1,260 @@
+"""Reference-facing API of the perturbation hot path (GPU only).
+
+Mirrors ``discoeb.perturbations`` (``src/discoeb/perturbations.py``):
+
+* :func:`evolve_perturbations` -- same keyword-only signature and the same
+  ``(y, kmodes, param)`` return as ``perturbations.py:926-997``;
+* :func:`evolve_perturbations_batched` -- signature of
+  ``perturbations.py:1000-1061``, returns ``(y, kmodes)``;
+* :func:`get_power` -- ``perturbations.py:1101-1123``;
+* :func:`evolve_perturbations_multi` -- many cosmologies in one launch (no
+  reference counterpart; the reference handles one ``param`` per call).
+
+All integration runs in the CUDA library through the C ABI; ``param`` is
+packed into the FP64 table blob (:mod:`tables`) and uploaded.  When a mode
+fails (max_steps reached, non-finite state) the call raises RuntimeError like
+diffrax does with ``throw=True``, unless ``throw=False``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+from . import tables as _tables
+
+_plans: dict = {}
+
+
+def _torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("discoeb_gb300 needs a CUDA device; none is available")
+    return torch
+
+
+def nvar(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax) -> int:
+    """Number of ODE variables (``perturbations.py:739``)."""
+    return 7 + (lmaxg + 1) + (lmaxgp + 1) + (lmaxr + 1) + nqmax * (lmaxnu + 1) + 2
+
+
+def _dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, nout, return_full, linear_solver):
+    ls = {"structured": _native.DEB_SOLVE_STRUCTURED, "dense": _native.DEB_SOLVE_DENSE}[linear_solver]
+    return _native.DebDims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, nout, 1 if return_full else 0, ls)
+
+
+def _cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps, safety=0.9, error_order=5.0,
+         hist_on_reject=False):
+    return _native.DebSolverCfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, safety, error_order,
+                                int(max_steps), 1 if hist_on_reject else 0)
+
+
+def get_plan(dims: _native.DebDims, nmode: int) -> _native.Plan:
+    """Cached plan for these hierarchy sizes with room for >= nmode modes."""
+    torch = _torch()
+    key = (torch.cuda.current_device(), dims.lmaxg, dims.lmaxgp, dims.lmaxr, dims.lmaxnu, dims.nqmax, dims.nout,
+           dims.return_full, dims.linear_solver)
+    p = _plans.get(key)
+    if p is None or p.max_modes < nmode:
+        _plans.pop(key, None)
+        p = _native.Plan(dims, max(nmode, 1))
+        _plans[key] = p
+    return p
+
+
+class DeviceProblem:
+    """Device-resident inputs/outputs of one launch, reusable across launches.
+
+    ``tables`` [ncosmo, blob_len], ``kmodes`` [nmode], ``cosmo_of_mode``
+    [nmode], ``tau_out`` [ncosmo, nout] -- numpy or torch; moved to the
+    current CUDA device once.  :meth:`launch` enqueues ``deb_forward`` on a
+    stream without synchronising.
+    """
+
+    def __init__(self, tables, kmodes, tau_out, cosmo_of_mode=None, *, lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax,
+                 return_full=False, linear_solver="structured"):
+        torch = _torch()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        as_t = lambda a, dt: (a if torch.is_tensor(a) else torch.as_tensor(np.ascontiguousarray(a))).to(dev, dt).contiguous()
+        self.tables = as_t(np.atleast_2d(tables) if not torch.is_tensor(tables) else tables, torch.float64)
+        self.k = as_t(kmodes, torch.float64)
+        self.tau_out = as_t(np.atleast_2d(tau_out) if not torch.is_tensor(tau_out) else tau_out, torch.float64)
+        self.nmode = int(self.k.shape[0])
+        self.ncosmo = int(self.tables.shape[0])
+        self.blob_len = int(self.tables.shape[1])
+        self.nout = int(self.tau_out.shape[1])
+        if cosmo_of_mode is None:
+            self.cosmo = None
+        else:
+            self.cosmo = as_t(cosmo_of_mode, torch.int32)
+        self.dims = _dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, self.nout, return_full, linear_solver)
+        self.n = nvar(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax)
+        self.osz = self.n if return_full else 20
+        self.y = torch.empty((self.nmode, self.nout, self.osz), dtype=torch.float64, device=dev)
+        self.status = torch.empty((self.nmode,), dtype=torch.int32, device=dev)
+        self.steps = torch.empty((self.nmode, 2), dtype=torch.int32, device=dev)
+        self.plan = get_plan(self.dims, self.nmode)
+        self.device = dev
+
+    def launch(self, cfg: _native.DebSolverCfg, stream=None):
+        torch = _torch()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        L = _native.load()
+        rc = L.deb_forward(self.plan.ptr, ctypes.c_void_p(self.tables.data_ptr()), self.ncosmo, self.blob_len,
+                           ctypes.c_void_p(self.k.data_ptr()),
+                           ctypes.c_void_p(self.cosmo.data_ptr() if self.cosmo is not None else 0), self.nmode,
+                           ctypes.c_void_p(self.tau_out.data_ptr()), ctypes.byref(cfg),
+                           ctypes.c_void_p(self.y.data_ptr()), ctypes.c_void_p(self.status.data_ptr()),
+                           ctypes.c_void_p(self.steps.data_ptr()), ctypes.c_void_p(s.cuda_stream))
+        _native.check(rc, "deb_forward")
+
+    def power(self, idx: int, stream=None):
+        """P(k) of field ``idx`` for every mode and output, on the device."""
+        torch = _torch()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        P = torch.empty((self.nmode, self.nout), dtype=torch.float64, device=self.device)
+        rc = _native.load().deb_get_power(ctypes.c_void_p(self.tables.data_ptr()), self.ncosmo, self.blob_len,
+                                          ctypes.c_void_p(self.k.data_ptr()),
+                                          ctypes.c_void_p(self.cosmo.data_ptr() if self.cosmo is not None else 0),
+                                          self.nmode, self.nout, ctypes.c_void_p(self.y.data_ptr()), self.osz, int(idx),
+                                          ctypes.c_void_p(P.data_ptr()), ctypes.c_void_p(s.cuda_stream))
+        _native.check(rc, "deb_get_power")
+        return P
+
+
+def _check_status(status: np.ndarray, kmodes: np.ndarray, throw: bool):
+    bad = np.nonzero(status != 0)[0]
+    if bad.size and throw:
+        names = [f"k={kmodes[i]:.4g}:{_native.MODE_STATUS.get(int(status[i]), status[i])}" for i in bad[:8]]
+        raise RuntimeError(f"{bad.size} mode(s) failed: " + ", ".join(names) + (" ..." if bad.size > 8 else ""))
+
+
+def solve(tables, kmodes, tau_out, cosmo_of_mode=None, *, lmaxg=11, lmaxgp=11, lmaxr=11, lmaxnu=8, nqmax=3,
+          rtol=1e-4, atol=1e-4, pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, max_steps=2048,
+          return_full=False, linear_solver="structured", throw=True, return_stats=False, output="numpy",
+          error_order=5.0, safety=0.9, hist_on_reject=False):
+    """Integrate modes of packed cosmologies on the GPU; y [nmode, nout, 20|nvar]."""
+    torch = _torch()
+    prob = DeviceProblem(tables, kmodes, tau_out, cosmo_of_mode, lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr, lmaxnu=lmaxnu,
+                         nqmax=nqmax, return_full=return_full, linear_solver=linear_solver)
+    cfg = _cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps, safety, error_order, hist_on_reject)
+    prob.launch(cfg)
+    status = prob.status.cpu().numpy()
+    _check_status(status, np.asarray(kmodes if not torch.is_tensor(kmodes) else kmodes.cpu()), throw)
+    y = prob.y if output == "torch" else prob.y.cpu().numpy()
+    if return_stats:
+        return y, {"status": status, "steps": prob.steps.cpu().numpy()}
+    return y
+
+
+def evolve_perturbations(*, param, aexp_out, kmin: float, kmax: float, num_k: int, lmaxg: int = 11, lmaxgp: int = 11,
+                         lmaxr: int = 11, lmaxnu: int = 8, nqmax: int = 3, rtol: float = 1e-4, atol: float = 1e-4,
+                         pcoeff: float = 0.25, icoeff: float = 0.80, dcoeff: float = 0.0, factormax: float = 20.0,
+                         factormin: float = 0.3, max_steps: int = 2048, return_full: bool = False, dologk: bool = True,
+                         throw: bool = True, linear_solver: str = "structured", output: str = "numpy"):
+    """Evolve the synchronous-gauge perturbations of all k-modes on the GPU.
+
+    Same arguments and return value as ``perturbations.py:926-997``:
+    ``y`` is ``[num_k, nout, 20]`` (``[num_k, nout, nvar]`` with
+    ``return_full``), ``kmodes`` the geomspace (or linspace) grid, and
+    ``param`` is updated in place with lmax*/nqmax/nout/tau_out.
+    """
+    kmodes = np.geomspace(kmin, kmax, num_k) if dologk else np.linspace(kmin, kmax, num_k)
+    aexp_out = np.atleast_1d(np.asarray(aexp_out, dtype=np.float64))
+    tau_out = _tables.tau_of_a(param, aexp_out)
+    blob = _tables.pack_cosmology(param, nqmax)
+    y = solve(blob[None, :], kmodes, tau_out[None, :], None, lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr, lmaxnu=lmaxnu,
+              nqmax=nqmax, rtol=rtol, atol=atol, pcoeff=pcoeff, icoeff=icoeff, dcoeff=dcoeff, factormax=factormax,
+              factormin=factormin, max_steps=max_steps, return_full=return_full, linear_solver=linear_solver,
+              throw=throw, output=output)
+    param["lmaxg"] = lmaxg
+    param["lmaxgp"] = lmaxgp
+    param["lmaxr"] = lmaxr
+    param["lmaxnu"] = lmaxnu
+    param["nqmax"] = nqmax
+    param["nout"] = aexp_out.shape[0]
+    param["tau_out"] = tau_out
+    return y, kmodes, param
+
+
+def evolve_perturbations_batched(*, param, aexp_out, kmin: float, kmax: float, num_k: int, lmaxg: int = 11,
+                                 lmaxgp: int = 11, lmaxr: int = 11, lmaxnu: int = 8, nqmax: int = 3, rtol: float = 1e-4,
+                                 atol: float = 1e-4, pcoeff: float = 0.25, icoeff: float = 0.80, dcoeff: float = 0.0,
+                                 factormax: float = 20.0, factormin: float = 0.3, max_steps: int = 2048,
+                                 batch_size: int = 16, throw: bool = True, output: str = "numpy"):
+    """Signature of ``perturbations.py:1000-1061``; returns ``(y, kmodes)``.
+
+    The reference groups ``batch_size`` modes under one shared start time
+    and one shared step sequence so they fit a vmapped dense solver.  The GPU
+    kernel needs no such grouping: every mode keeps its own start time and
+    step sequence (the ``evolve_perturbations`` semantics), so results equal
+    :func:`evolve_perturbations` and differ from the reference's batched
+    variant by that variant's own grouping error.  ``batch_size`` must
+    divide ``num_k`` as in the reference.
+    """
+    if num_k % batch_size != 0:
+        raise ValueError("num_k must be divisible by batch_size")
+    y, kmodes, _ = evolve_perturbations(param=dict(param), aexp_out=aexp_out, kmin=kmin, kmax=kmax, num_k=num_k,
+                                        lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr, lmaxnu=lmaxnu, nqmax=nqmax, rtol=rtol,
+                                        atol=atol, pcoeff=pcoeff, icoeff=icoeff, dcoeff=dcoeff, factormax=factormax,
+                                        factormin=factormin, max_steps=max_steps, throw=throw, output=output)
+    param["nout"] = np.atleast_1d(aexp_out).shape[0]
+    return y, kmodes
+
+
+def evolve_perturbations_multi(*, params, aexp_out, kmin: float, kmax: float, num_k: int, lmaxg: int = 11,
+                               lmaxgp: int = 11, lmaxr: int = 11, lmaxnu: int = 8, nqmax: int = 3, rtol: float = 1e-4,
+                               atol: float = 1e-4, pcoeff: float = 0.25, icoeff: float = 0.80, dcoeff: float = 0.0,
+                               factormax: float = 20.0, factormin: float = 0.3, max_steps: int = 2048,
+                               return_full: bool = False, dologk: bool = True, throw: bool = True,
+                               linear_solver: str = "structured", output: str = "numpy"):
+    """All modes of many cosmologies in one persistent launch.
+
+    Returns ``y [ncosmo, num_k, nout, 20]`` and ``kmodes``.
+    """
+    kmodes = np.geomspace(kmin, kmax, num_k) if dologk else np.linspace(kmin, kmax, num_k)
+    aexp_out = np.atleast_1d(np.asarray(aexp_out, dtype=np.float64))
+    tabs = _tables.pack_batch(params, nqmax)
+    tau = np.stack([_tables.tau_of_a(p, aexp_out) for p in params])
+    nc = len(params)
+    kk = np.tile(kmodes, nc)
+    com = np.repeat(np.arange(nc, dtype=np.int32), num_k)
+    y = solve(tabs, kk, tau, com, lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr, lmaxnu=lmaxnu, nqmax=nqmax, rtol=rtol,
+              atol=atol, pcoeff=pcoeff, icoeff=icoeff, dcoeff=dcoeff, factormax=factormax, factormin=factormin,
+              max_steps=max_steps, return_full=return_full, linear_solver=linear_solver, throw=throw, output=output)
+    return y.reshape(nc, num_k, aexp_out.shape[0], -1), kmodes
+
+
+def get_power(*, k, y, idx: int, param: dict):
+    """P(k) = 2 pi^2 A_s (k/k_p)^(n_s-1) k^-3 y[..., idx]^2 (``perturbations.py:1101-1123``).
+
+    Evaluated on the GPU by ``deb_get_power``.  ``y`` may have shape
+    ``[num_k, 20]`` or ``[num_k, nout, 20]`` (numpy or CUDA tensor); the
+    result has ``y``'s shape without the last axis and the container type of
+    ``y``.
+    """
+    torch = _torch()
+    is_t = torch.is_tensor(y)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    yt = (y if is_t else torch.as_tensor(np.asarray(y, dtype=np.float64))).to(dev, torch.float64).contiguous()
+    kt = (k if torch.is_tensor(k) else torch.as_tensor(np.asarray(k, dtype=np.float64))).to(dev, torch.float64).contiguous()
+    shape = tuple(yt.shape[:-1])
+    nmode = int(kt.shape[0])
+    nout = int(np.prod(shape[1:])) if len(shape) > 1 else 1
+    if int(np.prod(shape)) != nmode * nout:
+        raise ValueError("y must be [num_k, ..., nfields] with num_k == len(k)")
+    hdr = np.zeros((1, _tables.HDR_LEN + 3 * 2 * 7 + 2), dtype=np.float64)
+    hdr[0, 16] = float(param["A_s"])
+    hdr[0, 17] = float(param["n_s"])
+    hdr[0, 18] = float(param.get("k_p", 0.05))
+    ht = torch.as_tensor(hdr).to(dev)
+    P = torch.empty((nmode, nout), dtype=torch.float64, device=dev)
+    s = torch.cuda.current_stream()
+    rc = _native.load().deb_get_power(ctypes.c_void_p(ht.data_ptr()), 1, hdr.shape[1], ctypes.c_void_p(kt.data_ptr()),
+                                      ctypes.c_void_p(0), nmode, nout, ctypes.c_void_p(yt.data_ptr()), int(yt.shape[-1]),
+                                      int(idx), ctypes.c_void_p(P.data_ptr()), ctypes.c_void_p(s.cuda_stream))
+    _native.check(rc, "deb_get_power")
+    P = P.reshape(shape)
+    return P if is_t else P.cpu().numpy()

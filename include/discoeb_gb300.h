@@ -1,0 +1,135 @@
+/*
+ * discoeb_gb300.h -- C ABI of the GB300 perturbation solver.
+ *
+ * Replaces, for one GPU, the hot path of the reference's
+ *   discoeb.perturbations.evolve_perturbations   (src/discoeb/perturbations.py:926-997)
+ * i.e. the vmap over k-modes of evolve_one_mode (perturbations.py:728-781):
+ * start time + adiabatic ICs + Rodas5(transformed) + PID step control +
+ * SaveAt linear interpolation + conversion to the 20 output fields.  The
+ * get_power assembly (perturbations.py:1101-1123) is deb_get_power below.
+ *
+ * Conventions
+ *   - every pointer named d_* is a caller-owned DEVICE buffer;
+ *   - calls are stream-ordered on `stream` (a cudaStream_t passed as void*,
+ *     NULL = legacy default stream) and do not synchronise the host, except
+ *     deb_plan_create / deb_plan_destroy;
+ *   - return value 0 = success, < 0 = deb_status error code (no exceptions
+ *     cross the ABI); per-mode solver outcomes go to d_status;
+ *   - a plan is not thread-safe: one plan per stream.
+ *
+ * Table blob (FP64, one per cosmology, all blobs of one call the same length)
+ *   [0..31]   header: Omegam, Omegab, OmegaDE, Omegak, grhom, grhog, grhor,
+ *             Neff, Nmnu, amnu, w_DE_0, w_DE_a, cs2_DE, YHe, H0, taumin, A_s,
+ *             n_s, k_p, nq, n_spline[7], blob_len, magic (20231103), 0, 0, 0
+ *   splines   7 x (x[n], y[n], S[n]) in the order xe(log a), c_s^2 a(log a),
+ *             log rho_nu(log a), log p_nu(log a), a(tau), tau(a), xe(tau)
+ *             (fields _x_, _y_, _S_full_ of spline_interpolation.py:112-113)
+ *   nodes     q[nq], w[nq] of get_neutrino_momentum_bins (background.py:13-44)
+ */
+#ifndef DISCOEB_GB300_H
+#define DISCOEB_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DEB_HDR_LEN 32
+#define DEB_TABLE_MAGIC 20231103.0
+#define DEB_NOUT_FIELDS 20
+
+/* error codes (return values) */
+enum deb_status {
+  DEB_OK = 0,
+  DEB_ERR_INVALID = -1,     /* bad argument (sizes, NULL pointer, lmax < 3) */
+  DEB_ERR_TABLES = -2,      /* table blob header / magic / sizes inconsistent */
+  DEB_ERR_CUDA = -3,        /* a CUDA runtime call failed */
+  DEB_ERR_NOMEM = -4,       /* device allocation for the plan failed */
+  DEB_ERR_CAPACITY = -5     /* more modes or variables than the plan was made for */
+};
+
+/* per-mode outcome written to d_status (same meaning as the oracle's) */
+enum deb_mode_status {
+  DEB_MODE_OK = 0,
+  DEB_MODE_MAX_STEPS = 1,   /* diffrax would raise: max_steps reached (perturbations.py:762) */
+  DEB_MODE_DT_UNDERFLOW = 2,/* step size no longer advances tau */
+  DEB_MODE_NONFINITE = 3,   /* NaN/Inf in the error estimate (e.g. w = -1 exactly) */
+  DEB_MODE_BAD_INPUT = 4    /* k <= 0, cosmology index out of range, bad tables */
+};
+
+/* linear solver for W = I/(gamma h) - J */
+enum deb_linear_solver {
+  DEB_SOLVE_STRUCTURED = 0, /* exact block/chain elimination + rank-2 Woodbury, O(n) */
+  DEB_SOLVE_DENSE = 1       /* dense LU with partial pivoting, O(n^3), as the reference */
+};
+
+/* hierarchy sizes: the keyword arguments of evolve_perturbations (perturbations.py:926-930) */
+typedef struct deb_dims {
+  int lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax;
+  int nout;            /* output times per cosmology */
+  int return_full;     /* 0: 20 output fields, 1: full state of nvar entries */
+  int linear_solver;   /* enum deb_linear_solver */
+} deb_dims;
+
+/* PIDController arguments of evolve_one_mode (perturbations.py:759-760) plus
+   diffrax defaults the reference inherits (safety 0.9, error order 5). */
+typedef struct deb_solver_cfg {
+  double rtol, atol;
+  double pcoeff, icoeff, dcoeff;
+  double factormax, factormin;
+  double safety;
+  double error_order;
+  int max_steps;
+  int hist_on_reject;  /* 1: a rejected step also shifts the error history */
+} deb_solver_cfg;
+
+typedef struct deb_plan deb_plan;
+
+/* number of ODE variables, perturbations.py:739 */
+int deb_nvar(const deb_dims* dims);
+
+/* Create a plan for up to max_modes modes per call.  Allocates the solver
+   workspace on the current device (the only allocation the library makes). */
+int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** plan);
+
+/* Bytes of device workspace the plan holds. */
+int deb_plan_workspace_bytes(const deb_plan* plan, size_t* bytes);
+
+/*
+ * Integrate nmode k-modes (perturbations.py:980-987 for one cosmology; here
+ * any number of cosmologies share one launch).
+ *   d_tables        [ncosmo, blob_len] FP64 table blobs
+ *   d_k             [nmode] wavenumbers in 1/Mpc
+ *   d_cosmo_of_mode [nmode] cosmology index of each mode (NULL: all 0)
+ *   d_tau_out       [ncosmo, nout] conformal output times (tau_of_a(aexp_out))
+ *   d_y_out         [nmode, nout, 20] (or [nmode, nout, nvar] if return_full)
+ *   d_status        [nmode] deb_mode_status
+ *   d_steps         [nmode, 2] accepted, rejected step counts (may be NULL)
+ */
+int deb_forward(deb_plan* plan, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
+                const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+                double* d_y_out, int* d_status, int* d_steps, void* stream);
+
+/*
+ * get_power (perturbations.py:1101-1123):
+ *   P[m, o] = 2 pi^2 A_s (k_m/k_p)^(n_s-1) k_m^-3 y[m, o, idx]^2
+ * with A_s, n_s, k_p read from the mode's cosmology blob.
+ *   d_y      [nmode, nout, stride]   d_P [nmode, nout]
+ */
+int deb_get_power(const double* d_tables, int ncosmo, int blob_len, const double* d_k, const int* d_cosmo_of_mode,
+                  int nmode, int nout, const double* d_y, int stride, int idx, double* d_P, void* stream);
+
+void deb_plan_destroy(deb_plan* plan);
+
+/* Measured-peak helper for roofline reporting: times a chain of dependent
+   FP64 FMAs over the whole device and returns achieved FP64 FLOP/s. */
+int deb_measure_fp64_peak(double* flops_per_s, void* stream);
+
+const char* deb_error_string(int code);
+int deb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DISCOEB_GB300_H */

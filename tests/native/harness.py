@@ -1,0 +1,76 @@
+"""ctypes wrapper of the test-only host build of the kernel core (core_harness.cpp)."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "core_harness.cpp")
+_CORE = os.path.join(_HERE, "..", "..", "disco-eb_gb300", "csrc", "deb_core.cuh")
+_LIB = os.path.join(_HERE, "_build", "libcore_harness.so")
+_lib = None
+dp = ctypes.POINTER(ctypes.c_double)
+ip = ctypes.POINTER(ctypes.c_int)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        os.makedirs(os.path.dirname(_LIB), exist_ok=True)
+        if not os.path.exists(_LIB) or os.path.getmtime(_LIB) < max(os.path.getmtime(_SRC), os.path.getmtime(_CORE)):
+            subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", _LIB, _SRC])
+        L = ctypes.CDLL(_LIB)
+        L.h_rhs.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, ctypes.c_double, dp, dp, dp]
+        L.h_solve_W.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, ctypes.c_double, dp, ctypes.c_double, dp, dp, ctypes.c_int]
+        L.h_start.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, dp, dp]
+        L.h_solve.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp, ip, ctypes.c_int, dp, ctypes.c_int, ip, dp, ctypes.c_int,
+                              ctypes.c_int, ctypes.c_int, dp, ip]
+        _lib = L
+    return _lib
+
+
+def _p(a, t=ctypes.c_double):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def _d(dims):
+    return np.array(dims, dtype=np.int32)
+
+
+def rhs(blob, dims, k, tau, y):
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    f, jc0 = np.empty_like(y), np.empty_like(y)
+    rc = lib().h_rhs(_p(blob), blob.shape[0], _p(_d(dims), ctypes.c_int), k, tau, _p(y), _p(f), _p(jc0))
+    assert rc == 0, rc
+    return f, jc0
+
+
+def solve_W(blob, dims, k, tau, y, dt, b, dense=False):
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.empty_like(b)
+    rc = lib().h_solve_W(_p(blob), blob.shape[0], _p(_d(dims), ctypes.c_int), k, tau, _p(y), dt, _p(b), _p(x), int(dense))
+    assert rc == 0, rc
+    return x
+
+
+def solve(tables, kmodes, tau_out, *, cosmo_of_mode=None, lmaxg=11, lmaxgp=11, lmaxr=11, lmaxnu=8, nqmax=3, rtol=1e-4,
+          atol=1e-4, pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, max_steps=2048,
+          return_full=False, error_order=5.0, safety=0.9, hist_on_reject=False, dense=False):
+    tables = np.ascontiguousarray(np.atleast_2d(tables), dtype=np.float64)
+    kmodes = np.ascontiguousarray(kmodes, dtype=np.float64)
+    tau_out = np.ascontiguousarray(np.atleast_2d(tau_out), dtype=np.float64)
+    nmode, nout = kmodes.shape[0], tau_out.shape[1]
+    com = np.ascontiguousarray(np.zeros(nmode) if cosmo_of_mode is None else cosmo_of_mode, dtype=np.int32)
+    dims = _d([lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax])
+    cfg = np.array([rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, error_order, safety,
+                    1.0 if hist_on_reject else 0.0])
+    n = 7 + (lmaxg + 1) + (lmaxgp + 1) + (lmaxr + 1) + nqmax * (lmaxnu + 1) + 2
+    y = np.empty((nmode, nout, n if return_full else 20))
+    st = np.zeros((nmode, 3), dtype=np.int32)
+    rc = lib().h_solve(_p(tables), tables.shape[0], tables.shape[1], _p(kmodes), _p(com, ctypes.c_int), nmode, _p(tau_out),
+                       nout, _p(dims, ctypes.c_int), _p(cfg), int(max_steps), int(return_full), int(dense), _p(y),
+                       _p(st, ctypes.c_int))
+    assert rc == 0, rc
+    return y, st
