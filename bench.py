@@ -166,7 +166,7 @@ def run_ours(args):
 
     inp = make_inputs(args.workload, rank, world)
     dims = inp["dims"]
-    prob = deb.DeviceProblem(inp["tables"], inp["k"], inp["tau"], inp["cosmo"], **dims)
+    prob = deb.DeviceProblem(inp["tables"], inp["k"], inp["tau"], inp["cosmo"], exec_mode=args.exec_mode, **dims)
     cfg = pt._cfg(inp["rtol"], inp["atol"], 0.25, 0.80, 0.0, 20.0, 0.3, args.max_steps)
     stream = torch.cuda.current_stream()
 
@@ -212,7 +212,7 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         y = deb.solve(host_tabs, host_k, host_tau, host_com, rtol=inp["rtol"], atol=inp["atol"], max_steps=args.max_steps,
-                      throw=False, **dims)
+                      throw=False, exec_mode=args.exec_mode, **dims)
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     h2d = host_tabs.nbytes + host_k.nbytes + host_tau.nbytes + host_com.nbytes
@@ -230,7 +230,8 @@ def run_ours(args):
         "dtype": "f64", "data": "synthetic (seeded cosmology sample, host RECFAST tables)",
         "config": {"workload": args.workload, "ncosmo_per_gpu": inp["ncosmo"], "num_k": inp["num_k"],
                    "modes_per_step": int(inp["k"].shape[0]), "nvar": prob.n, "rtol": inp["rtol"],
-                   "linear_solver": "structured", "l2": "working set > L2 (workspace %.2f GB)" % (prob.plan.workspace_bytes() / 1e9),
+                   "linear_solver": "structured", "exec_mode": ["auto", "lane", "warp"][prob.plan.dims.exec_mode]
+                   if args.exec_mode != "auto" else "auto", "l2": "working set > L2 (workspace %.2f GB)" % (prob.plan.workspace_bytes() / 1e9),
                    "redrawn_cosmologies": inp["rejected"]},
         "e2e": {"value": total_cosmo / t_e2e if world == 1 else None, "unit": "cosmology solves/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -285,6 +286,7 @@ def main():
     ap.add_argument("--max-steps", type=int, default=4096)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--exec-mode", default="auto", choices=["auto", "lane", "warp"])
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

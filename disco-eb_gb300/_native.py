@@ -13,13 +13,14 @@ LIB_PATH = os.path.join(HERE, "_build", "libdiscoeb_gb300.so")
 
 DEB_SOLVE_STRUCTURED = 0
 DEB_SOLVE_DENSE = 1
+EXEC_MODES = {"auto": 0, "lane": 1, "warp": 2}
 MODE_STATUS = {0: "OK", 1: "MAX_STEPS", 2: "DT_UNDERFLOW", 3: "NONFINITE", 4: "BAD_INPUT"}
 
 
 class DebDims(ctypes.Structure):
     _fields_ = [("lmaxg", ctypes.c_int), ("lmaxgp", ctypes.c_int), ("lmaxr", ctypes.c_int), ("lmaxnu", ctypes.c_int),
                 ("nqmax", ctypes.c_int), ("nout", ctypes.c_int), ("return_full", ctypes.c_int),
-                ("linear_solver", ctypes.c_int)]
+                ("linear_solver", ctypes.c_int), ("exec_mode", ctypes.c_int)]
 
 
 class DebSolverCfg(ctypes.Structure):

@@ -184,20 +184,60 @@ enum { Q_V = 0, Q_DV, Q_DLF, Q_GH, Q_GE, Q_R1, Q_DT, NQARR };
 enum { S_D = 0, S_W00I, S_ID, S_IDAH, S_GH2, S_GH3, S_GH5, S_GH7, S_GHR0, S_GHQE, S_GE4, S_GE6, S_GE8,
        S_GER1, S_GEQE, S_R13, S_R15, S_R17, S_R1R0, S_R1QE, S_R1QT, S_DTT, S_DTP, S_DTR };
 HD int misc_len(int nq) { return M_Q + NQARR * nq; }
-HD long slot_len(const Dims& D, bool dense) {
-  long L = (long)NV * D.n + misc_len(D.nq);
-  if (dense) L += (long)D.n * D.n + D.n;
-  return L;
-}
+HD long slot_len(const Dims& D) { return (long)NV * D.n + misc_len(D.nq); }
+HD long dense_len(const Dims& D) { return (long)D.n * D.n + D.n; }
 
 struct WS {
-  double* p;
+  double* p;      // vectors + MISC
   int stride;
   long n;
   long misc0;
+  double* dp;     // dense matrix + pivots (dense path only)
+  int dstride;
   HD double& v(int vec, int j) const { return p[((long)vec * n + j) * stride]; }
   HD double& m(int off) const { return p[(misc0 + off) * stride]; }
-  HD double& e(long off) const { return p[off * stride]; }
+  HD double& e(long off) const { return dp[off * dstride]; }
+};
+
+// A group of G lanes that cooperates on one mode: G = 1 (one thread per
+// mode; also the host build) or G = 32 (one warp per mode, state in shared
+// memory).  Vector loops stride by G, chains are spread over lanes, scalar
+// work is done redundantly or by the leading lane.  No sync/shuffle may sit
+// inside a lane-divergent branch.
+template <int G>
+struct Grp {
+  int lane;
+  HD bool lead() const { return lane == 0; }
+  HD void sync() const {
+#ifdef __CUDA_ARCH__
+    if (G > 1) __syncwarp();
+#endif
+  }
+  HD double sum(double x) const {
+#ifdef __CUDA_ARCH__
+    if (G > 1)
+      for (int o = G / 2; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+#endif
+    return x;
+  }
+  HD Dual sum(Dual x) const { return Dual(sum(x.v), sum(x.d)); }
+  HD bool any(bool b) const {
+#ifdef __CUDA_ARCH__
+    if (G > 1) return __any_sync(0xffffffffu, b);
+#endif
+    return b;
+  }
+  // index of the largest |value| (first index on ties) across the group
+  HD void argmax(double& best, int& bi) const {
+#ifdef __CUDA_ARCH__
+    if (G > 1)
+      for (int o = G / 2; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+#endif
+  }
 };
 
 // ------------------------------------------------------------------ constants
@@ -272,9 +312,10 @@ HD double aprimeoa(const Cosmo& c, const ModeConst& m, double a) {
 // ------------------------------------------------------------------ RHS
 // f = model_synchronous(tau, y) (perturbations.py:84-371).  With S = Dual the
 // a-dependence is differentiated: vout receives f, vjc receives d f / d a.
-template <class S>
-HD void rhs(const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, double tau, const WS& w, int vin,
-            int vout, int vjc) {
+// Ends with a group sync; expects vin to be complete (synced) on entry.
+template <class S, int G>
+HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, double tau, const WS& w,
+            int vin, int vout, int vjc) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, iq1 = iq0 + nq, iq2 = iq1 + nq, iq3 = iq2 + nq;
   const int igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
   const double k = m.k, k2 = m.k2;
@@ -286,12 +327,9 @@ HD void rhs(const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, dou
     w.v(vout, j) = val(f);
     if (vjc >= 0) w.v(vjc, j) = der(f);
   };
-  const double eta = Y(2), dc = Y(3), tc = Y(4), db = Y(5), tb = Y(6), dg = Y(7), tg = Y(8), y9 = Y(9);
-  const double dr = Y(ir), tr = Y(ir + 1), y_r2 = Y(ir + 2);
-  const double dq = Y(n - 2), tq = Y(n - 1);
   // massive neutrino momentum sums (nu_perturb, perturbations.py:22-50)
   S drhonu = 0.0, dpnu = 0.0, fnu = 0.0;
-  for (int i = 0; i < nq; ++i) {
+  for (int i = gp.lane; i < nq; i += G) {
     const double amq = m.amnu / LDG(c.q + i);
     S aq = g.a * amq;
     S v = 1.0 / dsqrt(1.0 + aq * aq);
@@ -300,71 +338,88 @@ HD void rhs(const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, dou
     drhonu = drhonu + wq * p0 / v;
     dpnu = dpnu + wq * p0 * v;
     fnu = fnu + wq * Y(iq1 + i);
-    w.m(M_Q + i) = val(v);                 // v_q and d v_q / d a for the element loop
-    if (vjc >= 0) w.m(M_Q + nq + i) = der(v);
+    w.m(M_Q + Q_V * nq + i) = val(v);         // v_q and d v_q / d a for the element loop
+    if (vjc >= 0) w.m(M_Q + Q_DV * nq + i) = der(v);
   }
+  drhonu = gp.sum(drhonu);
+  dpnu = gp.sum(dpnu);
+  fnu = gp.sum(fnu);
+  gp.sync();
   dpnu = dpnu / 3.0;
+  const double eta = Y(2), dc = Y(3), tc = Y(4), db = Y(5), tb = Y(6), dg = Y(7), tg = Y(8), y9 = Y(9);
+  const double dr = Y(ir), tr = Y(ir + 1), y_r2 = Y(ir + 2);
+  const double dq = Y(n - 2), tq = Y(n - 1);
   S rptQ = (1.0 + g.wQ) * g.rhoQ * m.grhom * m.ODE * tq * g.a2;
   S dgrho = m.grhom * (m.Oc * dc + m.Ob * db) * g.ia + (m.grhog * dg + m.grhor * (m.Neff * dr + m.Nmnu * drhonu)) * g.ia2 +
             m.grhom * m.ODE * dq * g.rhoQ * g.a2;
-  S dgpres = (m.grhog * dg + m.grhor * m.Neff * dr) * g.ia2 / 3.0 + m.grhor * m.Nmnu * dpnu * g.ia2 +
-             (m.cs2Q * m.grhom * m.ODE * dq * g.rhoQ * g.a2 + (m.cs2Q - g.ca2) * (3.0 * g.aH * rptQ * m.ik2));
+  S hp = (2.0 * k2 * eta + dgrho) * g.iaH;
   S dgtheta = m.grhom * (m.Oc * tc + m.Ob * tb) * g.ia + (4.0 / 3.0) * (m.grhog * tg + m.Neff * m.grhor * tr) * g.ia2 +
               m.Nmnu * m.grhor * k * fnu * g.ia2 + rptQ;
-  S hp = (2.0 * k2 * eta + dgrho) * g.iaH;
   S etap = 0.5 * dgtheta * m.ik2;
-  S alpha = (hp + 6.0 * etap) * 0.5 * m.ik2;
-  put(0, g.aH * g.a);
-  put(1, -(dgrho + 3.0 * dgpres) * g.a);
-  put(2, etap);
-  put(3, -tc - 0.5 * hp);
-  put(4, -g.aH * tc);
-  put(5, -tb - 0.5 * hp);
-  put(6, -g.aH * tb + k2 * g.cs2 * db + g.pb43 * g.opac * (tg - tb));
-  // photons, temperature (BLT11 2.4)
-  const double polter = y9 + Y(igp) + Y(igp + 2);
-  put(7, (4.0 / 3.0) * (-tg - 0.5 * hp));
-  put(8, k2 * (0.25 * dg - 0.5 * y9) - g.opac * (tg - tb));
-  put(9, (8.0 / 15.0) * (tg + k2 * alpha) - 0.6 * k * Y(10) - g.opac * (y9 - 0.1 * polter));
-  for (int l = 3; l < lg; ++l)
-    put(7 + l, k * (T.lo[l] * Y(6 + l) - T.up[l] * Y(8 + l)) - g.opac * Y(7 + l));
-  put(7 + lg, k * Y(6 + lg) - (lg + 1.0) * itau * Y(7 + lg) - g.opac * Y(7 + lg));
-  // photons, polarisation
-  put(igp, -k * Y(igp + 1) - g.opac * Y(igp) + g.opac * polter * 0.5);
-  put(igp + 1, k * (T.lo[1] * Y(igp) - T.up[1] * Y(igp + 2)) - g.opac * Y(igp + 1));
-  put(igp + 2, k * (T.lo[2] * Y(igp + 1) - T.up[2] * Y(igp + 3)) - g.opac * Y(igp + 2) + g.opac * polter * 0.1);
-  for (int l = 3; l < lgp; ++l)
-    put(igp + l, k * (T.lo[l] * Y(igp + l - 1) - T.up[l] * Y(igp + l + 1)) - g.opac * Y(igp + l));
-  put(igp + lgp, k * Y(igp + lgp - 1) - (lgp + 1.0) * itau * Y(igp + lgp) - g.opac * Y(igp + lgp));
-  // massless neutrinos
-  put(ir, (4.0 / 3.0) * (-tr - 0.5 * hp));
-  put(ir + 1, k2 * (0.25 * dr - 0.5 * y_r2));
-  put(ir + 2, (8.0 / 15.0) * (tr + k2 * alpha) - 0.6 * k * Y(ir + 3));
-  for (int l = 3; l < lr; ++l) w.v(vout, ir + l) = k * (T.lo[l] * Y(ir + l - 1) - T.up[l] * Y(ir + l + 1));
-  if (vjc >= 0) for (int l = 3; l < lr; ++l) w.v(vjc, ir + l) = 0.0;
-  put(ir + lr, S(k * Y(ir + lr - 1) - (lr + 1.0) * itau * Y(ir + lr)));
-  // massive neutrinos, l-major [l][q]
-  for (int i = 0; i < nq; ++i) {
-    S v = mk<S>(w.m(M_Q + i), vjc >= 0 ? w.m(M_Q + nq + i) : 0.0);
-    const double dlf = w.m(M_Q + 2 * nq + i);
-    S kv = k * v;
-    put(iq0 + i, -kv * Y(iq1 + i) + hp * dlf / 6.0);
-    put(iq1 + i, kv * (Y(iq0 + i) - 2.0 * Y(iq2 + i)) / 3.0);
-    put(iq2 + i, kv * (2.0 * Y(iq1 + i) - 3.0 * Y(iq3 + i)) / 5.0 - (hp / 15.0 + 0.4 * etap) * dlf);
-    for (int l = 3; l < lnu; ++l)
-      put(iq0 + l * nq + i, kv * (T.lo[l] * Y(iq0 + (l - 1) * nq + i) - T.up[l] * Y(iq0 + (l + 1) * nq + i)));
-    put(iq0 + lnu * nq + i, kv * Y(iq0 + (lnu - 1) * nq + i) - (lnu + 1.0) * itau * Y(iq0 + lnu * nq + i));
+  if (gp.lead()) {
+    S dgpres = (m.grhog * dg + m.grhor * m.Neff * dr) * g.ia2 / 3.0 + m.grhor * m.Nmnu * dpnu * g.ia2 +
+               (m.cs2Q * m.grhom * m.ODE * dq * g.rhoQ * g.a2 + (m.cs2Q - g.ca2) * (3.0 * g.aH * rptQ * m.ik2));
+    S alpha = (hp + 6.0 * etap) * 0.5 * m.ik2;
+    put(0, g.aH * g.a);
+    put(1, -(dgrho + 3.0 * dgpres) * g.a);
+    put(2, etap);
+    put(3, -tc - 0.5 * hp);
+    put(4, -g.aH * tc);
+    put(5, -tb - 0.5 * hp);
+    put(6, -g.aH * tb + k2 * g.cs2 * db + g.pb43 * g.opac * (tg - tb));
+    // photons, temperature (BLT11 2.4)
+    const double polter = y9 + Y(igp) + Y(igp + 2);
+    put(7, (4.0 / 3.0) * (-tg - 0.5 * hp));
+    put(8, k2 * (0.25 * dg - 0.5 * y9) - g.opac * (tg - tb));
+    put(9, (8.0 / 15.0) * (tg + k2 * alpha) - 0.6 * k * Y(10) - g.opac * (y9 - 0.1 * polter));
+    put(7 + lg, k * Y(6 + lg) - (lg + 1.0) * itau * Y(7 + lg) - g.opac * Y(7 + lg));
+    // photons, polarisation l = 0..2 and truncation
+    put(igp, -k * Y(igp + 1) - g.opac * Y(igp) + g.opac * polter * 0.5);
+    put(igp + 1, k * (T.lo[1] * Y(igp) - T.up[1] * Y(igp + 2)) - g.opac * Y(igp + 1));
+    put(igp + 2, k * (T.lo[2] * Y(igp + 1) - T.up[2] * Y(igp + 3)) - g.opac * Y(igp + 2) + g.opac * polter * 0.1);
+    put(igp + lgp, k * Y(igp + lgp - 1) - (lgp + 1.0) * itau * Y(igp + lgp) - g.opac * Y(igp + lgp));
+    // massless neutrinos l = 0..2 and truncation
+    put(ir, (4.0 / 3.0) * (-tr - 0.5 * hp));
+    put(ir + 1, k2 * (0.25 * dr - 0.5 * y_r2));
+    put(ir + 2, (8.0 / 15.0) * (tr + k2 * alpha) - 0.6 * k * Y(ir + 3));
+    put(ir + lr, S(k * Y(ir + lr - 1) - (lr + 1.0) * itau * Y(ir + lr)));
+    // dark-energy fluid (BL10 3.5, 3.6)
+    put(n - 2, -(1.0 + g.wQ) * (tq + 0.5 * hp) - 3.0 * (m.cs2Q - g.wQ) * g.aH * dq -
+                   9.0 * (1.0 + g.wQ) * (m.cs2Q - g.ca2) * g.aH * g.aH * m.ik2 * tq);
+    put(n - 1, -(1.0 - 3.0 * m.cs2Q) * g.aH * tq + m.cs2Q / (1.0 + g.wQ) * k2 * dq);
   }
-  // dark-energy fluid (BL10 3.5, 3.6)
-  put(n - 2, -(1.0 + g.wQ) * (tq + 0.5 * hp) - 3.0 * (m.cs2Q - g.wQ) * g.aH * dq -
-                 9.0 * (1.0 + g.wQ) * (m.cs2Q - g.ca2) * g.aH * g.aH * m.ik2 * tq);
-  put(n - 1, -(1.0 - 3.0 * m.cs2Q) * g.aH * tq + m.cs2Q / (1.0 + g.wQ) * k2 * dq);
+  for (int l = 3 + gp.lane; l < lg; l += G)
+    put(7 + l, k * (T.lo[l] * Y(6 + l) - T.up[l] * Y(8 + l)) - g.opac * Y(7 + l));
+  for (int l = 3 + gp.lane; l < lgp; l += G)
+    put(igp + l, k * (T.lo[l] * Y(igp + l - 1) - T.up[l] * Y(igp + l + 1)) - g.opac * Y(igp + l));
+  for (int l = 3 + gp.lane; l < lr; l += G) put(ir + l, S(k * (T.lo[l] * Y(ir + l - 1) - T.up[l] * Y(ir + l + 1))));
+  // massive neutrinos, l-major [l][q]
+  const int nmass = nq * (lnu + 1);
+  for (int e = gp.lane; e < nmass; e += G) {
+    const int l = e / nq, i = e - l * nq;
+    S v = mk<S>(w.m(M_Q + Q_V * nq + i), vjc >= 0 ? w.m(M_Q + Q_DV * nq + i) : 0.0);
+    S kv = k * v;
+    S f;
+    if (l == 0) {
+      f = -kv * Y(iq1 + i) + hp * w.m(M_Q + Q_DLF * nq + i) / 6.0;
+    } else if (l == 1) {
+      f = kv * (Y(iq0 + i) - 2.0 * Y(iq2 + i)) / 3.0;
+    } else if (l == 2) {
+      f = kv * (2.0 * Y(iq1 + i) - 3.0 * Y(iq3 + i)) / 5.0 - (hp / 15.0 + 0.4 * etap) * w.m(M_Q + Q_DLF * nq + i);
+    } else if (l < lnu) {
+      f = kv * (T.lo[l] * Y(iq0 + (l - 1) * nq + i) - T.up[l] * Y(iq0 + (l + 1) * nq + i));
+    } else {
+      f = kv * Y(iq0 + (lnu - 1) * nq + i) - (lnu + 1.0) * itau * Y(iq0 + lnu * nq + i);
+    }
+    put(iq0 + e, f);
+  }
+  gp.sync();
 }
-
 
 // ------------------------------------------------------------------ outputs
 // convert_to_output_variables (perturbations.py:374-523) of the state held in
 // vector vin; Friedmann aH from the tables, 20 fields to out[0..19*ostride].
+// Scalar work: called by one lane.
 HD void outputs(const Cosmo& c, const ModeConst& m, const Dims& D, const WS& w, int vin, double* out, long ostride) {
   const int nq = D.nq, iq0 = D.iq0, iq1 = iq0 + nq, n = D.n;
   const double k = m.k, k2 = m.k2;
@@ -412,10 +467,13 @@ HD void outputs(const Cosmo& c, const ModeConst& m, const Dims& D, const WS& w, 
 
 // ------------------------------------------------------------------ initial conditions
 // adiabatic_ics_one_mode (perturbations.py:526-627), written into vector vout.
-HD void initial_conditions(const Cosmo& c, const ModeConst& m, const Dims& D, double tau, const WS& w, int vout) {
+template <int G>
+HD void initial_conditions(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, double tau, const WS& w,
+                           int vout) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, iq1 = iq0 + nq, iq2 = iq1 + nq;
   const double k = m.k;
-  for (int j = 0; j < n; ++j) w.v(vout, j) = 0.0;
+  for (int j = gp.lane; j < n; j += G) w.v(vout, j) = 0.0;
+  gp.sync();
   const double a = spl_eval(c.sp[SP_A_TAU], tau);
   const double rn = exp(spl_eval(c.sp[SP_LRHONU_LOGA], log(a)));
   const double a4 = a * a * a * a;
@@ -435,16 +493,19 @@ HD void initial_conditions(const Cosmo& c, const ModeConst& m, const Dims& D, do
                      3.0 * (8.0 * fracnu * fracnu + 50.0 * fracnu + 275.0) / 20.0 / (2.0 * fracnu + 15.0) * tau * om) * ci;
   const double sr = (kt * kt) / (45.0 + 12.0 * fracnu) * (3.0 * s2 - 1.0) *
                     (1.0 + (4.0 * fracnu - 5.0) / 4.0 / (2.0 * fracnu + 15.0) * tau * om) * ci;
-  const double wQ = m.w0 + m.wa * (1.0 - a);
-  const double dq = (kt * kt) / 4.0 * (1.0 + wQ) * (4.0 - 3.0 * m.cs2Q) / (4.0 - 6.0 * wQ + 3.0 * m.cs2Q) * ci * s2;
-  const double tq = (kt * kt * kt * kt) / tau / 4.0 * m.cs2Q / (4.0 - 6.0 * wQ + 3.0 * m.cs2Q) * ci * s2;
-  const double eta = ci * (1.0 - (kt * kt) / 12.0 / (15.0 + 4.0 * fracnu) *
-                                     (5.0 + 4.0 * s2 * fracnu -
-                                      (16.0 * fracnu * fracnu + 280.0 * fracnu + 325.0) / 10.0 / (2.0 * fracnu + 15.0) * tau * om));
-  w.v(vout, 0) = a; w.v(vout, 2) = eta; w.v(vout, 3) = 0.75 * dg;
-  w.v(vout, 5) = 0.75 * dg; w.v(vout, 6) = tg; w.v(vout, 7) = dg; w.v(vout, 8) = tg;
-  w.v(vout, D.ir) = dr; w.v(vout, D.ir + 1) = tr; w.v(vout, D.ir + 2) = sr * 2.0;
-  for (int i = 0; i < nq; ++i) {
+  if (gp.lead()) {
+    const double wQ = m.w0 + m.wa * (1.0 - a);
+    const double dq = (kt * kt) / 4.0 * (1.0 + wQ) * (4.0 - 3.0 * m.cs2Q) / (4.0 - 6.0 * wQ + 3.0 * m.cs2Q) * ci * s2;
+    const double tq = (kt * kt * kt * kt) / tau / 4.0 * m.cs2Q / (4.0 - 6.0 * wQ + 3.0 * m.cs2Q) * ci * s2;
+    const double eta = ci * (1.0 - (kt * kt) / 12.0 / (15.0 + 4.0 * fracnu) *
+                                       (5.0 + 4.0 * s2 * fracnu -
+                                        (16.0 * fracnu * fracnu + 280.0 * fracnu + 325.0) / 10.0 / (2.0 * fracnu + 15.0) * tau * om));
+    w.v(vout, 0) = a; w.v(vout, 2) = eta; w.v(vout, 3) = 0.75 * dg;
+    w.v(vout, 5) = 0.75 * dg; w.v(vout, 6) = tg; w.v(vout, 7) = dg; w.v(vout, 8) = tg;
+    w.v(vout, D.ir) = dr; w.v(vout, D.ir + 1) = tr; w.v(vout, D.ir + 2) = sr * 2.0;
+    w.v(vout, n - 2) = dq; w.v(vout, n - 1) = tq;
+  }
+  for (int i = gp.lane; i < nq; i += G) {
     const double q = LDG(c.q + i);
     const double aq = a * m.amnu / q;
     const double v = 1.0 / sqrt(1.0 + aq * aq);
@@ -454,10 +515,11 @@ HD void initial_conditions(const Cosmo& c, const ModeConst& m, const Dims& D, do
     w.v(vout, iq2 + i) = -0.5 * dlf * sr;
     w.m(M_Q + Q_DLF * nq + i) = dlf;
   }
-  w.v(vout, n - 2) = dq; w.v(vout, n - 1) = tq;
+  gp.sync();
 }
 
-// determine_starting_time (perturbations.py:630-681) with root_find_bisect (util.py:365-396)
+// determine_starting_time (perturbations.py:630-681) with root_find_bisect
+// (util.py:365-396).  Scalar; every lane computes the same value.
 HD double start_time(const Cosmo& c, const ModeConst& m) {
   const double small_k = 0.0004, large_k = 0.07;
   const double tau0 = hdr(c, H_TAUMIN);
@@ -490,16 +552,14 @@ HD double start_time(const Cosmo& c, const ModeConst& m) {
 }
 
 // ------------------------------------------------------------------ structured factorization
-// Chain coefficients of M = d I - B (see file header).  A chain is the list
-// of indices start, start+stride, ... ; LO[i] = M[i, prev], UP[i] = M[i, next].
+// Chains of M = d I - B (see file header).  A chain is the list of indices
+// start, start+stride, ... ; LO[i] = M[i, prev], UP[i] = M[i, next].
 // Bottom-up elimination: p_last = M_ii, p_i = M_ii - UP_i LO_next / p_next,
-// PI = 1/p.  All chain pivots are >= d > 0: the products UP_i LO_next are
-// negative for every free-streaming hierarchy and the diagonal damping
-// (opacity, truncation (l+1)/tau) is non-negative.
-struct StepScal {
-  double d, dt, t0;
-};
-
+// PI = 1/p.  Every chain pivot is >= d > 0: UP_i LO_next < 0 for every
+// free-streaming hierarchy and the diagonal damping (opacity, truncation
+// (l+1)/tau) is non-negative.
+// Chain numbering: 0 massless nu, 1..nq massive nu q-1, nq+1 photon T tail
+// (l >= 3, attached to T2 = index 9), nq+2 photon P tail (attached to P2).
 HD void chain_pivots(const WS& w, int start, int stride, int cnt, double d_last, double d_rest) {
   int i = start + (cnt - 1) * stride;
   double pinv = 1.0 / d_last;
@@ -509,6 +569,40 @@ HD void chain_pivots(const WS& w, int start, int stride, int cnt, double d_last,
     const double p = d_rest - w.v(V_UP, ii) * w.v(V_LO, ii + stride) * pinv;
     pinv = 1.0 / p;
     w.v(V_PI, ii) = pinv;
+  }
+}
+
+HD void chain_fill_factor(const ModeConst& m, const Dims& D, const Tab& T, const WS& w, double d, double itau, double op,
+                          int ch) {
+  const int nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
+  const double k = m.k, k2 = m.k2;
+  if (ch == 0) {
+    w.v(V_UP, ir) = 4.0 / 3.0;
+    w.v(V_LO, ir + 1) = -0.25 * k2; w.v(V_UP, ir + 1) = 0.5 * k2;
+    w.v(V_LO, ir + 2) = -8.0 / 15.0; w.v(V_UP, ir + 2) = 0.6 * k;
+    for (int l = 3; l < lr; ++l) { w.v(V_LO, ir + l) = -k * T.lo[l]; w.v(V_UP, ir + l) = k * T.up[l]; }
+    w.v(V_LO, ir + lr) = -k;
+    chain_pivots(w, ir, 1, lr + 1, d + (lr + 1.0) * itau, d);
+  } else if (ch <= nq) {
+    const int i = ch - 1;
+    const double kv = k * w.m(M_Q + Q_V * nq + i);
+    for (int l = 0; l < lnu; ++l) {
+      const int e = iq0 + l * nq + i;
+      if (l > 0) w.v(V_LO, e) = -kv * T.lo[l];
+      w.v(V_UP, e) = kv * T.up[l];
+    }
+    w.v(V_LO, iq0 + lnu * nq + i) = -kv;
+    chain_pivots(w, iq0 + i, nq, lnu + 1, d + (lnu + 1.0) * itau, d);
+  } else if (ch == nq + 1) {
+    w.v(V_UP, 9) = 0.6 * k;
+    for (int l = 3; l < lg; ++l) { w.v(V_LO, 7 + l) = -k * T.lo[l]; w.v(V_UP, 7 + l) = k * T.up[l]; }
+    w.v(V_LO, 7 + lg) = -k;
+    chain_pivots(w, 10, 1, lg - 2, d + op + (lg + 1.0) * itau, d + op);
+  } else {
+    w.v(V_UP, igp + 2) = 0.6 * k;
+    for (int l = 3; l < lgp; ++l) { w.v(V_LO, igp + l) = -k * T.lo[l]; w.v(V_UP, igp + l) = k * T.up[l]; }
+    w.v(V_LO, igp + lgp) = -k;
+    chain_pivots(w, igp + 3, 1, lgp - 2, d + op + (lgp + 1.0) * itau, d + op);
   }
 }
 
@@ -545,234 +639,239 @@ HD void small_solve(const WS& w, int off, int pivoff, double* r) {
   for (int i = N - 1; i >= 0; --i) { double s = r[i]; for (int j = i + 1; j < N; ++j) s -= w.m(off + i * N + j) * r[j]; r[i] = s / w.m(off + i * N + i); }
 }
 
-// Fill LO/UP for all chains, the core and DE blocks, and factor M.  Uses the
-// background at (t0, y0) in g; vq (v_q values) must be in MISC.
-HD void factor_M(const ModeConst& m, const Dims& D, const Tab& T, const WS& w, double d, double tau, const Bg<double>& g) {
-  const int nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
-  const double k = m.k, k2 = m.k2, itau = 1.0 / tau, op = g.opac;
-  // massless neutrinos r0..r_lr
-  w.v(V_UP, ir) = 4.0 / 3.0;
-  w.v(V_LO, ir + 1) = -0.25 * k2; w.v(V_UP, ir + 1) = 0.5 * k2;
-  w.v(V_LO, ir + 2) = -8.0 / 15.0; w.v(V_UP, ir + 2) = 0.6 * k;
-  for (int l = 3; l < lr; ++l) { w.v(V_LO, ir + l) = -k * T.lo[l]; w.v(V_UP, ir + l) = k * T.up[l]; }
-  w.v(V_LO, ir + lr) = -k;
-  chain_pivots(w, ir, 1, lr + 1, d + (lr + 1.0) * itau, d);
-  // massive neutrinos, chain q: iq0 + l*nq + q
-  for (int i = 0; i < nq; ++i) {
-    const double kv = k * w.m(M_Q + Q_V * nq + i);
-    for (int l = 0; l < lnu; ++l) {
-      const int e = iq0 + l * nq + i;
-      if (l > 0) w.v(V_LO, e) = -kv * T.lo[l];
-      w.v(V_UP, e) = kv * T.up[l];
-    }
-    w.v(V_LO, iq0 + lnu * nq + i) = -kv;
-    chain_pivots(w, iq0 + i, nq, lnu + 1, d + (lnu + 1.0) * itau, d);
-  }
-  // photon temperature tail T3..T_lg attached to T2 (index 9)
-  w.v(V_UP, 9) = 0.6 * k;
-  for (int l = 3; l < lg; ++l) { w.v(V_LO, 7 + l) = -k * T.lo[l]; w.v(V_UP, 7 + l) = k * T.up[l]; }
-  w.v(V_LO, 7 + lg) = -k;
-  chain_pivots(w, 10, 1, lg - 2, d + op + (lg + 1.0) * itau, d + op);
-  // photon polarisation tail P3..P_lgp attached to P2
-  w.v(V_UP, igp + 2) = 0.6 * k;
-  for (int l = 3; l < lgp; ++l) { w.v(V_LO, igp + l) = -k * T.lo[l]; w.v(V_UP, igp + l) = k * T.up[l]; }
-  w.v(V_LO, igp + lgp) = -k;
-  chain_pivots(w, igp + 3, 1, lgp - 2, d + op + (lgp + 1.0) * itau, d + op);
-  // 8x8 photon-baryon core: db, tb, dg, tg, T2, P0, P1, P2
-  for (int i = 0; i < 64; ++i) w.m(M_CORE + i) = 0.0;
-#define CM(r, c_) w.m(M_CORE + (r) * 8 + (c_))
-  CM(0, 0) = d; CM(0, 1) = 1.0;
-  CM(1, 0) = -k2 * g.cs2; CM(1, 1) = d + g.aH + g.pb43 * op; CM(1, 3) = -g.pb43 * op;
-  CM(2, 2) = d; CM(2, 3) = 4.0 / 3.0;
-  CM(3, 1) = -op; CM(3, 2) = -0.25 * k2; CM(3, 3) = d + op; CM(3, 4) = 0.5 * k2;
-  CM(4, 3) = -8.0 / 15.0; CM(4, 4) = d + 0.9 * op - w.v(V_UP, 9) * w.v(V_LO, 10) * w.v(V_PI, 10);
-  CM(4, 5) = -0.1 * op; CM(4, 7) = -0.1 * op;
-  CM(5, 4) = -0.5 * op; CM(5, 5) = d + 0.5 * op; CM(5, 6) = k; CM(5, 7) = -0.5 * op;
-  CM(6, 5) = -k * T.lo[1]; CM(6, 6) = d + op; CM(6, 7) = k * T.up[1];
-  CM(7, 4) = -0.1 * op; CM(7, 5) = -0.1 * op; CM(7, 6) = -k * T.lo[2];
-  CM(7, 7) = d + 0.9 * op - w.v(V_UP, igp + 2) * w.v(V_LO, igp + 3) * w.v(V_PI, igp + 3);
-#undef CM
-  small_lu<8>(w, M_CORE, M_CPIV);
-  // dark energy 2x2 (rows n-2, n-1)
-  const double wQ = g.wQ, cs2Q = m.cs2Q;
-  w.m(M_DE + 0) = d + 3.0 * (cs2Q - wQ) * g.aH;
-  w.m(M_DE + 1) = (1.0 + wQ) + 9.0 * (1.0 + wQ) * (cs2Q - g.ca2) * g.aH * g.aH * m.ik2;
-  w.m(M_DE + 2) = -cs2Q / (1.0 + wQ) * k2;
-  w.m(M_DE + 3) = d + (1.0 - 3.0 * cs2Q) * g.aH;
-  {
-    // LU with partial pivoting; M_DE+4 = 1 if rows swapped
-    double a00 = w.m(M_DE + 0), a01 = w.m(M_DE + 1), a10 = w.m(M_DE + 2), a11 = w.m(M_DE + 3);
+// entries of the 8x8 photon-baryon core of M (db, tb, dg, tg, T2, P0, P1, P2)
+// and of the 2x2 dark-energy block, before the tail folds
+HD void core_entries(const ModeConst& m, const Tab& T, const Bg<double>& g, double d, double* core, double* de) {
+  const double k = m.k, k2 = m.k2, op = g.opac;
+  for (int i = 0; i < 64; ++i) core[i] = 0.0;
+  core[0] = d; core[1] = 1.0;
+  core[8] = -k2 * g.cs2; core[9] = d + g.aH + g.pb43 * op; core[11] = -g.pb43 * op;
+  core[18] = d; core[19] = 4.0 / 3.0;
+  core[25] = -op; core[26] = -0.25 * k2; core[27] = d + op; core[28] = 0.5 * k2;
+  core[35] = -8.0 / 15.0; core[36] = d + 0.9 * op; core[37] = -0.1 * op; core[39] = -0.1 * op;
+  core[44] = -0.5 * op; core[45] = d + 0.5 * op; core[46] = k; core[47] = -0.5 * op;
+  core[53] = -k * T.lo[1]; core[54] = d + op; core[55] = k * T.up[1];
+  core[60] = -0.1 * op; core[61] = -0.1 * op; core[62] = -k * T.lo[2]; core[63] = d + 0.9 * op;
+  de[0] = d + 3.0 * (m.cs2Q - g.wQ) * g.aH;
+  de[1] = (1.0 + g.wQ) + 9.0 * (1.0 + g.wQ) * (m.cs2Q - g.ca2) * g.aH * g.aH * m.ik2;
+  de[2] = -m.cs2Q / (1.0 + g.wQ) * k2;
+  de[3] = d + (1.0 - 3.0 * m.cs2Q) * g.aH;
+}
+
+// Fill chain coefficients and factor M (chains per lane; core and DE on the
+// leading lane).  Needs v_q in MISC (written by the RHS at this a).
+template <int G>
+HD void factor_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab& T, const WS& w, double d, double tau,
+                 const Bg<double>& g) {
+  const int nq = D.nq, igp = D.igp;
+  const double itau = 1.0 / tau, op = g.opac;
+  for (int ch = gp.lane; ch < nq + 3; ch += G) chain_fill_factor(m, D, T, w, d, itau, op, ch);
+  gp.sync();
+  if (gp.lead()) {
+    double core[64], de[4];
+    core_entries(m, T, g, d, core, de);
+    core[36] -= w.v(V_UP, 9) * w.v(V_LO, 10) * w.v(V_PI, 10);
+    core[63] -= w.v(V_UP, igp + 2) * w.v(V_LO, igp + 3) * w.v(V_PI, igp + 3);
+    for (int i = 0; i < 64; ++i) w.m(M_CORE + i) = core[i];
+    small_lu<8>(w, M_CORE, M_CPIV);
+    // dark energy 2x2 (rows n-2, n-1): LU with partial pivoting, M_DE+4 = 1 if swapped
+    double a00 = de[0], a01 = de[1], a10 = de[2], a11 = de[3];
     double sw = 0.0;
     if (fabs(a10) > fabs(a00)) { double t0_ = a00, t1_ = a01; a00 = a10; a01 = a11; a10 = t0_; a11 = t1_; sw = 1.0; }
     const double l = a10 / a00;
     w.m(M_DE + 0) = a00; w.m(M_DE + 1) = a01; w.m(M_DE + 2) = l; w.m(M_DE + 3) = a11 - l * a01; w.m(M_DE + 4) = sw;
   }
+  gp.sync();
 }
 
-// z = M^{-1} r on indices >= 2, in place on vector vr.
-HD void solve_M(const ModeConst& m, const Dims& D, const WS& w, double d, double aH, int vr) {
+// z = M^{-1} r on indices >= 2, in place on vector vr.  Expects vr synced.
+template <int G>
+HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS& w, double d, double aH, int vr) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
-  const double id = 1.0 / d;
-  // eta
-  w.v(vr, 2) = w.v(vr, 2) * id;
-  // CDM: [[d, 1], [0, d + aH]]
-  {
-    const double z4 = w.v(vr, 4) / (d + aH);
+  (void)m;
+  if (gp.lead()) {
+    const double id = 1.0 / d;
+    w.v(vr, 2) = w.v(vr, 2) * id;                      // eta
+    const double z4 = w.v(vr, 4) / (d + aH);           // CDM [[d, 1], [0, d + aH]]
     w.v(vr, 4) = z4;
     w.v(vr, 3) = (w.v(vr, 3) - z4) * id;
-  }
-  // DE
-  {
-    double r0 = w.v(vr, n - 2), r1 = w.v(vr, n - 1);
+    double r0 = w.v(vr, n - 2), r1 = w.v(vr, n - 1);   // DE
     if (w.m(M_DE + 4) != 0.0) { double t = r0; r0 = r1; r1 = t; }
     r1 -= w.m(M_DE + 2) * r0;
     const double z1 = r1 / w.m(M_DE + 3);
     const double z0 = (r0 - w.m(M_DE + 1) * z1) / w.m(M_DE + 0);
     w.v(vr, n - 2) = z0; w.v(vr, n - 1) = z1;
   }
-  // full chains: massless, massive
-  auto full_chain = [&](int start, int stride, int cnt) {
-    for (int j = cnt - 2; j >= 0; --j) {
-      const int i = start + j * stride;
-      w.v(vr, i) -= w.v(V_UP, i) * w.v(vr, i + stride) * w.v(V_PI, i + stride);
+  for (int ch = gp.lane; ch < nq + 3; ch += G) {
+    if (ch <= nq) {
+      // full chain: forward sweep from the top, then back substitution from l = 0
+      const int start = ch == 0 ? ir : iq0 + ch - 1;
+      const int stride = ch == 0 ? 1 : nq;
+      const int cnt = ch == 0 ? lr + 1 : lnu + 1;
+      for (int j = cnt - 2; j >= 0; --j) {
+        const int i = start + j * stride;
+        w.v(vr, i) -= w.v(V_UP, i) * w.v(vr, i + stride) * w.v(V_PI, i + stride);
+      }
+      double z = w.v(vr, start) * w.v(V_PI, start);
+      w.v(vr, start) = z;
+      for (int j = 1; j < cnt; ++j) {
+        const int i = start + j * stride;
+        z = (w.v(vr, i) - w.v(V_LO, i) * z) * w.v(V_PI, i);
+        w.v(vr, i) = z;
+      }
+    } else {
+      // tail forward sweep up to the attach point
+      const int start = ch == nq + 1 ? 10 : igp + 3;
+      const int cnt = ch == nq + 1 ? lg - 2 : lgp - 2;
+      const int attach = start - 1;
+      for (int j = cnt - 2; j >= 0; --j) {
+        const int i = start + j;
+        w.v(vr, i) -= w.v(V_UP, i) * w.v(vr, i + 1) * w.v(V_PI, i + 1);
+      }
+      w.v(vr, attach) -= w.v(V_UP, attach) * w.v(vr, start) * w.v(V_PI, start);
     }
-    double z = w.v(vr, start) * w.v(V_PI, start);
-    w.v(vr, start) = z;
-    for (int j = 1; j < cnt; ++j) {
-      const int i = start + j * stride;
-      z = (w.v(vr, i) - w.v(V_LO, i) * z) * w.v(V_PI, i);
-      w.v(vr, i) = z;
-    }
-  };
-  full_chain(ir, 1, lr + 1);
-  for (int i = 0; i < nq; ++i) full_chain(iq0 + i, nq, lnu + 1);
-  // tails: forward sweep up to the attach point
-  auto tail_fwd = [&](int start, int cnt, int attach) {
-    for (int j = cnt - 2; j >= 0; --j) {
-      const int i = start + j;
-      w.v(vr, i) -= w.v(V_UP, i) * w.v(vr, i + 1) * w.v(V_PI, i + 1);
-    }
-    w.v(vr, attach) -= w.v(V_UP, attach) * w.v(vr, start) * w.v(V_PI, start);
-  };
-  auto tail_back = [&](int start, int cnt, int attach) {
-    double z = w.v(vr, attach);
+  }
+  gp.sync();
+  if (gp.lead()) {
+    double r[8] = {w.v(vr, 5), w.v(vr, 6), w.v(vr, 7), w.v(vr, 8), w.v(vr, 9), w.v(vr, igp), w.v(vr, igp + 1), w.v(vr, igp + 2)};
+    small_solve<8>(w, M_CORE, M_CPIV, r);
+    w.v(vr, 5) = r[0]; w.v(vr, 6) = r[1]; w.v(vr, 7) = r[2]; w.v(vr, 8) = r[3]; w.v(vr, 9) = r[4];
+    w.v(vr, igp) = r[5]; w.v(vr, igp + 1) = r[6]; w.v(vr, igp + 2) = r[7];
+  }
+  gp.sync();
+  for (int t = gp.lane; t < 2; t += G) {
+    const int start = t == 0 ? 10 : igp + 3;
+    const int cnt = t == 0 ? lg - 2 : lgp - 2;
+    double z = w.v(vr, start - 1);
     for (int j = 0; j < cnt; ++j) {
       const int i = start + j;
       z = (w.v(vr, i) - w.v(V_LO, i) * z) * w.v(V_PI, i);
       w.v(vr, i) = z;
     }
-  };
-  tail_fwd(10, lg - 2, 9);
-  tail_fwd(igp + 3, lgp - 2, igp + 2);
-  double r[8] = {w.v(vr, 5), w.v(vr, 6), w.v(vr, 7), w.v(vr, 8), w.v(vr, 9), w.v(vr, igp), w.v(vr, igp + 1), w.v(vr, igp + 2)};
-  small_solve<8>(w, M_CORE, M_CPIV, r);
-  w.v(vr, 5) = r[0]; w.v(vr, 6) = r[1]; w.v(vr, 7) = r[2]; w.v(vr, 8) = r[3]; w.v(vr, 9) = r[4];
-  w.v(vr, igp) = r[5]; w.v(vr, igp + 1) = r[6]; w.v(vr, igp + 2) = r[7];
-  tail_back(10, lg - 2, 9);
-  tail_back(igp + 3, lgp - 2, igp + 2);
+  }
+  gp.sync();
 }
 
-// g_h . v and g_e . v (the metric functionals h', eta' as rows)
-HD void functionals(const Dims& D, const WS& w, int vr, double& sh, double& se) {
+// g_h . v and g_e . v (the metric functionals h', eta' as rows); all lanes get the sums
+template <int G>
+HD void functionals(const Grp<G>& gp, const Dims& D, const WS& w, int vr, double& sh, double& se) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
-  double h = w.m(M_SCAL + S_GH2) * w.v(vr, 2) + w.m(M_SCAL + S_GH3) * w.v(vr, 3) + w.m(M_SCAL + S_GH5) * w.v(vr, 5) +
-             w.m(M_SCAL + S_GH7) * w.v(vr, 7) + w.m(M_SCAL + S_GHR0) * w.v(vr, ir) + w.m(M_SCAL + S_GHQE) * w.v(vr, n - 2);
-  double e = w.m(M_SCAL + S_GE4) * w.v(vr, 4) + w.m(M_SCAL + S_GE6) * w.v(vr, 6) + w.m(M_SCAL + S_GE8) * w.v(vr, 8) +
-             w.m(M_SCAL + S_GER1) * w.v(vr, ir + 1) + w.m(M_SCAL + S_GEQE) * w.v(vr, n - 1);
-  for (int i = 0; i < nq; ++i) {
+  double h = 0.0, e = 0.0;
+  if (gp.lead()) {
+    h = w.m(M_SCAL + S_GH2) * w.v(vr, 2) + w.m(M_SCAL + S_GH3) * w.v(vr, 3) + w.m(M_SCAL + S_GH5) * w.v(vr, 5) +
+        w.m(M_SCAL + S_GH7) * w.v(vr, 7) + w.m(M_SCAL + S_GHR0) * w.v(vr, ir) + w.m(M_SCAL + S_GHQE) * w.v(vr, n - 2);
+    e = w.m(M_SCAL + S_GE4) * w.v(vr, 4) + w.m(M_SCAL + S_GE6) * w.v(vr, 6) + w.m(M_SCAL + S_GE8) * w.v(vr, 8) +
+        w.m(M_SCAL + S_GER1) * w.v(vr, ir + 1) + w.m(M_SCAL + S_GEQE) * w.v(vr, n - 1);
+  }
+  for (int i = gp.lane; i < nq; i += G) {
     h += w.m(M_Q + Q_GH * nq + i) * w.v(vr, iq0 + i);
     e += w.m(M_Q + Q_GE * nq + i) * w.v(vr, iq0 + nq + i);
   }
-  sh = h; se = e;
+  sh = gp.sum(h);
+  se = gp.sum(e);
 }
 
-// Per-step factorization of W = d I - J at (t0, y0).  Needs: JC0 (d f/d a),
-// background g at a0, v_q in MISC.  Writes LO/UP/PI, core/DE LU, ZH, ZE,
-// capacitance inverse and the sparse row-1 / functional coefficients.
-HD void factor_W(const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, const WS& w, double d, double tau, const Bg<double>& g) {
+// Per-step factorization of W = d I - J at (t0, y0).  Needs JC0 (d f/d a),
+// the background g at a0 and v_q in MISC.  Writes LO/UP/PI, core/DE LU, ZH,
+// ZE, the capacitance inverse and the sparse row-1 / functional coefficients.
+template <int G>
+HD void factor_W(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, const WS& w,
+                 double d, double tau, const Bg<double>& g) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
-  const double a = g.a;
-  w.m(M_SCAL + S_D) = d;
-  w.m(M_SCAL + S_W00I) = 1.0 / (d - w.v(V_JC0, 0));
-  factor_M(m, D, T, w, d, tau, g);
-  // functional coefficients (d h'/d y and d eta'/d y)
-  const double iaH = g.iaH;
-  w.m(M_SCAL + S_GH2) = 2.0 * m.k2 * iaH;
-  w.m(M_SCAL + S_GH3) = m.grhom * m.Oc * g.ia * iaH;
-  w.m(M_SCAL + S_GH5) = m.grhom * m.Ob * g.ia * iaH;
-  w.m(M_SCAL + S_GH7) = m.grhog * g.ia2 * iaH;
-  w.m(M_SCAL + S_GHR0) = m.grhor * m.Neff * g.ia2 * iaH;
-  w.m(M_SCAL + S_GHQE) = m.grhom * m.ODE * g.rhoQ * g.a2 * iaH;
-  const double h2 = 0.5 * m.ik2;
-  w.m(M_SCAL + S_GE4) = m.grhom * m.Oc * g.ia * h2;
-  w.m(M_SCAL + S_GE6) = m.grhom * m.Ob * g.ia * h2;
-  w.m(M_SCAL + S_GE8) = (4.0 / 3.0) * m.grhog * g.ia2 * h2;
-  w.m(M_SCAL + S_GER1) = (4.0 / 3.0) * m.Neff * m.grhor * g.ia2 * h2;
-  w.m(M_SCAL + S_GEQE) = (1.0 + g.wQ) * g.rhoQ * m.grhom * m.ODE * g.a2 * h2;
-  // row 1: J[1, j] = -a (d dgrho/d y_j + 3 d dgpres/d y_j)
-  w.m(M_SCAL + S_R13) = -m.grhom * m.Oc;
-  w.m(M_SCAL + S_R15) = -m.grhom * m.Ob;
-  w.m(M_SCAL + S_R17) = -2.0 * m.grhog * g.ia;
-  w.m(M_SCAL + S_R1R0) = -2.0 * m.grhor * m.Neff * g.ia;
-  w.m(M_SCAL + S_R1QE) = -m.grhom * m.ODE * g.rhoQ * g.a2 * a * (1.0 + 3.0 * m.cs2Q);
-  w.m(M_SCAL + S_R1QT) = -9.0 * (m.cs2Q - g.ca2) * g.aH * (1.0 + g.wQ) * g.rhoQ * m.grhom * m.ODE * g.a2 * a * m.ik2;
-  for (int i = 0; i < nq; ++i) {
+  const double a = g.a, iaH = g.iaH, h2 = 0.5 * m.ik2;
+  if (gp.lead()) {
+    w.m(M_SCAL + S_D) = d;
+    w.m(M_SCAL + S_W00I) = 1.0 / (d - w.v(V_JC0, 0));
+    // functional coefficients (d h'/d y and d eta'/d y)
+    w.m(M_SCAL + S_GH2) = 2.0 * m.k2 * iaH;
+    w.m(M_SCAL + S_GH3) = m.grhom * m.Oc * g.ia * iaH;
+    w.m(M_SCAL + S_GH5) = m.grhom * m.Ob * g.ia * iaH;
+    w.m(M_SCAL + S_GH7) = m.grhog * g.ia2 * iaH;
+    w.m(M_SCAL + S_GHR0) = m.grhor * m.Neff * g.ia2 * iaH;
+    w.m(M_SCAL + S_GHQE) = m.grhom * m.ODE * g.rhoQ * g.a2 * iaH;
+    w.m(M_SCAL + S_GE4) = m.grhom * m.Oc * g.ia * h2;
+    w.m(M_SCAL + S_GE6) = m.grhom * m.Ob * g.ia * h2;
+    w.m(M_SCAL + S_GE8) = (4.0 / 3.0) * m.grhog * g.ia2 * h2;
+    w.m(M_SCAL + S_GER1) = (4.0 / 3.0) * m.Neff * m.grhor * g.ia2 * h2;
+    w.m(M_SCAL + S_GEQE) = (1.0 + g.wQ) * g.rhoQ * m.grhom * m.ODE * g.a2 * h2;
+    // row 1: J[1, j] = -a (d dgrho/d y_j + 3 d dgpres/d y_j)
+    w.m(M_SCAL + S_R13) = -m.grhom * m.Oc;
+    w.m(M_SCAL + S_R15) = -m.grhom * m.Ob;
+    w.m(M_SCAL + S_R17) = -2.0 * m.grhog * g.ia;
+    w.m(M_SCAL + S_R1R0) = -2.0 * m.grhor * m.Neff * g.ia;
+    w.m(M_SCAL + S_R1QE) = -m.grhom * m.ODE * g.rhoQ * g.a2 * a * (1.0 + 3.0 * m.cs2Q);
+    w.m(M_SCAL + S_R1QT) = -9.0 * (m.cs2Q - g.ca2) * g.aH * (1.0 + g.wQ) * g.rhoQ * m.grhom * m.ODE * g.a2 * a * m.ik2;
+  }
+  for (int i = gp.lane; i < nq; i += G) {
     const double v = w.m(M_Q + Q_V * nq + i);
     const double wq = LDG(c.w + i);
     w.m(M_Q + Q_GH * nq + i) = m.grhor * m.Nmnu * wq / v * g.ia2 * iaH;
     w.m(M_Q + Q_GE * nq + i) = m.Nmnu * m.grhor * m.k * wq * g.ia2 * h2;
     w.m(M_Q + Q_R1 * nq + i) = -m.grhor * m.Nmnu * wq * (1.0 / v + v) * g.ia;
   }
+  for (int j = gp.lane; j < n; j += G) { w.v(V_ZH, j) = 0.0; w.v(V_ZE, j) = 0.0; }
+  factor_M<G>(gp, m, D, T, w, d, tau, g);   // syncs
   // u_h into ZH, u_e into ZE (sparse), then M^{-1}
-  for (int j = 0; j < n; ++j) { w.v(V_ZH, j) = 0.0; w.v(V_ZE, j) = 0.0; }
-  w.v(V_ZH, 3) = -0.5; w.v(V_ZH, 5) = -0.5; w.v(V_ZH, 7) = -2.0 / 3.0; w.v(V_ZH, 9) = 4.0 / 15.0;
-  w.v(V_ZH, ir) = -2.0 / 3.0; w.v(V_ZH, ir + 2) = 4.0 / 15.0; w.v(V_ZH, n - 2) = -0.5 * (1.0 + g.wQ);
-  w.v(V_ZE, 2) = 1.0; w.v(V_ZE, 9) = 1.6; w.v(V_ZE, ir + 2) = 1.6;
-  for (int i = 0; i < nq; ++i) {
+  if (gp.lead()) {
+    w.v(V_ZH, 3) = -0.5; w.v(V_ZH, 5) = -0.5; w.v(V_ZH, 7) = -2.0 / 3.0; w.v(V_ZH, 9) = 4.0 / 15.0;
+    w.v(V_ZH, ir) = -2.0 / 3.0; w.v(V_ZH, ir + 2) = 4.0 / 15.0; w.v(V_ZH, n - 2) = -0.5 * (1.0 + g.wQ);
+    w.v(V_ZE, 2) = 1.0; w.v(V_ZE, 9) = 1.6; w.v(V_ZE, ir + 2) = 1.6;
+  }
+  for (int i = gp.lane; i < nq; i += G) {
     const double dlf = w.m(M_Q + Q_DLF * nq + i);
     w.v(V_ZH, iq0 + i) = dlf / 6.0;
     w.v(V_ZH, iq0 + 2 * nq + i) = -dlf / 15.0;
     w.v(V_ZE, iq0 + 2 * nq + i) = -0.4 * dlf;
   }
-  solve_M(m, D, w, d, g.aH, V_ZH);
-  solve_M(m, D, w, d, g.aH, V_ZE);
+  gp.sync();
+  solve_M<G>(gp, m, D, w, d, g.aH, V_ZH);
+  solve_M<G>(gp, m, D, w, d, g.aH, V_ZE);
   double hh, eh, he, ee;
-  functionals(D, w, V_ZH, hh, eh);
-  functionals(D, w, V_ZE, he, ee);
+  functionals<G>(gp, D, w, V_ZH, hh, eh);
+  functionals<G>(gp, D, w, V_ZE, he, ee);
   // C = I - G^T Z = [[1 - hh, -he], [-eh, 1 - ee]]
-  const double c00 = 1.0 - hh, c01 = -he, c10 = -eh, c11 = 1.0 - ee;
-  const double idet = 1.0 / (c00 * c11 - c01 * c10);
-  w.m(M_CINV + 0) = c11 * idet; w.m(M_CINV + 1) = -c01 * idet;
-  w.m(M_CINV + 2) = -c10 * idet; w.m(M_CINV + 3) = c00 * idet;
+  if (gp.lead()) {
+    const double c00 = 1.0 - hh, c01 = -he, c10 = -eh, c11 = 1.0 - ee;
+    const double idet = 1.0 / (c00 * c11 - c01 * c10);
+    w.m(M_CINV + 0) = c11 * idet; w.m(M_CINV + 1) = -c01 * idet;
+    w.m(M_CINV + 2) = -c10 * idet; w.m(M_CINV + 3) = c00 * idet;
+  }
+  gp.sync();
 }
 
-// x = W^{-1} b in place on vector vb.
-HD void solve_W(const ModeConst& m, const Dims& D, const WS& w, double aH, int vb) {
+// x = W^{-1} b in place on vector vb.  Expects vb synced; ends synced.
+template <int G>
+HD void solve_W(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS& w, double aH, int vb) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
   const double d = w.m(M_SCAL + S_D);
   const double x0 = w.v(vb, 0) * w.m(M_SCAL + S_W00I);
-  w.v(vb, 0) = x0;
-  for (int j = 1; j < n; ++j) w.v(vb, j) += w.v(V_JC0, j) * x0;
-  solve_M(m, D, w, d, aH, vb);
+  gp.sync();
+  for (int j = 1 + gp.lane; j < n; j += G) w.v(vb, j) += w.v(V_JC0, j) * x0;
+  if (gp.lead()) w.v(vb, 0) = x0;
+  gp.sync();
+  solve_M<G>(gp, m, D, w, d, aH, vb);
   double sh, se;
-  functionals(D, w, vb, sh, se);
+  functionals<G>(gp, D, w, vb, sh, se);
   const double th = w.m(M_CINV + 0) * sh + w.m(M_CINV + 1) * se;
   const double te = w.m(M_CINV + 2) * sh + w.m(M_CINV + 3) * se;
-  for (int j = 2; j < n; ++j) w.v(vb, j) += w.v(V_ZH, j) * th + w.v(V_ZE, j) * te;
-  double s1 = w.v(vb, 1) + w.m(M_SCAL + S_R13) * w.v(vb, 3) + w.m(M_SCAL + S_R15) * w.v(vb, 5) +
-              w.m(M_SCAL + S_R17) * w.v(vb, 7) + w.m(M_SCAL + S_R1R0) * w.v(vb, ir) +
-              w.m(M_SCAL + S_R1QE) * w.v(vb, n - 2) + w.m(M_SCAL + S_R1QT) * w.v(vb, n - 1);
-  for (int i = 0; i < nq; ++i) s1 += w.m(M_Q + Q_R1 * nq + i) * w.v(vb, iq0 + i);
-  w.v(vb, 1) = s1 / d;
+  gp.sync();
+  for (int j = 2 + gp.lane; j < n; j += G) w.v(vb, j) += w.v(V_ZH, j) * th + w.v(V_ZE, j) * te;
+  gp.sync();
+  double s1 = 0.0;
+  if (gp.lead())
+    s1 = w.m(M_SCAL + S_R13) * w.v(vb, 3) + w.m(M_SCAL + S_R15) * w.v(vb, 5) + w.m(M_SCAL + S_R17) * w.v(vb, 7) +
+         w.m(M_SCAL + S_R1R0) * w.v(vb, ir) + w.m(M_SCAL + S_R1QE) * w.v(vb, n - 2) + w.m(M_SCAL + S_R1QT) * w.v(vb, n - 1);
+  for (int i = gp.lane; i < nq; i += G) s1 += w.m(M_Q + Q_R1 * nq + i) * w.v(vb, iq0 + i);
+  s1 = gp.sum(s1);
+  if (gp.lead()) w.v(vb, 1) = (w.v(vb, 1) + s1) / d;
+  gp.sync();
 }
 
 // ------------------------------------------------------------------ dense reference-method path
 // W = d I - J assembled densely from the same pieces and factored by LU with
 // partial pivoting, like the reference's lu_factor / lu_solve
 // (ode_integrators_stiff.py:774-776, 783).  Kept for validation and as the
-// "plain" method; O(n^3) per step.
-HD long dense_off(const Dims& D) { return (long)NV * D.n + misc_len(D.nq); }
-
+// plain method; O(n^3) per step.  Rows are spread over the lanes.
 template <class F>
 HD void visit_u(const Dims& D, const WS& w, double wQ, F f) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
@@ -798,20 +897,19 @@ HD void visit_g(const Dims& D, const WS& w, F f) {
   }
 }
 
-// Assemble and factor the dense W.  Must run after factor_W (which fills the
-// chain coefficients and functional/row-1 coefficients) and before the core /
-// DE LU overwrite -- so factor_W calls it between factor_M's fills and LU.
-HD void dense_assemble(const ModeConst& m, const Dims& D, const Tab& T, const WS& w, double d, double tau,
-                       const Bg<double>& g, const double* core, const double* de) {
+// Assemble and factor the dense W after factor_W (which leaves the chain
+// coefficients and functional/row-1 coefficients in place).
+template <int G>
+HD void dense_factor(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab& T, const WS& w, double d, double tau,
+                     const Bg<double>& g) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
-  const long A0 = dense_off(D);
-  auto A = [&](int i, int j) -> double& { return w.e(A0 + (long)i * n + j); };
+  auto A = [&](int i, int j) -> double& { return w.e((long)i * n + j); };
   const double itau = 1.0 / tau, op = g.opac;
-  for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) A(i, j) = (i == j) ? d : 0.0;
-  for (int i = 0; i < n; ++i) A(i, 0) -= w.v(V_JC0, i);
-  // CDM, eta
-  A(3, 4) = 1.0; A(4, 4) = d + g.aH;
-  // chains: off-diagonals from LO/UP (M entries), diagonal damping
+  for (int i = gp.lane; i < n; i += G) {
+    for (int j = 0; j < n; ++j) A(i, j) = (i == j) ? d : 0.0;
+    A(i, 0) -= w.v(V_JC0, i);
+  }
+  gp.sync();
   auto chain = [&](int start, int stride, int cnt, double damp, double damp_last, bool attach) {
     for (int j = 0; j < cnt; ++j) {
       const int i = start + j * stride;
@@ -820,52 +918,81 @@ HD void dense_assemble(const ModeConst& m, const Dims& D, const Tab& T, const WS
       A(i, i) = d + (j == cnt - 1 ? damp_last : damp);
     }
   };
-  chain(ir, 1, lr + 1, 0.0, (lr + 1.0) * itau, false);
-  for (int i = 0; i < nq; ++i) chain(iq0 + i, nq, lnu + 1, 0.0, (lnu + 1.0) * itau, false);
-  chain(10, 1, lg - 2, op, op + (lg + 1.0) * itau, true);
-  chain(igp + 3, 1, lgp - 2, op, op + (lgp + 1.0) * itau, true);
-  A(9, 10) = w.v(V_UP, 9);
-  A(igp + 2, igp + 3) = w.v(V_UP, igp + 2);
-  const int cidx[8] = {5, 6, 7, 8, 9, igp, igp + 1, igp + 2};
-  for (int r = 0; r < 8; ++r) for (int cc = 0; cc < 8; ++cc) A(cidx[r], cidx[cc]) = core[r * 8 + cc];
-  A(n - 2, n - 2) = de[0]; A(n - 2, n - 1) = de[1]; A(n - 1, n - 2) = de[2]; A(n - 1, n - 1) = de[3];
-  // rank-2 metric coupling
-  visit_u(D, w, g.wQ, [&](int i, double uh, double ue) {
-    visit_g(D, w, [&](int j, double gh, double ge) { A(i, j) -= uh * gh + ue * ge; });
-  });
-  // row 1
-  for (int j = 1; j < n; ++j) A(1, j) = (j == 1) ? d : 0.0;
-  A(1, 0) = -w.v(V_JC0, 1);
-  A(1, 3) = -w.m(M_SCAL + S_R13); A(1, 5) = -w.m(M_SCAL + S_R15); A(1, 7) = -w.m(M_SCAL + S_R17);
-  A(1, ir) = -w.m(M_SCAL + S_R1R0); A(1, n - 2) = -w.m(M_SCAL + S_R1QE); A(1, n - 1) = -w.m(M_SCAL + S_R1QT);
-  for (int i = 0; i < nq; ++i) A(1, iq0 + i) = -w.m(M_Q + Q_R1 * nq + i);
-  // LU with partial pivoting (first maximal |pivot|)
-  const long P0 = A0 + (long)n * n;
+  for (int ch = gp.lane; ch < nq + 3; ch += G) {
+    if (ch == 0) chain(ir, 1, lr + 1, 0.0, (lr + 1.0) * itau, false);
+    else if (ch <= nq) chain(iq0 + ch - 1, nq, lnu + 1, 0.0, (lnu + 1.0) * itau, false);
+    else if (ch == nq + 1) chain(10, 1, lg - 2, op, op + (lg + 1.0) * itau, true);
+    else chain(igp + 3, 1, lgp - 2, op, op + (lgp + 1.0) * itau, true);
+  }
+  gp.sync();
+  if (gp.lead()) {
+    A(3, 4) = 1.0; A(4, 4) = d + g.aH;
+    A(9, 10) = w.v(V_UP, 9);
+    A(igp + 2, igp + 3) = w.v(V_UP, igp + 2);
+    double core[64], de[4];
+    core_entries(m, T, g, d, core, de);
+    const int cidx[8] = {5, 6, 7, 8, 9, igp, igp + 1, igp + 2};
+    for (int r = 0; r < 8; ++r) for (int cc = 0; cc < 8; ++cc) A(cidx[r], cidx[cc]) = core[r * 8 + cc];
+    A(n - 2, n - 2) = de[0]; A(n - 2, n - 1) = de[1]; A(n - 1, n - 2) = de[2]; A(n - 1, n - 1) = de[3];
+    visit_u(D, w, g.wQ, [&](int i, double uh, double ue) {
+      visit_g(D, w, [&](int j, double gh, double ge) { A(i, j) -= uh * gh + ue * ge; });
+    });
+    for (int j = 1; j < n; ++j) A(1, j) = (j == 1) ? d : 0.0;
+    A(1, 0) = -w.v(V_JC0, 1);
+    A(1, 3) = -w.m(M_SCAL + S_R13); A(1, 5) = -w.m(M_SCAL + S_R15); A(1, 7) = -w.m(M_SCAL + S_R17);
+    A(1, ir) = -w.m(M_SCAL + S_R1R0); A(1, n - 2) = -w.m(M_SCAL + S_R1QE); A(1, n - 1) = -w.m(M_SCAL + S_R1QT);
+    for (int i = 0; i < nq; ++i) A(1, iq0 + i) = -w.m(M_Q + Q_R1 * nq + i);
+  }
+  gp.sync();
+  // LU with partial pivoting (first maximal |pivot|), rows over lanes
+  const long P0 = (long)n * n;
   for (int kk = 0; kk < n; ++kk) {
-    int p = kk;
-    double mx = fabs(A(kk, kk));
-    for (int i = kk + 1; i < n; ++i) { const double v = fabs(A(i, kk)); if (v > mx) { mx = v; p = i; } }
-    w.e(P0 + kk) = (double)p;
-    if (p != kk) for (int j = 0; j < n; ++j) { const double t = A(kk, j); A(kk, j) = A(p, j); A(p, j) = t; }
+    double best = -1.0;
+    int bi = kk;
+    for (int i = kk + gp.lane; i < n; i += G) {
+      const double v = fabs(A(i, kk));
+      if (v > best) { best = v; bi = i; }
+    }
+    gp.argmax(best, bi);
+    if (gp.lead()) w.e(P0 + kk) = (double)bi;
+    if (bi != kk)
+      for (int j = gp.lane; j < n; j += G) { const double t = A(kk, j); A(kk, j) = A(bi, j); A(bi, j) = t; }
+    gp.sync();
     const double inv = 1.0 / A(kk, kk);
-    for (int i = kk + 1; i < n; ++i) {
+    for (int i = kk + 1 + gp.lane; i < n; i += G) {
       const double l = A(i, kk) * inv;
       A(i, kk) = l;
       if (l != 0.0) for (int j = kk + 1; j < n; ++j) A(i, j) -= l * A(kk, j);
     }
+    gp.sync();
   }
 }
 
-HD void dense_solve(const Dims& D, const WS& w, int vb) {
+template <int G>
+HD void dense_solve(const Grp<G>& gp, const Dims& D, const WS& w, int vb) {
   const int n = D.n;
-  const long A0 = dense_off(D), P0 = A0 + (long)n * n;
-  auto A = [&](int i, int j) -> double { return w.e(A0 + (long)i * n + j); };
-  for (int kk = 0; kk < n; ++kk) {
-    const int p = (int)w.e(P0 + kk);
-    if (p != kk) { const double t = w.v(vb, kk); w.v(vb, kk) = w.v(vb, p); w.v(vb, p) = t; }
+  const long P0 = (long)n * n;
+  auto A = [&](int i, int j) -> double { return w.e((long)i * n + j); };
+  if (gp.lead())
+    for (int kk = 0; kk < n; ++kk) {
+      const int p = (int)w.e(P0 + kk);
+      if (p != kk) { const double t = w.v(vb, kk); w.v(vb, kk) = w.v(vb, p); w.v(vb, p) = t; }
+    }
+  gp.sync();
+  for (int i = 1; i < n; ++i) {
+    double s = 0.0;
+    for (int j = gp.lane; j < i; j += G) s += A(i, j) * w.v(vb, j);
+    s = gp.sum(s);
+    if (gp.lead()) w.v(vb, i) -= s;
+    gp.sync();
   }
-  for (int i = 1; i < n; ++i) { double s = w.v(vb, i); for (int j = 0; j < i; ++j) s -= A(i, j) * w.v(vb, j); w.v(vb, i) = s; }
-  for (int i = n - 1; i >= 0; --i) { double s = w.v(vb, i); for (int j = i + 1; j < n; ++j) s -= A(i, j) * w.v(vb, j); w.v(vb, i) = s / A(i, i); }
+  for (int i = n - 1; i >= 0; --i) {
+    double s = 0.0;
+    for (int j = i + 1 + gp.lane; j < n; j += G) s += A(i, j) * w.v(vb, j);
+    s = gp.sum(s);
+    if (gp.lead()) w.v(vb, i) = (w.v(vb, i) - s) / A(i, i);
+    gp.sync();
+  }
 }
 
 // ------------------------------------------------------------------ controller + step
@@ -874,19 +1001,21 @@ struct Ctl {
   int max_steps, hist_on_reject, dense, return_full, nout;
 };
 
+// Integration state; every lane of a group holds an identical copy.
 struct Run {
   double t0, t1, T1, prev_inv, prev_prev_inv;
   int vy, vy1, steps, acc, rej, status;
 };
 
 // start a mode: start time, ICs, first step size (perturbations.py:742-756)
-HD void mode_begin(const Cosmo& c, const ModeConst& m, const Dims& D, const Ctl& ctl, const WS& w, const double* tau_out,
-                   Run& r) {
+template <int G>
+HD void mode_begin(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Ctl& ctl, const WS& w,
+                   const double* tau_out, Run& r) {
   double tmax = LDG(tau_out), tmin = tmax;
   for (int o = 1; o < ctl.nout; ++o) { const double t = LDG(tau_out + o); tmax = t > tmax ? t : tmax; tmin = t < tmin ? t : tmin; }
   const double ts = start_time(c, m);
   const double t0 = 0.99 * (tmin < ts ? tmin : ts);
-  initial_conditions(c, m, D, t0, w, V_Y);
+  initial_conditions<G>(gp, c, m, D, t0, w, V_Y);
   r.t0 = t0; r.T1 = tmax;
   const double dt0 = (t0 / 4.0 < 0.5 * (tmax - t0)) ? t0 / 4.0 : 0.5 * (tmax - t0);
   r.t1 = t0 + dt0 < tmax ? t0 + dt0 : tmax;
@@ -896,84 +1025,72 @@ HD void mode_begin(const Cosmo& c, const ModeConst& m, const Dims& D, const Ctl&
 
 // One attempted Rodas5 step (ode_integrators_stiff.py:718-834) plus the PID
 // decision.  Returns true while the mode still needs steps.
-HD bool mode_step(const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, const Rodas& R, const Ctl& ctl,
-                  const WS& w, const double* tau_out, double* yout, long ostride, Run& r) {
+template <int G>
+HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, const Rodas& R,
+                  const Ctl& ctl, const WS& w, const double* tau_out, double* yout, long ostride, Run& r) {
   if (!(r.t0 < r.T1)) return false;
   if (r.steps >= ctl.max_steps) { r.status = ST_MAX_STEPS; return false; }
   const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
   const double t0 = r.t0, dt = r.t1 - r.t0;
   const int vy = r.vy;
   // f(t0, y0) and d f / d a in one forward-mode pass
-  rhs<Dual>(c, m, D, T, t0, w, vy, V_F, V_JC0);
+  rhs<Dual, G>(gp, c, m, D, T, t0, w, vy, V_F, V_JC0);
   Bg<double> g;
   background<double>(c, m, w.v(vy, 0), g);
   const double d = 1.0 / (dt * R.gamma);
-  factor_W(c, m, D, T, w, d, t0, g);
-  if (ctl.dense) {
-    // rebuild the core and DE blocks of M (factor_W overwrote them with LU factors)
-    double core[64], de[4];
-    {
-      const double k = m.k, k2 = m.k2, op = g.opac;
-      for (int i = 0; i < 64; ++i) core[i] = 0.0;
-      core[0] = d; core[1] = 1.0;
-      core[8] = -k2 * g.cs2; core[9] = d + g.aH + g.pb43 * op; core[11] = -g.pb43 * op;
-      core[18] = d; core[19] = 4.0 / 3.0;
-      core[25] = -op; core[26] = -0.25 * k2; core[27] = d + op; core[28] = 0.5 * k2;
-      core[35] = -8.0 / 15.0; core[36] = d + 0.9 * op; core[37] = -0.1 * op; core[39] = -0.1 * op;
-      core[44] = -0.5 * op; core[45] = d + 0.5 * op; core[46] = k; core[47] = -0.5 * op;
-      core[53] = -k * T.lo[1]; core[54] = d + op; core[55] = k * T.up[1];
-      core[60] = -0.1 * op; core[61] = -0.1 * op; core[62] = -k * T.lo[2]; core[63] = d + 0.9 * op;
-      de[0] = d + 3.0 * (m.cs2Q - g.wQ) * g.aH;
-      de[1] = (1.0 + g.wQ) + 9.0 * (1.0 + g.wQ) * (m.cs2Q - g.ca2) * g.aH * g.aH * m.ik2;
-      de[2] = -m.cs2Q / (1.0 + g.wQ) * k2;
-      de[3] = d + (1.0 - 3.0 * m.cs2Q) * g.aH;
-    }
-    dense_assemble(m, D, T, w, d, t0, g, core, de);
-  }
+  factor_W<G>(gp, c, m, D, T, w, d, t0, g);
+  if (ctl.dense) dense_factor<G>(gp, m, D, T, w, d, t0, g);
   // d f / d tau: only the (l+1)/tau truncation terms
   const double it2 = 1.0 / (t0 * t0);
   const double dTT = (lg + 1.0) * it2 * w.v(vy, 7 + lg);
   const double dTP = (lgp + 1.0) * it2 * w.v(vy, igp + lgp);
   const double dTR = (lr + 1.0) * it2 * w.v(vy, ir + lr);
-  for (int i = 0; i < nq; ++i) w.m(M_Q + Q_DT * nq + i) = (lnu + 1.0) * it2 * w.v(vy, iq0 + lnu * nq + i);
+  for (int i = gp.lane; i < nq; i += G) w.m(M_Q + Q_DT * nq + i) = (lnu + 1.0) * it2 * w.v(vy, iq0 + lnu * nq + i);
   const double idt = 1.0 / dt;
   for (int s = 0; s < 8; ++s) {
     const int vk = V_K0 + s;
     if (s > 0) {
       if (s <= 5) {
-        for (int j = 0; j < n; ++j) {
+        for (int j = gp.lane; j < n; j += G) {
           double acc = w.v(vy, j);
           for (int q = 0; q < s; ++q) acc += R.a[s][q] * w.v(V_K0 + q, j);
           w.v(V_U, j) = acc;
         }
       } else {
-        for (int j = 0; j < n; ++j) w.v(V_U, j) += w.v(V_K0 + s - 1, j);
+        for (int j = gp.lane; j < n; j += G) w.v(V_U, j) += w.v(V_K0 + s - 1, j);
       }
-      rhs<double>(c, m, D, T, t0 + R.c[s] * dt, w, V_U, V_F, -1);
+      gp.sync();
+      rhs<double, G>(gp, c, m, D, T, t0 + R.c[s] * dt, w, V_U, V_F, -1);
     }
-    for (int j = 0; j < n; ++j) {
+    for (int j = gp.lane; j < n; j += G) {
       double acc = w.v(V_F, j);
       for (int q = 0; q < s; ++q) acc += (R.C[s][q] * idt) * w.v(V_K0 + q, j);
       w.v(vk, j) = acc;
     }
+    gp.sync();
     if (s <= 4) {
       const double dd = dt * R.d[s];
-      w.v(vk, 7 + lg) += dd * dTT;
-      w.v(vk, igp + lgp) += dd * dTP;
-      w.v(vk, ir + lr) += dd * dTR;
-      for (int i = 0; i < nq; ++i) w.v(vk, iq0 + lnu * nq + i) += dd * w.m(M_Q + Q_DT * nq + i);
+      if (gp.lead()) {
+        w.v(vk, 7 + lg) += dd * dTT;
+        w.v(vk, igp + lgp) += dd * dTP;
+        w.v(vk, ir + lr) += dd * dTR;
+      }
+      for (int i = gp.lane; i < nq; i += G) w.v(vk, iq0 + lnu * nq + i) += dd * w.m(M_Q + Q_DT * nq + i);
+      gp.sync();
     }
-    if (ctl.dense) dense_solve(D, w, vk);
-    else solve_W(m, D, w, g.aH, vk);
+    if (ctl.dense) dense_solve<G>(gp, D, w, vk);
+    else solve_W<G>(gp, m, D, w, g.aH, vk);
   }
   // y1 = u + k8 ; error estimate k8
   const int vy1 = r.vy1, vk8 = V_K0 + 7;
   bool bad = false;
-  for (int j = 0; j < n; ++j) {
+  for (int j = gp.lane; j < n; j += G) {
     const double v = w.v(V_U, j) + w.v(vk8, j);
     w.v(vy1, j) = v;
     bad = bad || !isfinite_(v);
   }
+  bad = gp.any(bad);
+  gp.sync();
   const int eidx[6] = {0, 2, 3, 5, 6, 7};
   const double ew[6] = {1.0, m.k2, 1.0, 1.0, m.ik2, 1.0};
   double ss = 0.0;
@@ -1007,11 +1124,13 @@ HD bool mode_step(const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& 
         const double cf = (tt - r.t0) / (r.t1 - r.t0);
         double* dst = yout + (long)o * (ctl.return_full ? n : 20) * ostride;
         if (ctl.return_full) {
-          for (int j = 0; j < n; ++j) { const double y0 = w.v(vy, j); dst[(long)j * ostride] = y0 + cf * (w.v(vy1, j) - y0); }
+          for (int j = gp.lane; j < n; j += G) { const double y0 = w.v(vy, j); dst[(long)j * ostride] = y0 + cf * (w.v(vy1, j) - y0); }
         } else {
-          for (int j = 0; j < n; ++j) { const double y0 = w.v(vy, j); w.v(V_U, j) = y0 + cf * (w.v(vy1, j) - y0); }
-          outputs(c, m, D, w, V_U, dst, ostride);
+          for (int j = gp.lane; j < n; j += G) { const double y0 = w.v(vy, j); w.v(V_U, j) = y0 + cf * (w.v(vy1, j) - y0); }
+          gp.sync();
+          if (gp.lead()) outputs(c, m, D, w, V_U, dst, ostride);
         }
+        gp.sync();
       }
     }
     r.vy = vy1; r.vy1 = vy;

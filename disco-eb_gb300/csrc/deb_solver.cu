@@ -40,14 +40,40 @@ struct KParams {
   double* y_out;
   int* status;
   int* steps;
-  double* ws;
-  long slot_len;
+  double* ws;         // lane mode: interleaved slots; warp mode: unused (shared memory) unless smem == 0
+  double* dws;        // dense matrices (dense path only)
+  long slot_len, dense_len;
+  int smem;           // warp mode: slots live in dynamic shared memory
   int* queue;
   deb::Ctl ctl;
   deb::Dims D;
 };
 
-__global__ void __launch_bounds__(kBlock) forward_kernel(KParams P) {
+// Validate mode m and load its cosmology; fills NaN outputs.  Same on every lane.
+__device__ bool prepare_mode(const KParams& P, int m, deb::Cosmo& c, deb::ModeConst& mc, const double*& tau_out,
+                             double*& yout, int lane, int G) {
+  const int osz = P.ctl.return_full ? P.D.n : DEB_NOUT_FIELDS;
+  const int ci = P.cosmo ? P.cosmo[m] : 0;
+  const double k = P.k[m];
+  double* dst = P.y_out + (long)m * P.ctl.nout * osz;
+  for (int i = lane; i < P.ctl.nout * osz; i += G) dst[i] = __longlong_as_double(0x7ff8000000000000LL);
+  bool ok = ci >= 0 && ci < P.ncosmo && k > 0.0 && isfinite(k);
+  if (ok) ok = deb::load_cosmo(P.tables + (long)ci * P.blob_len, P.blob_len, c) && c.nq == P.D.nq;
+  if (!ok) {
+    if (lane == 0) {
+      P.status[m] = deb::ST_BAD_INPUT;
+      if (P.steps) { P.steps[2 * m] = 0; P.steps[2 * m + 1] = 0; }
+    }
+    return false;
+  }
+  deb::mode_const(c, k, mc);
+  tau_out = P.tau_out + (long)ci * P.ctl.nout;
+  yout = dst;
+  return true;
+}
+
+// One thread per mode: 32 modes per warp, slots interleaved in global memory.
+__global__ void __launch_bounds__(kBlock) forward_lane_kernel(KParams P) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const long warp = tid >> 5;
@@ -56,48 +82,70 @@ __global__ void __launch_bounds__(kBlock) forward_kernel(KParams P) {
   w.stride = 32;
   w.n = P.D.n;
   w.misc0 = (long)deb::NV * P.D.n;
-  const int osz = P.ctl.return_full ? P.D.n : DEB_NOUT_FIELDS;
+  w.dp = P.dws ? P.dws + warp * 32 * P.dense_len + lane : nullptr;
+  w.dstride = 32;
+  const deb::Grp<1> gp{0};
   int mode = -1;
   deb::Cosmo c;
   deb::ModeConst mc;
   deb::Run run;
   const double* tau_out = nullptr;
   double* yout = nullptr;
-
   auto fetch = [&]() -> bool {
     for (;;) {
       const int m = atomicAdd(P.queue, 1);
       if (m >= P.nmode) return false;
       mode = m;
-      const int ci = P.cosmo ? P.cosmo[m] : 0;
-      const double k = P.k[m];
-      double* dst = P.y_out + (long)m * P.ctl.nout * osz;
-      for (int i = 0; i < P.ctl.nout * osz; ++i) dst[i] = __longlong_as_double(0x7ff8000000000000LL);
-      bool ok = ci >= 0 && ci < P.ncosmo && k > 0.0 && isfinite(k);
-      if (ok) ok = deb::load_cosmo(P.tables + (long)ci * P.blob_len, P.blob_len, c) && c.nq == P.D.nq;
-      if (!ok) {
-        P.status[m] = deb::ST_BAD_INPUT;
-        if (P.steps) { P.steps[2 * m] = 0; P.steps[2 * m + 1] = 0; }
-        continue;
-      }
-      deb::mode_const(c, k, mc);
-      tau_out = P.tau_out + (long)ci * P.ctl.nout;
-      yout = dst;
-      deb::mode_begin(c, mc, P.D, P.ctl, w, tau_out, run);
+      if (!prepare_mode(P, m, c, mc, tau_out, yout, 0, 1)) continue;
+      deb::mode_begin<1>(gp, c, mc, P.D, P.ctl, w, tau_out, run);
       return true;
     }
   };
-
   bool active = fetch();
   while (__any_sync(0xffffffffu, active)) {
     if (active) {
-      const bool more = deb::mode_step(c, mc, P.D, c_tab, c_rodas, P.ctl, w, tau_out, yout, 1, run);
+      const bool more = deb::mode_step<1>(gp, c, mc, P.D, c_tab, c_rodas, P.ctl, w, tau_out, yout, 1, run);
       if (!more) {
         P.status[mode] = run.status;
         if (P.steps) { P.steps[2 * mode] = run.acc; P.steps[2 * mode + 1] = run.rej; }
         active = fetch();
       }
     }
+  }
+}
+
+// One warp per mode: the mode's vectors and MISC block in shared memory.
+__global__ void __launch_bounds__(256) forward_warp_kernel(KParams P) {
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const long gwarp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  deb::WS w;
+  w.p = P.smem ? smem + (long)wib * P.slot_len : P.ws + gwarp * P.slot_len;
+  w.stride = 1;
+  w.n = P.D.n;
+  w.misc0 = (long)deb::NV * P.D.n;
+  w.dp = P.dws ? P.dws + gwarp * P.dense_len : nullptr;
+  w.dstride = 1;
+  const deb::Grp<32> gp{lane};
+  deb::Cosmo c;
+  deb::ModeConst mc;
+  deb::Run run;
+  const double* tau_out = nullptr;
+  double* yout = nullptr;
+  for (;;) {
+    int m = 0;
+    if (lane == 0) m = atomicAdd(P.queue, 1);
+    m = __shfl_sync(0xffffffffu, m, 0);
+    if (m >= P.nmode) break;
+    if (!prepare_mode(P, m, c, mc, tau_out, yout, lane, 32)) continue;
+    deb::mode_begin<32>(gp, c, mc, P.D, P.ctl, w, tau_out, run);
+    while (deb::mode_step<32>(gp, c, mc, P.D, c_tab, c_rodas, P.ctl, w, tau_out, yout, 1, run)) {}
+    if (lane == 0) {
+      P.status[m] = run.status;
+      if (P.steps) { P.steps[2 * m] = run.acc; P.steps[2 * m + 1] = run.rej; }
+    }
+    __syncwarp();
   }
 }
 
@@ -147,10 +195,15 @@ int upload_constants() {
 
 struct deb_plan {
   deb::Dims D;
-  int dense, return_full, nout;
-  int max_modes, nslots, nblocks;
-  long slot_len;
-  double* ws;
+  int dense, return_full, nout, exec_mode;
+  int max_modes, nsm;
+  long slot_len, dense_len;
+  // lane mode
+  int lane_blocks, lane_slots;
+  // warp mode
+  int warp_block_warps, warp_blocks, warp_smem;
+  double* ws;       // lane slots (or warp slots when shared memory is too small)
+  double* dws;      // dense matrices
   int* queue;
   size_t ws_bytes;
 };
@@ -185,31 +238,80 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
       dims->lmaxnu > deb::LMAX_TABLE)
     return DEB_ERR_INVALID;
   if (dims->linear_solver != DEB_SOLVE_STRUCTURED && dims->linear_solver != DEB_SOLVE_DENSE) return DEB_ERR_INVALID;
+  if (dims->exec_mode < DEB_EXEC_AUTO || dims->exec_mode > DEB_EXEC_WARP) return DEB_ERR_INVALID;
   int rc = upload_constants();
   if (rc) return rc;
-  int dev = 0, nsm = 0;
+  int dev = 0, nsm = 0, smem_optin = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return DEB_ERR_CUDA;
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return DEB_ERR_CUDA;
+  if (cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return DEB_ERR_CUDA;
   deb_plan* p = new deb_plan();
   p->D = deb::make_dims(dims->lmaxg, dims->lmaxgp, dims->lmaxr, dims->lmaxnu, dims->nqmax);
   p->dense = dims->linear_solver == DEB_SOLVE_DENSE;
   p->return_full = dims->return_full;
   p->nout = dims->nout;
   p->max_modes = max_modes;
-  p->slot_len = deb::slot_len(p->D, p->dense);
-  // slots: enough for every mode, at most 4 blocks per SM, and at most
-  // 16 GiB of workspace
-  long cap = (long)nsm * 4 * kBlock;
-  const long mem_cap = (16L << 30) / (p->slot_len * 8);
-  if (cap > mem_cap) cap = (mem_cap / 32) * 32;
-  if (cap < 32) cap = 32;
-  long want = ((long)max_modes + 31) / 32 * 32;
-  long ns = want < cap ? want : cap;
-  p->nblocks = (int)((ns + kBlock - 1) / kBlock);
-  p->nslots = p->nblocks * kBlock;
-  p->ws_bytes = (size_t)p->nslots * p->slot_len * sizeof(double);
-  if (cudaMalloc(&p->ws, p->ws_bytes) != cudaSuccess) { delete p; return DEB_ERR_NOMEM; }
-  if (cudaMalloc(&p->queue, sizeof(int) * 4) != cudaSuccess) { cudaFree(p->ws); delete p; return DEB_ERR_NOMEM; }
+  p->nsm = nsm;
+  p->slot_len = deb::slot_len(p->D);
+  p->dense_len = p->dense ? deb::dense_len(p->D) : 0;
+  const long per_slot = p->slot_len + p->dense_len;
+  // execution mode: lane per mode once the batch fills every SM sub-partition
+  // with >= 1 warp of modes, else warp per mode
+  int mode = dims->exec_mode;
+  if (mode == DEB_EXEC_AUTO) mode = ((long)max_modes >= (long)nsm * 4 * 32 && !p->dense) ? DEB_EXEC_LANE : DEB_EXEC_WARP;
+  p->exec_mode = mode;
+  // slot counts are capped at 16 GiB of workspace
+  const long mem_cap = (16L << 30) / (per_slot * 8);
+  long nslots;
+  if (mode == DEB_EXEC_LANE) {
+    long cap = (long)nsm * 4 * kBlock;
+    if (cap > mem_cap) cap = (mem_cap / 32) * 32;
+    if (cap < 32) cap = 32;
+    long want = ((long)max_modes + 31) / 32 * 32;
+    long ns = want < cap ? want : cap;
+    p->lane_blocks = (int)((ns + kBlock - 1) / kBlock);
+    p->lane_slots = p->lane_blocks * kBlock;
+    nslots = p->lane_slots;
+  } else {
+    const long slot_bytes = p->slot_len * 8;
+    int wpb = (int)((long)smem_optin / slot_bytes);
+    p->warp_smem = wpb >= 1;
+    if (wpb > 8) wpb = 8;
+    if (wpb < 1) wpb = 4;
+    p->warp_block_warps = wpb;
+    // blocks per SM limited by shared memory (228 KB per SM) and 32 warps per SM
+    int per_sm = 1;
+    if (p->warp_smem) {
+      const long blk = slot_bytes * wpb;
+      per_sm = (int)((228L * 1024) / (blk + 1024));
+      if (per_sm < 1) per_sm = 1;
+      if (per_sm * wpb > 32) per_sm = 32 / wpb;
+    } else {
+      per_sm = 2;
+    }
+    long cap_warps = (long)nsm * per_sm * wpb;
+    if (cap_warps > mem_cap) cap_warps = mem_cap;
+    long want = max_modes;
+    long nw = want < cap_warps ? want : cap_warps;
+    p->warp_blocks = (int)((nw + wpb - 1) / wpb);
+    nslots = (long)p->warp_blocks * wpb;
+    if (p->warp_smem) {
+      const int bytes = (int)(slot_bytes * wpb);
+      if (cudaFuncSetAttribute(forward_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) {
+        delete p;
+        return DEB_ERR_CUDA;
+      }
+    }
+  }
+  const bool need_ws = mode == DEB_EXEC_LANE || !p->warp_smem;
+  p->ws_bytes = (size_t)nslots * (need_ws ? p->slot_len : 0) * sizeof(double) + (size_t)nslots * p->dense_len * sizeof(double);
+  p->ws = nullptr;
+  p->dws = nullptr;
+  if (need_ws && cudaMalloc(&p->ws, (size_t)nslots * p->slot_len * sizeof(double)) != cudaSuccess) { delete p; return DEB_ERR_NOMEM; }
+  if (p->dense && cudaMalloc(&p->dws, (size_t)nslots * p->dense_len * sizeof(double)) != cudaSuccess) {
+    cudaFree(p->ws); delete p; return DEB_ERR_NOMEM;
+  }
+  if (cudaMalloc(&p->queue, sizeof(int) * 4) != cudaSuccess) { cudaFree(p->ws); cudaFree(p->dws); delete p; return DEB_ERR_NOMEM; }
   *out = p;
   return DEB_OK;
 }
@@ -223,6 +325,7 @@ int deb_plan_workspace_bytes(const deb_plan* p, size_t* bytes) {
 void deb_plan_destroy(deb_plan* p) {
   if (!p) return;
   cudaFree(p->ws);
+  cudaFree(p->dws);
   cudaFree(p->queue);
   delete p;
 }
@@ -239,7 +342,8 @@ int deb_forward(deb_plan* p, const double* d_tables, int ncosmo, int blob_len, c
   KParams P;
   P.tables = d_tables; P.ncosmo = ncosmo; P.blob_len = blob_len; P.k = d_k; P.cosmo = d_cosmo_of_mode;
   P.nmode = nmode; P.tau_out = d_tau_out; P.y_out = d_y_out; P.status = d_status; P.steps = d_steps;
-  P.ws = p->ws; P.slot_len = p->slot_len; P.queue = p->queue; P.D = p->D;
+  P.ws = p->ws; P.dws = p->dws; P.slot_len = p->slot_len; P.dense_len = p->dense_len; P.queue = p->queue; P.D = p->D;
+  P.smem = p->warp_smem;
   P.ctl.rtol = cfg->rtol; P.ctl.atol = cfg->atol;
   P.ctl.b1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / cfg->error_order;
   P.ctl.b2 = -(cfg->pcoeff + 2.0 * cfg->dcoeff) / cfg->error_order;
@@ -248,9 +352,17 @@ int deb_forward(deb_plan* p, const double* d_tables, int ncosmo, int blob_len, c
   P.ctl.max_steps = cfg->max_steps; P.ctl.hist_on_reject = cfg->hist_on_reject;
   P.ctl.dense = p->dense; P.ctl.return_full = p->return_full; P.ctl.nout = p->nout;
   if (cudaMemsetAsync(p->queue, 0, sizeof(int), s) != cudaSuccess) return DEB_ERR_CUDA;
-  long need = ((long)nmode + kBlock - 1) / kBlock;
-  const int blocks = (int)(need < p->nblocks ? need : p->nblocks);
-  forward_kernel<<<blocks, kBlock, 0, s>>>(P);
+  if (p->exec_mode == DEB_EXEC_LANE) {
+    long need = ((long)nmode + kBlock - 1) / kBlock;
+    const int blocks = (int)(need < p->lane_blocks ? need : p->lane_blocks);
+    forward_lane_kernel<<<blocks, kBlock, 0, s>>>(P);
+  } else {
+    const int wpb = p->warp_block_warps;
+    long need = ((long)nmode + wpb - 1) / wpb;
+    const int blocks = (int)(need < p->warp_blocks ? need : p->warp_blocks);
+    const size_t smem = p->warp_smem ? (size_t)p->slot_len * 8 * wpb : 0;
+    forward_warp_kernel<<<blocks, 32 * wpb, smem, s>>>(P);
+  }
   if (cudaGetLastError() != cudaSuccess) return DEB_ERR_CUDA;
   return DEB_OK;
 }

@@ -40,9 +40,10 @@ def nvar(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax) -> int:
     return 7 + (lmaxg + 1) + (lmaxgp + 1) + (lmaxr + 1) + nqmax * (lmaxnu + 1) + 2
 
 
-def _dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, nout, return_full, linear_solver):
+def _dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, nout, return_full, linear_solver, exec_mode="auto"):
     ls = {"structured": _native.DEB_SOLVE_STRUCTURED, "dense": _native.DEB_SOLVE_DENSE}[linear_solver]
-    return _native.DebDims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, nout, 1 if return_full else 0, ls)
+    return _native.DebDims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, nout, 1 if return_full else 0, ls,
+                           _native.EXEC_MODES[exec_mode])
 
 
 def _cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps, safety=0.9, error_order=5.0,
@@ -55,9 +56,11 @@ def get_plan(dims: _native.DebDims, nmode: int) -> _native.Plan:
     """Cached plan for these hierarchy sizes with room for >= nmode modes."""
     torch = _torch()
     key = (torch.cuda.current_device(), dims.lmaxg, dims.lmaxgp, dims.lmaxr, dims.lmaxnu, dims.nqmax, dims.nout,
-           dims.return_full, dims.linear_solver)
+           dims.return_full, dims.linear_solver, dims.exec_mode)
     p = _plans.get(key)
-    if p is None or p.max_modes < nmode:
+    # an automatic plan is re-made when the batch size moves it across the
+    # lane/warp threshold (the execution mode is fixed at plan creation)
+    if p is None or p.max_modes < nmode or (dims.exec_mode == 0 and p.max_modes > 4 * max(nmode, 1)):
         _plans.pop(key, None)
         p = _native.Plan(dims, max(nmode, 1))
         _plans[key] = p
@@ -74,7 +77,7 @@ class DeviceProblem:
     """
 
     def __init__(self, tables, kmodes, tau_out, cosmo_of_mode=None, *, lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax,
-                 return_full=False, linear_solver="structured"):
+                 return_full=False, linear_solver="structured", exec_mode="auto"):
         torch = _torch()
         dev = torch.device("cuda", torch.cuda.current_device())
         as_t = lambda a, dt: (a if torch.is_tensor(a) else torch.as_tensor(np.ascontiguousarray(a))).to(dev, dt).contiguous()
@@ -89,7 +92,7 @@ class DeviceProblem:
             self.cosmo = None
         else:
             self.cosmo = as_t(cosmo_of_mode, torch.int32)
-        self.dims = _dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, self.nout, return_full, linear_solver)
+        self.dims = _dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, self.nout, return_full, linear_solver, exec_mode)
         self.n = nvar(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax)
         self.osz = self.n if return_full else 20
         self.y = torch.empty((self.nmode, self.nout, self.osz), dtype=torch.float64, device=dev)
@@ -134,11 +137,11 @@ def _check_status(status: np.ndarray, kmodes: np.ndarray, throw: bool):
 def solve(tables, kmodes, tau_out, cosmo_of_mode=None, *, lmaxg=11, lmaxgp=11, lmaxr=11, lmaxnu=8, nqmax=3,
           rtol=1e-4, atol=1e-4, pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, max_steps=2048,
           return_full=False, linear_solver="structured", throw=True, return_stats=False, output="numpy",
-          error_order=5.0, safety=0.9, hist_on_reject=False):
+          error_order=5.0, safety=0.9, hist_on_reject=False, exec_mode="auto"):
     """Integrate modes of packed cosmologies on the GPU; y [nmode, nout, 20|nvar]."""
     torch = _torch()
     prob = DeviceProblem(tables, kmodes, tau_out, cosmo_of_mode, lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr, lmaxnu=lmaxnu,
-                         nqmax=nqmax, return_full=return_full, linear_solver=linear_solver)
+                         nqmax=nqmax, return_full=return_full, linear_solver=linear_solver, exec_mode=exec_mode)
     cfg = _cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps, safety, error_order, hist_on_reject)
     prob.launch(cfg)
     status = prob.status.cpu().numpy()

@@ -64,12 +64,20 @@ enum deb_linear_solver {
   DEB_SOLVE_DENSE = 1       /* dense LU with partial pivoting, O(n^3), as the reference */
 };
 
+/* how modes map onto the GPU */
+enum deb_exec_mode {
+  DEB_EXEC_AUTO = 0,        /* warp per mode for small batches, lane per mode for large ones */
+  DEB_EXEC_LANE = 1,        /* one thread per mode, state interleaved in global memory */
+  DEB_EXEC_WARP = 2         /* one warp per mode, state in shared memory */
+};
+
 /* hierarchy sizes: the keyword arguments of evolve_perturbations (perturbations.py:926-930) */
 typedef struct deb_dims {
   int lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax;
   int nout;            /* output times per cosmology */
   int return_full;     /* 0: 20 output fields, 1: full state of nvar entries */
   int linear_solver;   /* enum deb_linear_solver */
+  int exec_mode;       /* enum deb_exec_mode */
 } deb_dims;
 
 /* PIDController arguments of evolve_one_mode (perturbations.py:759-760) plus
@@ -90,7 +98,7 @@ typedef struct deb_plan deb_plan;
 int deb_nvar(const deb_dims* dims);
 
 /* Create a plan for up to max_modes modes per call.  Allocates the solver
-   workspace on the current device (the only allocation the library makes). */
+   workspace on the current device; deb_forward itself allocates nothing. */
 int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** plan);
 
 /* Bytes of device workspace the plan holds. */
@@ -122,8 +130,9 @@ int deb_get_power(const double* d_tables, int ncosmo, int blob_len, const double
 
 void deb_plan_destroy(deb_plan* plan);
 
-/* Measured-peak helper for roofline reporting: times a chain of dependent
-   FP64 FMAs over the whole device and returns achieved FP64 FLOP/s. */
+/* Measured-peak helper for roofline reporting: runs independent FP64 FMA
+   chains on every SM and returns the achieved FP64 FLOP/s (FMA = 2).
+   Allocates and frees 8 bytes of device memory and synchronises `stream`. */
 int deb_measure_fp64_peak(double* flops_per_s, void* stream);
 
 const char* deb_error_string(int code);

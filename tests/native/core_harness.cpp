@@ -13,15 +13,18 @@ using namespace deb;
 
 namespace {
 struct Ctx {
-  Dims D; Cosmo c; ModeConst m; Tab T; Rodas R; std::vector<double> buf; WS w;
+  Dims D; Cosmo c; ModeConst m; Tab T; Rodas R; std::vector<double> buf, dbuf; WS w;
 };
+const Grp<1> GP{0};
 bool setup(Ctx& x, const double* blob, int blob_len, const int* dims, double k, bool dense) {
   x.D = make_dims(dims[0], dims[1], dims[2], dims[3], dims[4]);
   if (!load_cosmo(blob, blob_len, x.c)) return false;
   mode_const(x.c, k, x.m);
   fill_tables(x.T); fill_rodas(x.R);
-  x.buf.assign(slot_len(x.D, dense), 0.0);
+  x.buf.assign(slot_len(x.D), 0.0);
+  x.dbuf.assign(dense ? dense_len(x.D) : 1, 0.0);
   x.w.p = x.buf.data(); x.w.stride = 1; x.w.n = x.D.n; x.w.misc0 = (long)NV * x.D.n;
+  x.w.dp = x.dbuf.data(); x.w.dstride = 1;
   for (int i = 0; i < x.D.nq; ++i) {
     double q = x.c.q[i];
     x.w.m(M_Q + Q_DLF * x.D.nq + i) = -q / (1.0 + std::exp(-q));
@@ -36,9 +39,9 @@ extern "C" {
 int h_rhs(const double* blob, int blob_len, const int* dims, double k, double tau, const double* y, double* f, double* jc0) {
   Ctx x; if (!setup(x, blob, blob_len, dims, k, false)) return -2;
   for (int j = 0; j < x.D.n; ++j) x.w.v(V_Y, j) = y[j];
-  rhs<Dual>(x.c, x.m, x.D, x.T, tau, x.w, V_Y, V_F, V_JC0);
+  rhs<Dual, 1>(GP, x.c, x.m, x.D, x.T, tau, x.w, V_Y, V_F, V_JC0);
   for (int j = 0; j < x.D.n; ++j) { f[j] = x.w.v(V_F, j); jc0[j] = x.w.v(V_JC0, j); }
-  rhs<double>(x.c, x.m, x.D, x.T, tau, x.w, V_Y, V_U, -1);
+  rhs<double, 1>(GP, x.c, x.m, x.D, x.T, tau, x.w, V_Y, V_U, -1);
   for (int j = 0; j < x.D.n; ++j) if (x.w.v(V_U, j) != f[j] && !(f[j] != f[j])) return -10;
   return 0;
 }
@@ -49,32 +52,16 @@ int h_solve_W(const double* blob, int blob_len, const int* dims, double k, doubl
   Ctx x; if (!setup(x, blob, blob_len, dims, k, dense != 0)) return -2;
   const int n = x.D.n;
   for (int j = 0; j < n; ++j) x.w.v(V_Y, j) = y[j];
-  rhs<Dual>(x.c, x.m, x.D, x.T, tau, x.w, V_Y, V_F, V_JC0);
+  rhs<Dual, 1>(GP, x.c, x.m, x.D, x.T, tau, x.w, V_Y, V_F, V_JC0);
   Bg<double> g; background<double>(x.c, x.m, y[0], g);
   const double d = 1.0 / (dt * x.R.gamma);
-  factor_W(x.c, x.m, x.D, x.T, x.w, d, tau, g);
+  factor_W<1>(GP, x.c, x.m, x.D, x.T, x.w, d, tau, g);
   for (int j = 0; j < n; ++j) x.w.v(V_K0, j) = b[j];
   if (dense) {
-    double core[64], de[4];
-    // same rebuild as mode_step
-    const double kk = x.m.k, k2 = x.m.k2, op = g.opac;
-    for (int i = 0; i < 64; ++i) core[i] = 0.0;
-    core[0] = d; core[1] = 1.0;
-    core[8] = -k2 * g.cs2; core[9] = d + g.aH + g.pb43 * op; core[11] = -g.pb43 * op;
-    core[18] = d; core[19] = 4.0 / 3.0;
-    core[25] = -op; core[26] = -0.25 * k2; core[27] = d + op; core[28] = 0.5 * k2;
-    core[35] = -8.0 / 15.0; core[36] = d + 0.9 * op; core[37] = -0.1 * op; core[39] = -0.1 * op;
-    core[44] = -0.5 * op; core[45] = d + 0.5 * op; core[46] = kk; core[47] = -0.5 * op;
-    core[53] = -kk * x.T.lo[1]; core[54] = d + op; core[55] = kk * x.T.up[1];
-    core[60] = -0.1 * op; core[61] = -0.1 * op; core[62] = -kk * x.T.lo[2]; core[63] = d + 0.9 * op;
-    de[0] = d + 3.0 * (x.m.cs2Q - g.wQ) * g.aH;
-    de[1] = (1.0 + g.wQ) + 9.0 * (1.0 + g.wQ) * (x.m.cs2Q - g.ca2) * g.aH * g.aH * x.m.ik2;
-    de[2] = -x.m.cs2Q / (1.0 + g.wQ) * k2;
-    de[3] = d + (1.0 - 3.0 * x.m.cs2Q) * g.aH;
-    dense_assemble(x.m, x.D, x.T, x.w, d, tau, g, core, de);
-    dense_solve(x.D, x.w, V_K0);
+    dense_factor<1>(GP, x.m, x.D, x.T, x.w, d, tau, g);
+    dense_solve<1>(GP, x.D, x.w, V_K0);
   } else {
-    solve_W(x.m, x.D, x.w, g.aH, V_K0);
+    solve_W<1>(GP, x.m, x.D, x.w, g.aH, V_K0);
   }
   for (int j = 0; j < n; ++j) xout[j] = x.w.v(V_K0, j);
   return 0;
@@ -83,7 +70,7 @@ int h_solve_W(const double* blob, int blob_len, const int* dims, double k, doubl
 int h_start(const double* blob, int blob_len, const int* dims, double k, double* tau_start, double* y0) {
   Ctx x; if (!setup(x, blob, blob_len, dims, k, false)) return -2;
   *tau_start = start_time(x.c, x.m);
-  initial_conditions(x.c, x.m, x.D, 0.99 * *tau_start, x.w, V_Y);
+  initial_conditions<1>(GP, x.c, x.m, x.D, 0.99 * *tau_start, x.w, V_Y);
   for (int j = 0; j < x.D.n; ++j) y0[j] = x.w.v(V_Y, j);
   return 0;
 }
@@ -105,8 +92,8 @@ int h_solve(const double* tables, int ncosmo, int blob_len, const double* kmodes
     double* dst = y_out + (long)mi * nout * osz;
     for (int i = 0; i < nout * osz; ++i) dst[i] = std::numeric_limits<double>::quiet_NaN();
     Run r;
-    mode_begin(x.c, x.m, x.D, ctl, x.w, tau_out + (long)ci * nout, r);
-    while (mode_step(x.c, x.m, x.D, x.T, x.R, ctl, x.w, tau_out + (long)ci * nout, dst, 1, r)) {}
+    mode_begin<1>(GP, x.c, x.m, x.D, ctl, x.w, tau_out + (long)ci * nout, r);
+    while (mode_step<1>(GP, x.c, x.m, x.D, x.T, x.R, ctl, x.w, tau_out + (long)ci * nout, dst, 1, r)) {}
     stats[3 * mi] = r.status; stats[3 * mi + 1] = r.acc; stats[3 * mi + 2] = r.rej;
   }
   return 0;
