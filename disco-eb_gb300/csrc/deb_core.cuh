@@ -28,6 +28,8 @@
 // The result equals the dense solution to rounding; the work is O(n).
 #pragma once
 
+#include <type_traits>
+
 #ifdef __CUDACC__
 #define HD __host__ __device__ __forceinline__
 #ifdef __CUDA_ARCH__
@@ -187,16 +189,18 @@ HD int misc_len(int nq) { return M_Q + NQARR * nq; }
 HD long slot_len(const Dims& D) { return (long)NV * D.n + misc_len(D.nq); }
 HD long dense_len(const Dims& D) { return (long)D.n * D.n + D.n; }
 
+// Element stride follows the group width: one thread per mode interleaves
+// the 32 modes of a warp (stride 32), one warp per mode is contiguous.
+template <int G>
 struct WS {
+  static constexpr int S = (G == 1) ? 32 : 1;
   double* p;      // vectors + MISC
-  int stride;
-  long n;
-  long misc0;
+  int n;
+  int misc0;
   double* dp;     // dense matrix + pivots (dense path only)
-  int dstride;
-  HD double& v(int vec, int j) const { return p[((long)vec * n + j) * stride]; }
-  HD double& m(int off) const { return p[(misc0 + off) * stride]; }
-  HD double& e(long off) const { return dp[off * dstride]; }
+  HD double& v(int vec, int j) const { return p[(vec * n + j) * S]; }
+  HD double& m(int off) const { return p[(misc0 + off) * S]; }
+  HD double& e(int off) const { return dp[off * S]; }
 };
 
 // A group of G lanes that cooperates on one mode: G = 1 (one thread per
@@ -290,7 +294,7 @@ HD void background(const Cosmo& c, const ModeConst& m, S a, Bg<S>& g) {
   g.rhoQ = dexp(m.pQ * g.la + 3.0 * (a - 1.0) * m.wa);
   S grho = m.grhom * m.Om * g.ia + (m.grhog + m.grhor * (m.Neff + m.Nmnu * g.rhonu)) * g.ia2 +
            m.grhom * m.ODE * g.rhoQ * g.a2 + m.grhom * m.Ok;
-  g.aH = dsqrt(grho / 3.0);
+  g.aH = dsqrt(grho * (1.0 / 3.0));
   g.iaH = 1.0 / g.aH;
   g.wQ = m.w0 + m.wa * (1.0 - a);
   S wQp = -m.wa * g.aH * a;
@@ -314,18 +318,25 @@ HD double aprimeoa(const Cosmo& c, const ModeConst& m, double a) {
 // a-dependence is differentiated: vout receives f, vjc receives d f / d a.
 // Ends with a group sync; expects vin to be complete (synced) on entry.
 template <class S, int G>
-HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, double tau, const WS& w,
-            int vin, int vout, int vjc) {
+HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, double tau, const WS<G>& w,
+            int vin, int vout, int vjc, Bg<double>* gout = nullptr) {
+  constexpr bool kDual = !std::is_same<S, double>::value;
   const int n = D.n, nq = D.nq, iq0 = D.iq0, iq1 = iq0 + nq, iq2 = iq1 + nq, iq3 = iq2 + nq;
   const int igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
   const double k = m.k, k2 = m.k2;
   const double itau = 1.0 / tau;
   Bg<S> g;
   background<S>(c, m, make_var<S>(w.v(vin, 0)), g);
+  if (gout) {
+    gout->a = val(g.a); gout->ia = val(g.ia); gout->ia2 = val(g.ia2); gout->a2 = val(g.a2); gout->la = val(g.la);
+    gout->cs2 = val(g.cs2); gout->xe = val(g.xe); gout->rhonu = val(g.rhonu); gout->rhoQ = val(g.rhoQ);
+    gout->aH = val(g.aH); gout->iaH = val(g.iaH); gout->wQ = val(g.wQ); gout->ca2 = val(g.ca2);
+    gout->opac = val(g.opac); gout->pb43 = val(g.pb43);
+  }
   auto Y = [&](int j) -> double { return w.v(vin, j); };
   auto put = [&](int j, S f) {
     w.v(vout, j) = val(f);
-    if (vjc >= 0) w.v(vjc, j) = der(f);
+    if constexpr (kDual) w.v(vjc, j) = der(f);
   };
   // massive neutrino momentum sums (nu_perturb, perturbations.py:22-50)
   S drhonu = 0.0, dpnu = 0.0, fnu = 0.0;
@@ -339,13 +350,13 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
     dpnu = dpnu + wq * p0 * v;
     fnu = fnu + wq * Y(iq1 + i);
     w.m(M_Q + Q_V * nq + i) = val(v);         // v_q and d v_q / d a for the element loop
-    if (vjc >= 0) w.m(M_Q + Q_DV * nq + i) = der(v);
+    if constexpr (kDual) w.m(M_Q + Q_DV * nq + i) = der(v);
   }
   drhonu = gp.sum(drhonu);
   dpnu = gp.sum(dpnu);
   fnu = gp.sum(fnu);
   gp.sync();
-  dpnu = dpnu / 3.0;
+  dpnu = dpnu * (1.0 / 3.0);
   const double eta = Y(2), dc = Y(3), tc = Y(4), db = Y(5), tb = Y(6), dg = Y(7), tg = Y(8), y9 = Y(9);
   const double dr = Y(ir), tr = Y(ir + 1), y_r2 = Y(ir + 2);
   const double dq = Y(n - 2), tq = Y(n - 1);
@@ -357,7 +368,7 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
               m.Nmnu * m.grhor * k * fnu * g.ia2 + rptQ;
   S etap = 0.5 * dgtheta * m.ik2;
   if (gp.lead()) {
-    S dgpres = (m.grhog * dg + m.grhor * m.Neff * dr) * g.ia2 / 3.0 + m.grhor * m.Nmnu * dpnu * g.ia2 +
+    S dgpres = (m.grhog * dg + m.grhor * m.Neff * dr) * g.ia2 * (1.0 / 3.0) + m.grhor * m.Nmnu * dpnu * g.ia2 +
                (m.cs2Q * m.grhom * m.ODE * dq * g.rhoQ * g.a2 + (m.cs2Q - g.ca2) * (3.0 * g.aH * rptQ * m.ik2));
     S alpha = (hp + 6.0 * etap) * 0.5 * m.ik2;
     put(0, g.aH * g.a);
@@ -393,25 +404,34 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
   for (int l = 3 + gp.lane; l < lgp; l += G)
     put(igp + l, k * (T.lo[l] * Y(igp + l - 1) - T.up[l] * Y(igp + l + 1)) - g.opac * Y(igp + l));
   for (int l = 3 + gp.lane; l < lr; l += G) put(ir + l, S(k * (T.lo[l] * Y(ir + l - 1) - T.up[l] * Y(ir + l + 1))));
-  // massive neutrinos, l-major [l][q]
+  // massive neutrinos, l-major [l][q]; element e = l nq + i walked with
+  // incremental (l, i) so the loop needs no integer division
   const int nmass = nq * (lnu + 1);
+  const int dl = G / nq, di = G - dl * nq;
+  int l = gp.lane / nq, i = gp.lane - l * nq;
+  const S hp6 = hp * (1.0 / 6.0);
+  const S hp_eta = hp * (1.0 / 15.0) + 0.4 * etap;
   for (int e = gp.lane; e < nmass; e += G) {
-    const int l = e / nq, i = e - l * nq;
-    S v = mk<S>(w.m(M_Q + Q_V * nq + i), vjc >= 0 ? w.m(M_Q + Q_DV * nq + i) : 0.0);
+    S v;
+    if constexpr (kDual) v = mk<S>(w.m(M_Q + Q_V * nq + i), w.m(M_Q + Q_DV * nq + i));
+    else v = w.m(M_Q + Q_V * nq + i);
     S kv = k * v;
     S f;
     if (l == 0) {
-      f = -kv * Y(iq1 + i) + hp * w.m(M_Q + Q_DLF * nq + i) / 6.0;
+      f = -kv * Y(iq1 + i) + hp6 * w.m(M_Q + Q_DLF * nq + i);
     } else if (l == 1) {
-      f = kv * (Y(iq0 + i) - 2.0 * Y(iq2 + i)) / 3.0;
+      f = kv * (Y(iq0 + i) - 2.0 * Y(iq2 + i)) * (1.0 / 3.0);
     } else if (l == 2) {
-      f = kv * (2.0 * Y(iq1 + i) - 3.0 * Y(iq3 + i)) / 5.0 - (hp / 15.0 + 0.4 * etap) * w.m(M_Q + Q_DLF * nq + i);
+      f = kv * (2.0 * Y(iq1 + i) - 3.0 * Y(iq3 + i)) * 0.2 - hp_eta * w.m(M_Q + Q_DLF * nq + i);
     } else if (l < lnu) {
       f = kv * (T.lo[l] * Y(iq0 + (l - 1) * nq + i) - T.up[l] * Y(iq0 + (l + 1) * nq + i));
     } else {
       f = kv * Y(iq0 + (lnu - 1) * nq + i) - (lnu + 1.0) * itau * Y(iq0 + lnu * nq + i);
     }
     put(iq0 + e, f);
+    l += dl;
+    i += di;
+    if (i >= nq) { i -= nq; ++l; }
   }
   gp.sync();
 }
@@ -420,7 +440,8 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
 // convert_to_output_variables (perturbations.py:374-523) of the state held in
 // vector vin; Friedmann aH from the tables, 20 fields to out[0..19*ostride].
 // Scalar work: called by one lane.
-HD void outputs(const Cosmo& c, const ModeConst& m, const Dims& D, const WS& w, int vin, double* out, long ostride) {
+template <int G>
+HD void outputs(const Cosmo& c, const ModeConst& m, const Dims& D, const WS<G>& w, int vin, double* out, long ostride) {
   const int nq = D.nq, iq0 = D.iq0, iq1 = iq0 + nq, n = D.n;
   const double k = m.k, k2 = m.k2;
   auto Y = [&](int j) -> double { return w.v(vin, j); };
@@ -468,7 +489,7 @@ HD void outputs(const Cosmo& c, const ModeConst& m, const Dims& D, const WS& w, 
 // ------------------------------------------------------------------ initial conditions
 // adiabatic_ics_one_mode (perturbations.py:526-627), written into vector vout.
 template <int G>
-HD void initial_conditions(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, double tau, const WS& w,
+HD void initial_conditions(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, double tau, const WS<G>& w,
                            int vout) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, iq1 = iq0 + nq, iq2 = iq1 + nq;
   const double k = m.k;
@@ -560,7 +581,8 @@ HD double start_time(const Cosmo& c, const ModeConst& m) {
 // (l+1)/tau) is non-negative.
 // Chain numbering: 0 massless nu, 1..nq massive nu q-1, nq+1 photon T tail
 // (l >= 3, attached to T2 = index 9), nq+2 photon P tail (attached to P2).
-HD void chain_pivots(const WS& w, int start, int stride, int cnt, double d_last, double d_rest) {
+template <int G>
+HD void chain_pivots(const WS<G>& w, int start, int stride, int cnt, double d_last, double d_rest) {
   int i = start + (cnt - 1) * stride;
   double pinv = 1.0 / d_last;
   w.v(V_PI, i) = pinv;
@@ -572,7 +594,8 @@ HD void chain_pivots(const WS& w, int start, int stride, int cnt, double d_last,
   }
 }
 
-HD void chain_fill_factor(const ModeConst& m, const Dims& D, const Tab& T, const WS& w, double d, double itau, double op,
+template <int G>
+HD void chain_fill_factor(const ModeConst& m, const Dims& D, const Tab& T, const WS<G>& w, double d, double itau, double op,
                           int ch) {
   const int nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
   const double k = m.k, k2 = m.k2;
@@ -582,7 +605,7 @@ HD void chain_fill_factor(const ModeConst& m, const Dims& D, const Tab& T, const
     w.v(V_LO, ir + 2) = -8.0 / 15.0; w.v(V_UP, ir + 2) = 0.6 * k;
     for (int l = 3; l < lr; ++l) { w.v(V_LO, ir + l) = -k * T.lo[l]; w.v(V_UP, ir + l) = k * T.up[l]; }
     w.v(V_LO, ir + lr) = -k;
-    chain_pivots(w, ir, 1, lr + 1, d + (lr + 1.0) * itau, d);
+    chain_pivots<G>(w, ir, 1, lr + 1, d + (lr + 1.0) * itau, d);
   } else if (ch <= nq) {
     const int i = ch - 1;
     const double kv = k * w.m(M_Q + Q_V * nq + i);
@@ -592,23 +615,23 @@ HD void chain_fill_factor(const ModeConst& m, const Dims& D, const Tab& T, const
       w.v(V_UP, e) = kv * T.up[l];
     }
     w.v(V_LO, iq0 + lnu * nq + i) = -kv;
-    chain_pivots(w, iq0 + i, nq, lnu + 1, d + (lnu + 1.0) * itau, d);
+    chain_pivots<G>(w, iq0 + i, nq, lnu + 1, d + (lnu + 1.0) * itau, d);
   } else if (ch == nq + 1) {
     w.v(V_UP, 9) = 0.6 * k;
     for (int l = 3; l < lg; ++l) { w.v(V_LO, 7 + l) = -k * T.lo[l]; w.v(V_UP, 7 + l) = k * T.up[l]; }
     w.v(V_LO, 7 + lg) = -k;
-    chain_pivots(w, 10, 1, lg - 2, d + op + (lg + 1.0) * itau, d + op);
+    chain_pivots<G>(w, 10, 1, lg - 2, d + op + (lg + 1.0) * itau, d + op);
   } else {
     w.v(V_UP, igp + 2) = 0.6 * k;
     for (int l = 3; l < lgp; ++l) { w.v(V_LO, igp + l) = -k * T.lo[l]; w.v(V_UP, igp + l) = k * T.up[l]; }
     w.v(V_LO, igp + lgp) = -k;
-    chain_pivots(w, igp + 3, 1, lgp - 2, d + op + (lgp + 1.0) * itau, d + op);
+    chain_pivots<G>(w, igp + 3, 1, lgp - 2, d + op + (lgp + 1.0) * itau, d + op);
   }
 }
 
 // small dense LU with partial pivoting in the MISC block (row-major, N <= 8)
-template <int N>
-HD void small_lu(const WS& w, int off, int pivoff) {
+template <int N, int G>
+HD void small_lu(const WS<G>& w, int off, int pivoff) {
   for (int kk = 0; kk < N; ++kk) {
     int p = kk;
     double mx = fabs(w.m(off + kk * N + kk));
@@ -626,17 +649,18 @@ HD void small_lu(const WS& w, int off, int pivoff) {
       if (l != 0.0)
         for (int j = kk + 1; j < N; ++j) w.m(off + i * N + j) -= l * w.m(off + kk * N + j);
     }
+    w.m(off + kk * N + kk) = inv;   // U_kk is kept as its reciprocal
   }
 }
 
-template <int N>
-HD void small_solve(const WS& w, int off, int pivoff, double* r) {
+template <int N, int G>
+HD void small_solve(const WS<G>& w, int off, int pivoff, double* r) {
   for (int kk = 0; kk < N; ++kk) {
     const int p = (int)w.m(pivoff + kk);
     if (p != kk) { double t = r[kk]; r[kk] = r[p]; r[p] = t; }
   }
   for (int i = 1; i < N; ++i) { double s = r[i]; for (int j = 0; j < i; ++j) s -= w.m(off + i * N + j) * r[j]; r[i] = s; }
-  for (int i = N - 1; i >= 0; --i) { double s = r[i]; for (int j = i + 1; j < N; ++j) s -= w.m(off + i * N + j) * r[j]; r[i] = s / w.m(off + i * N + i); }
+  for (int i = N - 1; i >= 0; --i) { double s = r[i]; for (int j = i + 1; j < N; ++j) s -= w.m(off + i * N + j) * r[j]; r[i] = s * w.m(off + i * N + i); }
 }
 
 // entries of the 8x8 photon-baryon core of M (db, tb, dg, tg, T2, P0, P1, P2)
@@ -661,11 +685,11 @@ HD void core_entries(const ModeConst& m, const Tab& T, const Bg<double>& g, doub
 // Fill chain coefficients and factor M (chains per lane; core and DE on the
 // leading lane).  Needs v_q in MISC (written by the RHS at this a).
 template <int G>
-HD void factor_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab& T, const WS& w, double d, double tau,
+HD void factor_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab& T, const WS<G>& w, double d, double tau,
                  const Bg<double>& g) {
   const int nq = D.nq, igp = D.igp;
   const double itau = 1.0 / tau, op = g.opac;
-  for (int ch = gp.lane; ch < nq + 3; ch += G) chain_fill_factor(m, D, T, w, d, itau, op, ch);
+  for (int ch = gp.lane; ch < nq + 3; ch += G) chain_fill_factor<G>(m, D, T, w, d, itau, op, ch);
   gp.sync();
   if (gp.lead()) {
     double core[64], de[4];
@@ -673,33 +697,37 @@ HD void factor_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab&
     core[36] -= w.v(V_UP, 9) * w.v(V_LO, 10) * w.v(V_PI, 10);
     core[63] -= w.v(V_UP, igp + 2) * w.v(V_LO, igp + 3) * w.v(V_PI, igp + 3);
     for (int i = 0; i < 64; ++i) w.m(M_CORE + i) = core[i];
-    small_lu<8>(w, M_CORE, M_CPIV);
+    small_lu<8, G>(w, M_CORE, M_CPIV);
     // dark energy 2x2 (rows n-2, n-1): LU with partial pivoting, M_DE+4 = 1 if swapped
     double a00 = de[0], a01 = de[1], a10 = de[2], a11 = de[3];
     double sw = 0.0;
     if (fabs(a10) > fabs(a00)) { double t0_ = a00, t1_ = a01; a00 = a10; a01 = a11; a10 = t0_; a11 = t1_; sw = 1.0; }
     const double l = a10 / a00;
-    w.m(M_DE + 0) = a00; w.m(M_DE + 1) = a01; w.m(M_DE + 2) = l; w.m(M_DE + 3) = a11 - l * a01; w.m(M_DE + 4) = sw;
+    w.m(M_DE + 0) = 1.0 / a00; w.m(M_DE + 1) = a01; w.m(M_DE + 2) = l; w.m(M_DE + 3) = 1.0 / (a11 - l * a01);
+    w.m(M_DE + 4) = sw;
+    w.m(M_SCAL + S_ID) = 1.0 / d;
+    w.m(M_SCAL + S_IDAH) = 1.0 / (d + g.aH);
   }
   gp.sync();
 }
 
 // z = M^{-1} r on indices >= 2, in place on vector vr.  Expects vr synced.
 template <int G>
-HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS& w, double d, double aH, int vr) {
+HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>& w, double d, double aH, int vr) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
   (void)m;
+  (void)d; (void)aH;
   if (gp.lead()) {
-    const double id = 1.0 / d;
+    const double id = w.m(M_SCAL + S_ID);
     w.v(vr, 2) = w.v(vr, 2) * id;                      // eta
-    const double z4 = w.v(vr, 4) / (d + aH);           // CDM [[d, 1], [0, d + aH]]
+    const double z4 = w.v(vr, 4) * w.m(M_SCAL + S_IDAH);  // CDM [[d, 1], [0, d + aH]]
     w.v(vr, 4) = z4;
     w.v(vr, 3) = (w.v(vr, 3) - z4) * id;
     double r0 = w.v(vr, n - 2), r1 = w.v(vr, n - 1);   // DE
     if (w.m(M_DE + 4) != 0.0) { double t = r0; r0 = r1; r1 = t; }
     r1 -= w.m(M_DE + 2) * r0;
-    const double z1 = r1 / w.m(M_DE + 3);
-    const double z0 = (r0 - w.m(M_DE + 1) * z1) / w.m(M_DE + 0);
+    const double z1 = r1 * w.m(M_DE + 3);
+    const double z0 = (r0 - w.m(M_DE + 1) * z1) * w.m(M_DE + 0);
     w.v(vr, n - 2) = z0; w.v(vr, n - 1) = z1;
   }
   for (int ch = gp.lane; ch < nq + 3; ch += G) {
@@ -708,11 +736,15 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS& w
       const int start = ch == 0 ? ir : iq0 + ch - 1;
       const int stride = ch == 0 ? 1 : nq;
       const int cnt = ch == 0 ? lr + 1 : lnu + 1;
+      int i = start + (cnt - 1) * stride;
+      double rn = w.v(vr, i), pn = w.v(V_PI, i);
       for (int j = cnt - 2; j >= 0; --j) {
-        const int i = start + j * stride;
-        w.v(vr, i) -= w.v(V_UP, i) * w.v(vr, i + stride) * w.v(V_PI, i + stride);
+        i -= stride;
+        rn = w.v(vr, i) - w.v(V_UP, i) * rn * pn;
+        pn = w.v(V_PI, i);
+        w.v(vr, i) = rn;
       }
-      double z = w.v(vr, start) * w.v(V_PI, start);
+      double z = rn * pn;
       w.v(vr, start) = z;
       for (int j = 1; j < cnt; ++j) {
         const int i = start + j * stride;
@@ -724,17 +756,21 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS& w
       const int start = ch == nq + 1 ? 10 : igp + 3;
       const int cnt = ch == nq + 1 ? lg - 2 : lgp - 2;
       const int attach = start - 1;
+      int i = start + cnt - 1;
+      double rn = w.v(vr, i), pn = w.v(V_PI, i);
       for (int j = cnt - 2; j >= 0; --j) {
-        const int i = start + j;
-        w.v(vr, i) -= w.v(V_UP, i) * w.v(vr, i + 1) * w.v(V_PI, i + 1);
+        --i;
+        rn = w.v(vr, i) - w.v(V_UP, i) * rn * pn;
+        pn = w.v(V_PI, i);
+        w.v(vr, i) = rn;
       }
-      w.v(vr, attach) -= w.v(V_UP, attach) * w.v(vr, start) * w.v(V_PI, start);
+      w.v(vr, attach) -= w.v(V_UP, attach) * rn * pn;
     }
   }
   gp.sync();
   if (gp.lead()) {
     double r[8] = {w.v(vr, 5), w.v(vr, 6), w.v(vr, 7), w.v(vr, 8), w.v(vr, 9), w.v(vr, igp), w.v(vr, igp + 1), w.v(vr, igp + 2)};
-    small_solve<8>(w, M_CORE, M_CPIV, r);
+    small_solve<8, G>(w, M_CORE, M_CPIV, r);
     w.v(vr, 5) = r[0]; w.v(vr, 6) = r[1]; w.v(vr, 7) = r[2]; w.v(vr, 8) = r[3]; w.v(vr, 9) = r[4];
     w.v(vr, igp) = r[5]; w.v(vr, igp + 1) = r[6]; w.v(vr, igp + 2) = r[7];
   }
@@ -754,7 +790,7 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS& w
 
 // g_h . v and g_e . v (the metric functionals h', eta' as rows); all lanes get the sums
 template <int G>
-HD void functionals(const Grp<G>& gp, const Dims& D, const WS& w, int vr, double& sh, double& se) {
+HD void functionals(const Grp<G>& gp, const Dims& D, const WS<G>& w, int vr, double& sh, double& se) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
   double h = 0.0, e = 0.0;
   if (gp.lead()) {
@@ -775,7 +811,7 @@ HD void functionals(const Grp<G>& gp, const Dims& D, const WS& w, int vr, double
 // the background g at a0 and v_q in MISC.  Writes LO/UP/PI, core/DE LU, ZH,
 // ZE, the capacitance inverse and the sparse row-1 / functional coefficients.
 template <int G>
-HD void factor_W(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, const WS& w,
+HD void factor_W(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, const WS<G>& w,
                  double d, double tau, const Bg<double>& g) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
   const double a = g.a, iaH = g.iaH, h2 = 0.5 * m.ik2;
@@ -841,7 +877,7 @@ HD void factor_W(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dim
 
 // x = W^{-1} b in place on vector vb.  Expects vb synced; ends synced.
 template <int G>
-HD void solve_W(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS& w, double aH, int vb) {
+HD void solve_W(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>& w, double aH, int vb) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
   const double d = w.m(M_SCAL + S_D);
   const double x0 = w.v(vb, 0) * w.m(M_SCAL + S_W00I);
@@ -863,7 +899,7 @@ HD void solve_W(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS& w
          w.m(M_SCAL + S_R1R0) * w.v(vb, ir) + w.m(M_SCAL + S_R1QE) * w.v(vb, n - 2) + w.m(M_SCAL + S_R1QT) * w.v(vb, n - 1);
   for (int i = gp.lane; i < nq; i += G) s1 += w.m(M_Q + Q_R1 * nq + i) * w.v(vb, iq0 + i);
   s1 = gp.sum(s1);
-  if (gp.lead()) w.v(vb, 1) = (w.v(vb, 1) + s1) / d;
+  if (gp.lead()) w.v(vb, 1) = (w.v(vb, 1) + s1) * w.m(M_SCAL + S_ID);
   gp.sync();
 }
 
@@ -872,8 +908,8 @@ HD void solve_W(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS& w
 // partial pivoting, like the reference's lu_factor / lu_solve
 // (ode_integrators_stiff.py:774-776, 783).  Kept for validation and as the
 // plain method; O(n^3) per step.  Rows are spread over the lanes.
-template <class F>
-HD void visit_u(const Dims& D, const WS& w, double wQ, F f) {
+template <int G, class F>
+HD void visit_u(const Dims& D, const WS<G>& w, double wQ, F f) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
   f(3, -0.5, 0.0); f(5, -0.5, 0.0); f(7, -2.0 / 3.0, 0.0); f(9, 4.0 / 15.0, 1.6);
   f(ir, -2.0 / 3.0, 0.0); f(ir + 2, 4.0 / 15.0, 1.6); f(n - 2, -0.5 * (1.0 + wQ), 0.0); f(2, 0.0, 1.0);
@@ -884,8 +920,8 @@ HD void visit_u(const Dims& D, const WS& w, double wQ, F f) {
   }
 }
 
-template <class F>
-HD void visit_g(const Dims& D, const WS& w, F f) {
+template <int G, class F>
+HD void visit_g(const Dims& D, const WS<G>& w, F f) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
   f(2, w.m(M_SCAL + S_GH2), 0.0); f(3, w.m(M_SCAL + S_GH3), 0.0); f(5, w.m(M_SCAL + S_GH5), 0.0);
   f(7, w.m(M_SCAL + S_GH7), 0.0); f(ir, w.m(M_SCAL + S_GHR0), 0.0); f(n - 2, w.m(M_SCAL + S_GHQE), 0.0);
@@ -900,10 +936,10 @@ HD void visit_g(const Dims& D, const WS& w, F f) {
 // Assemble and factor the dense W after factor_W (which leaves the chain
 // coefficients and functional/row-1 coefficients in place).
 template <int G>
-HD void dense_factor(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab& T, const WS& w, double d, double tau,
+HD void dense_factor(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab& T, const WS<G>& w, double d, double tau,
                      const Bg<double>& g) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
-  auto A = [&](int i, int j) -> double& { return w.e((long)i * n + j); };
+  auto A = [&](int i, int j) -> double& { return w.e(i * n + j); };
   const double itau = 1.0 / tau, op = g.opac;
   for (int i = gp.lane; i < n; i += G) {
     for (int j = 0; j < n; ++j) A(i, j) = (i == j) ? d : 0.0;
@@ -934,8 +970,8 @@ HD void dense_factor(const Grp<G>& gp, const ModeConst& m, const Dims& D, const 
     const int cidx[8] = {5, 6, 7, 8, 9, igp, igp + 1, igp + 2};
     for (int r = 0; r < 8; ++r) for (int cc = 0; cc < 8; ++cc) A(cidx[r], cidx[cc]) = core[r * 8 + cc];
     A(n - 2, n - 2) = de[0]; A(n - 2, n - 1) = de[1]; A(n - 1, n - 2) = de[2]; A(n - 1, n - 1) = de[3];
-    visit_u(D, w, g.wQ, [&](int i, double uh, double ue) {
-      visit_g(D, w, [&](int j, double gh, double ge) { A(i, j) -= uh * gh + ue * ge; });
+    visit_u<G>(D, w, g.wQ, [&](int i, double uh, double ue) {
+      visit_g<G>(D, w, [&](int j, double gh, double ge) { A(i, j) -= uh * gh + ue * ge; });
     });
     for (int j = 1; j < n; ++j) A(1, j) = (j == 1) ? d : 0.0;
     A(1, 0) = -w.v(V_JC0, 1);
@@ -945,7 +981,7 @@ HD void dense_factor(const Grp<G>& gp, const ModeConst& m, const Dims& D, const 
   }
   gp.sync();
   // LU with partial pivoting (first maximal |pivot|), rows over lanes
-  const long P0 = (long)n * n;
+  const int P0 = n * n;
   for (int kk = 0; kk < n; ++kk) {
     double best = -1.0;
     int bi = kk;
@@ -969,10 +1005,10 @@ HD void dense_factor(const Grp<G>& gp, const ModeConst& m, const Dims& D, const 
 }
 
 template <int G>
-HD void dense_solve(const Grp<G>& gp, const Dims& D, const WS& w, int vb) {
+HD void dense_solve(const Grp<G>& gp, const Dims& D, const WS<G>& w, int vb) {
   const int n = D.n;
-  const long P0 = (long)n * n;
-  auto A = [&](int i, int j) -> double { return w.e((long)i * n + j); };
+  const int P0 = n * n;
+  auto A = [&](int i, int j) -> double { return w.e(i * n + j); };
   if (gp.lead())
     for (int kk = 0; kk < n; ++kk) {
       const int p = (int)w.e(P0 + kk);
@@ -1009,7 +1045,7 @@ struct Run {
 
 // start a mode: start time, ICs, first step size (perturbations.py:742-756)
 template <int G>
-HD void mode_begin(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Ctl& ctl, const WS& w,
+HD void mode_begin(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Ctl& ctl, const WS<G>& w,
                    const double* tau_out, Run& r) {
   double tmax = LDG(tau_out), tmin = tmax;
   for (int o = 1; o < ctl.nout; ++o) { const double t = LDG(tau_out + o); tmax = t > tmax ? t : tmax; tmin = t < tmin ? t : tmin; }
@@ -1027,16 +1063,15 @@ HD void mode_begin(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const D
 // decision.  Returns true while the mode still needs steps.
 template <int G>
 HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, const Rodas& R,
-                  const Ctl& ctl, const WS& w, const double* tau_out, double* yout, long ostride, Run& r) {
+                  const Ctl& ctl, const WS<G>& w, const double* tau_out, double* yout, long ostride, Run& r) {
   if (!(r.t0 < r.T1)) return false;
   if (r.steps >= ctl.max_steps) { r.status = ST_MAX_STEPS; return false; }
   const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
   const double t0 = r.t0, dt = r.t1 - r.t0;
   const int vy = r.vy;
   // f(t0, y0) and d f / d a in one forward-mode pass
-  rhs<Dual, G>(gp, c, m, D, T, t0, w, vy, V_F, V_JC0);
   Bg<double> g;
-  background<double>(c, m, w.v(vy, 0), g);
+  rhs<Dual, G>(gp, c, m, D, T, t0, w, vy, V_F, V_JC0, &g);
   const double d = 1.0 / (dt * R.gamma);
   factor_W<G>(gp, c, m, D, T, w, d, t0, g);
   if (ctl.dense) dense_factor<G>(gp, m, D, T, w, d, t0, g);
@@ -1128,7 +1163,7 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
         } else {
           for (int j = gp.lane; j < n; j += G) { const double y0 = w.v(vy, j); w.v(V_U, j) = y0 + cf * (w.v(vy1, j) - y0); }
           gp.sync();
-          if (gp.lead()) outputs(c, m, D, w, V_U, dst, ostride);
+          if (gp.lead()) outputs<G>(c, m, D, w, V_U, dst, ostride);
         }
         gp.sync();
       }

@@ -77,13 +77,11 @@ __global__ void __launch_bounds__(kBlock) forward_lane_kernel(KParams P) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const long warp = tid >> 5;
-  deb::WS w;
+  deb::WS<1> w;
   w.p = P.ws + warp * 32 * P.slot_len + lane;
-  w.stride = 32;
   w.n = P.D.n;
-  w.misc0 = (long)deb::NV * P.D.n;
+  w.misc0 = deb::NV * P.D.n;
   w.dp = P.dws ? P.dws + warp * 32 * P.dense_len + lane : nullptr;
-  w.dstride = 32;
   const deb::Grp<1> gp{0};
   int mode = -1;
   deb::Cosmo c;
@@ -115,18 +113,15 @@ __global__ void __launch_bounds__(kBlock) forward_lane_kernel(KParams P) {
 }
 
 // One warp per mode: the mode's vectors and MISC block in shared memory.
-__global__ void __launch_bounds__(256) forward_warp_kernel(KParams P) {
+__global__ void __launch_bounds__(32) forward_warp_kernel(KParams P) {
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  const long gwarp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  deb::WS w;
-  w.p = P.smem ? smem + (long)wib * P.slot_len : P.ws + gwarp * P.slot_len;
-  w.stride = 1;
+  const long gwarp = blockIdx.x;
+  deb::WS<32> w;
+  w.p = P.smem ? smem : P.ws + gwarp * P.slot_len;
   w.n = P.D.n;
-  w.misc0 = (long)deb::NV * P.D.n;
+  w.misc0 = deb::NV * P.D.n;
   w.dp = P.dws ? P.dws + gwarp * P.dense_len : nullptr;
-  w.dstride = 1;
   const deb::Grp<32> gp{lane};
   deb::Cosmo c;
   deb::ModeConst mc;
@@ -258,7 +253,7 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
   // execution mode: lane per mode once the batch fills every SM sub-partition
   // with >= 1 warp of modes, else warp per mode
   int mode = dims->exec_mode;
-  if (mode == DEB_EXEC_AUTO) mode = ((long)max_modes >= (long)nsm * 4 * 32 && !p->dense) ? DEB_EXEC_LANE : DEB_EXEC_WARP;
+  if (mode == DEB_EXEC_AUTO) mode = DEB_EXEC_WARP;
   p->exec_mode = mode;
   // slot counts are capped at 16 GiB of workspace
   const long mem_cap = (16L << 30) / (per_slot * 8);
@@ -274,30 +269,24 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
     nslots = p->lane_slots;
   } else {
     const long slot_bytes = p->slot_len * 8;
-    int wpb = (int)((long)smem_optin / slot_bytes);
-    p->warp_smem = wpb >= 1;
-    if (wpb > 8) wpb = 8;
-    if (wpb < 1) wpb = 4;
-    p->warp_block_warps = wpb;
-    // blocks per SM limited by shared memory (228 KB per SM) and 32 warps per SM
-    int per_sm = 1;
+    p->warp_smem = slot_bytes <= smem_optin;
+    p->warp_block_warps = 1;
+    // blocks (= modes in flight) per SM limited by shared memory and by the
+    // 255-register budget of a 1-warp block (8 warps per SM)
+    int per_sm = 8;
     if (p->warp_smem) {
-      const long blk = slot_bytes * wpb;
-      per_sm = (int)((228L * 1024) / (blk + 1024));
+      const int by_smem = (int)((228L * 1024) / (slot_bytes + 1024));
+      if (by_smem < per_sm) per_sm = by_smem;
       if (per_sm < 1) per_sm = 1;
-      if (per_sm * wpb > 32) per_sm = 32 / wpb;
-    } else {
-      per_sm = 2;
     }
-    long cap_warps = (long)nsm * per_sm * wpb;
+    long cap_warps = (long)nsm * per_sm;
     if (cap_warps > mem_cap) cap_warps = mem_cap;
     long want = max_modes;
     long nw = want < cap_warps ? want : cap_warps;
-    p->warp_blocks = (int)((nw + wpb - 1) / wpb);
-    nslots = (long)p->warp_blocks * wpb;
+    p->warp_blocks = (int)nw;
+    nslots = nw;
     if (p->warp_smem) {
-      const int bytes = (int)(slot_bytes * wpb);
-      if (cudaFuncSetAttribute(forward_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) {
+      if (cudaFuncSetAttribute(forward_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)slot_bytes) != cudaSuccess) {
         delete p;
         return DEB_ERR_CUDA;
       }

@@ -13,7 +13,7 @@ using namespace deb;
 
 namespace {
 struct Ctx {
-  Dims D; Cosmo c; ModeConst m; Tab T; Rodas R; std::vector<double> buf, dbuf; WS w;
+  Dims D; Cosmo c; ModeConst m; Tab T; Rodas R; std::vector<double> buf, dbuf; WS<1> w;
 };
 const Grp<1> GP{0};
 bool setup(Ctx& x, const double* blob, int blob_len, const int* dims, double k, bool dense) {
@@ -21,10 +21,11 @@ bool setup(Ctx& x, const double* blob, int blob_len, const int* dims, double k, 
   if (!load_cosmo(blob, blob_len, x.c)) return false;
   mode_const(x.c, k, x.m);
   fill_tables(x.T); fill_rodas(x.R);
-  x.buf.assign(slot_len(x.D), 0.0);
-  x.dbuf.assign(dense ? dense_len(x.D) : 1, 0.0);
-  x.w.p = x.buf.data(); x.w.stride = 1; x.w.n = x.D.n; x.w.misc0 = (long)NV * x.D.n;
-  x.w.dp = x.dbuf.data(); x.w.dstride = 1;
+  // the one-thread-per-mode layout interleaves 32 modes; lane 0 is used here
+  x.buf.assign(slot_len(x.D) * 32, 0.0);
+  x.dbuf.assign(dense ? dense_len(x.D) * 32 : 1, 0.0);
+  x.w.p = x.buf.data(); x.w.n = x.D.n; x.w.misc0 = NV * x.D.n;
+  x.w.dp = x.dbuf.data();
   for (int i = 0; i < x.D.nq; ++i) {
     double q = x.c.q[i];
     x.w.m(M_Q + Q_DLF * x.D.nq + i) = -q / (1.0 + std::exp(-q));

