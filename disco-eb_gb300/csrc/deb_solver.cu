@@ -215,6 +215,7 @@ const char* deb_error_string(int code) {
     case DEB_ERR_CUDA: return "CUDA runtime error";
     case DEB_ERR_NOMEM: return "device allocation failed";
     case DEB_ERR_CAPACITY: return "plan capacity exceeded";
+    case DEB_ERR_STATIC_SCRATCH: return "one mode's solver state exceeds the static scratch array (DEB_STATIC_SCRATCH_BYTES)";
     default: return "unknown error";
   }
 }
@@ -366,6 +367,62 @@ int deb_get_power(const double* d_tables, int ncosmo, int blob_len, const double
   power_kernel<<<(unsigned)((tot + threads - 1) / threads), threads, 0, (cudaStream_t)stream>>>(
       d_tables, ncosmo, blob_len, d_k, d_cosmo_of_mode, nmode, nout, d_y, stride, idx, d_P);
   return cudaGetLastError() == cudaSuccess ? DEB_OK : DEB_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------- allocation-free entry point
+// Scratch of deb_forward_static: bytes [0, 256) hold the work-queue counter,
+// the rest holds one warp-mode slot per mode in flight.
+static __device__ __align__(256) double g_static_scratch[DEB_STATIC_SCRATCH_BYTES / sizeof(double)];
+static double* g_static_scratch_addr[64] = {nullptr};
+
+int deb_forward_static(const deb_dims* dims, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
+                       const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+                       double* d_y_out, int* d_status, int* d_steps, void* stream) {
+  if (!dims || !cfg || ncosmo <= 0 || nmode < 0 || blob_len <= deb::HDR_LEN) return DEB_ERR_INVALID;
+  if (dims->lmaxg < 3 || dims->lmaxgp < 3 || dims->lmaxr < 3 || dims->lmaxnu < 3 || dims->nqmax < 1 || dims->nout < 1)
+    return DEB_ERR_INVALID;
+  if (dims->lmaxg > deb::LMAX_TABLE || dims->lmaxgp > deb::LMAX_TABLE || dims->lmaxr > deb::LMAX_TABLE ||
+      dims->lmaxnu > deb::LMAX_TABLE)
+    return DEB_ERR_INVALID;
+  if (dims->linear_solver != DEB_SOLVE_STRUCTURED) return DEB_ERR_INVALID;
+  if (!(cfg->rtol >= 0.0) || !(cfg->atol >= 0.0) || cfg->max_steps <= 0 || !(cfg->error_order > 0.0)) return DEB_ERR_INVALID;
+  const deb::Dims D = deb::make_dims(dims->lmaxg, dims->lmaxgp, dims->lmaxr, dims->lmaxnu, dims->nqmax);
+  const long slot_len = deb::slot_len(D);
+  const long max_slots = (long)(DEB_STATIC_SCRATCH_BYTES - 256) / (slot_len * (long)sizeof(double));
+  if (max_slots < 1) return DEB_ERR_STATIC_SCRATCH;
+  if (nmode == 0) return DEB_OK;
+  if (!d_tables || !d_k || !d_tau_out || !d_y_out || !d_status) return DEB_ERR_INVALID;
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DEB_ERR_CUDA;
+  int rc = upload_constants();
+  if (rc) return rc;
+  if (!g_static_scratch_addr[dev]) {
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_static_scratch) != cudaSuccess || !ptr) return DEB_ERR_CUDA;
+    g_static_scratch_addr[dev] = (double*)ptr;
+  }
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return DEB_ERR_CUDA;
+  double* base = g_static_scratch_addr[dev];
+  cudaStream_t s = (cudaStream_t)stream;
+  KParams P;
+  P.tables = d_tables; P.ncosmo = ncosmo; P.blob_len = blob_len; P.k = d_k; P.cosmo = d_cosmo_of_mode;
+  P.nmode = nmode; P.tau_out = d_tau_out; P.y_out = d_y_out; P.status = d_status; P.steps = d_steps;
+  P.ws = base + 256 / sizeof(double); P.dws = nullptr; P.slot_len = slot_len; P.dense_len = 0;
+  P.queue = (int*)base; P.D = D; P.smem = 0;
+  P.ctl.rtol = cfg->rtol; P.ctl.atol = cfg->atol;
+  P.ctl.b1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / cfg->error_order;
+  P.ctl.b2 = -(cfg->pcoeff + 2.0 * cfg->dcoeff) / cfg->error_order;
+  P.ctl.b3 = cfg->dcoeff / cfg->error_order;
+  P.ctl.safety = cfg->safety; P.ctl.fmin = cfg->factormin; P.ctl.fmax = cfg->factormax;
+  P.ctl.max_steps = cfg->max_steps; P.ctl.hist_on_reject = cfg->hist_on_reject;
+  P.ctl.dense = 0; P.ctl.return_full = dims->return_full; P.ctl.nout = dims->nout;
+  long warps = (long)nsm * 8;
+  if (warps > max_slots) warps = max_slots;
+  if (warps > nmode) warps = nmode;
+  if (cudaMemsetAsync(P.queue, 0, sizeof(int), s) != cudaSuccess) return DEB_ERR_CUDA;
+  forward_warp_kernel<<<(unsigned)warps, 32, 0, s>>>(P);
+  if (cudaGetLastError() != cudaSuccess) return DEB_ERR_CUDA;
+  return DEB_OK;
 }
 
 int deb_measure_fp64_peak(double* flops_per_s, void* stream) {

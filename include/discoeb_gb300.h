@@ -46,7 +46,8 @@ enum deb_status {
   DEB_ERR_TABLES = -2,      /* table blob header / magic / sizes inconsistent */
   DEB_ERR_CUDA = -3,        /* a CUDA runtime call failed */
   DEB_ERR_NOMEM = -4,       /* device allocation for the plan failed */
-  DEB_ERR_CAPACITY = -5     /* more modes or variables than the plan was made for */
+  DEB_ERR_CAPACITY = -5,    /* more modes or variables than the plan was made for */
+  DEB_ERR_STATIC_SCRATCH = -6 /* deb_forward_static: one mode's state exceeds DEB_STATIC_SCRATCH_BYTES */
 };
 
 /* per-mode outcome written to d_status (same meaning as the oracle's) */
@@ -129,6 +130,36 @@ int deb_get_power(const double* d_tables, int ncosmo, int blob_len, const double
                   int nmode, int nout, const double* d_y, int stride, int idx, double* d_P, void* stream);
 
 void deb_plan_destroy(deb_plan* plan);
+
+/*
+ * Allocation-free variant of deb_forward.  No counterpart in the reference.
+ *
+ * Some callers cannot allocate device memory at all -- for example code that
+ * runs inside a host framework which owns every device buffer and passes them
+ * in (an XLA custom call, a serving process with a fixed memory pool).  They
+ * cannot create a plan, because deb_plan_create calls cudaMalloc.  This entry
+ * point needs no plan and allocates nothing: its scratch (the work-queue
+ * counter and the per-mode solver state) lives in one fixed array of
+ * DEB_STATIC_SCRATCH_BYTES compiled into the library, which every GPU that
+ * loads the library holds until the process exits.  The caller still passes
+ * all inputs and outputs, with the same meaning as for deb_forward.
+ *
+ *   - structured solver only (dims->linear_solver must be
+ *     DEB_SOLVE_STRUCTURED); one warp per mode with its state in the array;
+ *   - modes in flight are limited by the array (e.g. 348 at nvar 323, 1339 at
+ *     nvar 80); any nmode is processed through the work queue;
+ *   - returns DEB_ERR_STATIC_SCRATCH when one mode's state does not fit the
+ *     array;
+ *   - the first call on a device (with that device current) looks up the
+ *     array's device address with cudaGetSymbolAddress and uploads the
+ *     constant tables; make that first call before any stream capture;
+ *   - every call reuses the same array and resets the counter it needs, so
+ *     calls that overlap on the GPU (e.g. on two streams) race: serialise them.
+ */
+#define DEB_STATIC_SCRATCH_BYTES (16u << 20)
+int deb_forward_static(const deb_dims* dims, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
+                       const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+                       double* d_y_out, int* d_status, int* d_steps, void* stream);
 
 /* Measured-peak helper for roofline reporting: runs independent FP64 FMA
    chains on every SM and returns the achieved FP64 FLOP/s (FMA = 2).

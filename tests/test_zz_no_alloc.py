@@ -1,0 +1,79 @@
+"""The allocation-free entry point deb_forward_static against deb_forward.
+
+Callers that cannot allocate device memory -- code running inside a host
+framework that owns every device buffer, so neither it nor this library may
+call cudaMalloc -- use deb_forward_static instead of a plan.  Its scratch is a
+fixed array compiled into the library.  This test calls it through the C ABI
+twice in a row (the second call reuses the array the first one left behind)
+and compares each result with the planned entry point deb_forward, at the
+tolerance of the other GPU parity tests.  It is collected last so that a run
+stopping at the first failure has run every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+LCDM = dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=8, nqmax=3)
+
+
+def _c(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def test_static_entry_point_matches_planned_entry_point():
+    import torch
+
+    import discoeb_gb300.background as bg
+    import discoeb_gb300.tables as tb
+    from discoeb_gb300 import _native
+    from discoeb_gb300 import perturbations as pt
+    from discoeb_gb300.workloads import lcdm_massless_param
+
+    torch.cuda.set_device(0)
+    p = bg.evolve_background(param=lcdm_massless_param())
+    k = np.geomspace(1e-4, 1.0, 24)
+    a_out = [0.5, 1.0]
+    blob = tb.pack_cosmology(p, 3)
+    tau = tb.tau_of_a(p, a_out)
+    ref = pt.solve(blob[None], k, tau[None], rtol=1e-3, atol=1e-6, exec_mode="warp", **LCDM)
+
+    L = _native.load()
+    dev = torch.device("cuda", 0)
+    d_tab = torch.as_tensor(blob[None]).to(dev)
+    d_k = torch.as_tensor(k).to(dev)
+    d_tau = torch.as_tensor(tau[None]).to(dev)
+    d_y = torch.empty((k.size, len(a_out), 20), dtype=torch.float64, device=dev)
+    d_st = torch.empty(k.size, dtype=torch.int32, device=dev)
+    d_steps = torch.empty((k.size, 2), dtype=torch.int32, device=dev)
+    dims = pt._dims(nout=len(a_out), return_full=False, linear_solver="structured", **LCDM)
+    cfg = pt._cfg(1e-3, 1e-6, 0.25, 0.80, 0.0, 20.0, 0.3, 2048)
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        d_y.fill_(0.0)
+        d_st.fill_(-7)
+        rc = L.deb_forward_static(ctypes.byref(dims), _c(d_tab), 1, blob.shape[0], _c(d_k), None, k.size, _c(d_tau),
+                                  ctypes.byref(cfg), _c(d_y), _c(d_st), _c(d_steps), ctypes.c_void_p(stream.cuda_stream))
+        assert rc == 0, L.deb_error_string(rc)
+        torch.cuda.synchronize()
+        assert (d_st.cpu().numpy() == 0).all()
+        y = d_y.cpu().numpy()
+        np.testing.assert_allclose(y[:, :, 4] ** 2, ref[:, :, 4] ** 2, rtol=1e-6)
+        for f in (6, 8, 10):
+            np.testing.assert_allclose(y[:, :, f], ref[:, :, f], rtol=1e-6, atol=1e-9 * np.abs(ref[:, :, f]).max())
+
+
+def test_static_entry_point_rejects_state_beyond_the_array():
+    """A mode whose state exceeds DEB_STATIC_SCRATCH_BYTES is refused before any launch."""
+    from discoeb_gb300 import _native
+    from discoeb_gb300 import perturbations as pt
+
+    L = _native.load()
+    dims = pt._dims(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=100, nqmax=1200, nout=1, return_full=False,
+                    linear_solver="structured")
+    cfg = pt._cfg(1e-3, 1e-6, 0.25, 0.80, 0.0, 20.0, 0.3, 2048)
+    rc = L.deb_forward_static(ctypes.byref(dims), None, 1, 1000, None, None, 1, None, ctypes.byref(cfg), None, None,
+                              None, None)
+    assert rc == -6 and b"static scratch" in L.deb_error_string(rc)
