@@ -57,7 +57,7 @@ HD bool isfinite_(double x) { return isfinite(x); }
 // ------------------------------------------------------------------ blob layout
 enum { H_OMEGAM = 0, H_OMEGAB, H_OMEGADE, H_OMEGAK, H_GRHOM, H_GRHOG, H_GRHOR, H_NEFF, H_NMNU,
        H_AMNU, H_W0, H_WA, H_CS2DE, H_YHE, H_H0, H_TAUMIN, H_AS, H_NS, H_KP, H_NQ,
-       H_NSPL0 = 20, H_BLOBLEN = 27, H_MAGIC = 28, HDR_LEN = 32 };
+       H_NSPL0 = 20, H_BLOBLEN = 27, H_MAGIC = 28, H_DERIVED = 29, HDR_LEN = 32 };
 enum { SP_XE_LOGA = 0, SP_CS2A_LOGA, SP_LRHONU_LOGA, SP_LPNU_LOGA, SP_A_TAU, SP_TAU_A, SP_XE_TAU, NSPL };
 constexpr double TABLE_MAGIC = 20231103.0;
 
@@ -104,7 +104,9 @@ template <> HD double mk<double>(double v, double) { return v; }
 template <> HD Dual mk<Dual>(double v, double d) { return Dual(v, d); }
 
 // ------------------------------------------------------------------ tables
-struct Spl { const double *x, *y, *S; int n; };
+// x, y, S: the reference's spline fields; c: per-interval polynomial
+// coefficients (4 per interval); xf: knots rounded to FP32 for the search.
+struct Spl { const double *x, *y, *S, *c; const float* xf; int n; };
 
 struct Cosmo {
   const double* b;
@@ -127,33 +129,47 @@ HD bool load_cosmo(const double* b, int blob_len, Cosmo& c) {
   }
   c.q = p; c.w = p + c.nq;
   tot += 2 * c.nq;
+  const long doff = (long)LDG(b + H_DERIVED);
+  if (doff != tot) return false;
+  const double* dp = b + doff;
+  for (int s = 0; s < NSPL; ++s) {
+    const int n = c.sp[s].n;
+    c.sp[s].c = dp;
+    dp += 4 * (n - 1);
+    c.sp[s].xf = reinterpret_cast<const float*>(dp);
+    dp += (n + 1) / 2;
+    tot += 4 * (n - 1) + (n + 1) / 2;
+  }
   return tot <= blob_len && (int)LDG(b + H_BLOBLEN) == blob_len;
 }
 
 HD double hdr(const Cosmo& c, int i) { return LDG(c.b + i); }
 
-// left searchsorted clipped to [0, n-2] (spline_interpolation.py:143)
-HD int spl_locate(const Spl& s, double x) {
+// left searchsorted clipped to [0, n-2] (spline_interpolation.py:143): the
+// largest i with x[i] < xv, or 0.  An FP32 binary search on the rounded knots
+// lands within a knot or two; FP64 compares then fix the index exactly.
+HD int spl_locate(const Spl& s, double xv) {
+  const float xfv = (float)xv;
   int lo = 0, hi = s.n;
   while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (LDG(s.x + mid) < x) lo = mid + 1; else hi = mid;
+    const int mid = (lo + hi) >> 1;
+    if (LDG(s.xf + mid) < xfv) lo = mid + 1; else hi = mid;
   }
   int i = lo - 1;
   i = i < 0 ? 0 : i;
   i = i > s.n - 2 ? s.n - 2 : i;
+  while (i > 0 && !(LDG(s.x + i) < xv)) --i;
+  while (i < s.n - 2 && LDG(s.x + i + 1) < xv) ++i;
   return i;
 }
 
+// Natural cubic spline value (spline_interpolation.py:130-153) in polynomial
+// form about the left knot.
 template <class S> HD S spl_eval(const Spl& s, S x) {
-  int i = spl_locate(s, val(x));
-  double x0 = LDG(s.x + i), x1 = LDG(s.x + i + 1);
-  double h = x1 - x0;
-  S t = (x - x0) / h;
-  S A = 1.0 - t;
-  S B = t;
-  return A * LDG(s.y + i) + B * LDG(s.y + i + 1) +
-         ((A * A * A - A) * LDG(s.S + i) + (B * B * B - B) * LDG(s.S + i + 1)) * (h * h) / 6.0;
+  const int i = spl_locate(s, val(x));
+  const double* cf = s.c + 4 * i;
+  const S u = x - LDG(s.x + i);
+  return LDG(cf) + u * (LDG(cf + 1) + u * (LDG(cf + 2) + u * LDG(cf + 3)));
 }
 
 // ------------------------------------------------------------------ dimensions
@@ -181,7 +197,8 @@ enum { M_CORE = 0,          // 8x8 core LU (row-major)           64
        M_DE = 72,           // DE 2x2 LU + pivot flag              5
        M_CINV = 77,         // Woodbury capacitance inverse        4
        M_SCAL = 81,         // cached per-step scalars            24
-       M_Q = 105 };         // per-q arrays: v, dv/da, dlfdlq, ghq, geq, r1q, dTq  (7 nq)
+       M_CINV8 = 105,       // explicit inverse of the 8x8 core    64
+       M_Q = 169 };         // per-q arrays: v, dv/da, dlfdlq, ghq, geq, r1q, dTq  (7 nq)
 enum { Q_V = 0, Q_DV, Q_DLF, Q_GH, Q_GE, Q_R1, Q_DT, NQARR };
 enum { S_D = 0, S_W00I, S_ID, S_IDAH, S_GH2, S_GH3, S_GH5, S_GH7, S_GHR0, S_GHQE, S_GE4, S_GE6, S_GE8,
        S_GER1, S_GEQE, S_R13, S_R15, S_R17, S_R1R0, S_R1QE, S_R1QT, S_DTT, S_DTP, S_DTR };
@@ -225,6 +242,13 @@ struct Grp {
     return x;
   }
   HD Dual sum(Dual x) const { return Dual(sum(x.v), sum(x.d)); }
+  HD double bcast(double x, int src) const {
+#ifdef __CUDA_ARCH__
+    if (G > 1) return __shfl_sync(0xffffffffu, x, src);
+#endif
+    return x;
+  }
+  HD Dual bcast(Dual x, int src) const { return Dual(bcast(x.v, src), bcast(x.d, src)); }
   HD bool any(bool b) const {
 #ifdef __CUDA_ARCH__
     if (G > 1) return __any_sync(0xffffffffu, b);
@@ -281,17 +305,11 @@ HD void mode_const(const Cosmo& c, double k, ModeConst& m) {
 }
 
 template <class S>
-HD void background(const Cosmo& c, const ModeConst& m, S a, Bg<S>& g) {
-  g.a = a;
-  g.ia = 1.0 / a;
-  g.ia2 = g.ia * g.ia;
-  g.a2 = a * a;
-  g.la = dlog(a);
-  g.cs2 = spl_eval(c.sp[SP_CS2A_LOGA], g.la) * g.ia;
-  g.xe = spl_eval(c.sp[SP_XE_LOGA], g.la);
-  g.rhonu = dexp(spl_eval(c.sp[SP_LRHONU_LOGA], g.la));
-  // a^(-3(1+w0+wa)) exp(3(a-1) wa), background.py:111
-  g.rhoQ = dexp(m.pQ * g.la + 3.0 * (a - 1.0) * m.wa);
+HD void background_finish(const ModeConst& m, S a, Bg<S>& g, S cs2a, S xe, S rhonu, S rhoQ) {
+  g.cs2 = cs2a * g.ia;
+  g.xe = xe;
+  g.rhonu = rhonu;
+  g.rhoQ = rhoQ;
   S grho = m.grhom * m.Om * g.ia + (m.grhog + m.grhor * (m.Neff + m.Nmnu * g.rhonu)) * g.ia2 +
            m.grhom * m.ODE * g.rhoQ * g.a2 + m.grhom * m.Ok;
   g.aH = dsqrt(grho * (1.0 / 3.0));
@@ -301,6 +319,39 @@ HD void background(const Cosmo& c, const ModeConst& m, S a, Bg<S>& g) {
   g.ca2 = g.wQ - wQp / 3.0 / ((1.0 + g.wQ) + 1e-6) * g.iaH;
   g.opac = g.xe * m.akthom * g.ia2;
   g.pb43 = (4.0 / 3.0) * m.photbar0 * g.ia;
+}
+
+template <class S>
+HD void background_start(S a, Bg<S>& g) {
+  g.a = a;
+  g.ia = 1.0 / a;
+  g.ia2 = g.ia * g.ia;
+  g.a2 = a * a;
+  g.la = dlog(a);
+}
+
+template <class S>
+HD void background(const Cosmo& c, const ModeConst& m, S a, Bg<S>& g) {
+  background_start(a, g);
+  // a^(-3(1+w0+wa)) exp(3(a-1) wa), background.py:111
+  background_finish(m, a, g, spl_eval(c.sp[SP_CS2A_LOGA], g.la), spl_eval(c.sp[SP_XE_LOGA], g.la),
+                    dexp(spl_eval(c.sp[SP_LRHONU_LOGA], g.la)), dexp(m.pQ * g.la + 3.0 * (a - 1.0) * m.wa));
+}
+
+// The same with the three spline look-ups on lanes 0..2 and the two
+// exponentials on lanes 0..1 of a warp, broadcast by shuffles.
+template <class S, int G>
+HD void background_grp(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, S a, Bg<S>& g) {
+  if constexpr (G == 1) {
+    background(c, m, a, g);
+  } else {
+    background_start(a, g);
+    const int which = gp.lane == 1 ? SP_XE_LOGA : (gp.lane == 2 ? SP_LRHONU_LOGA : SP_CS2A_LOGA);
+    const S sv = spl_eval(c.sp[which], g.la);
+    const S cs2a = gp.bcast(sv, 0), xe = gp.bcast(sv, 1), lrhonu = gp.bcast(sv, 2);
+    const S ev = dexp(gp.lane == 0 ? lrhonu : S(m.pQ * g.la + 3.0 * (a - 1.0) * m.wa));
+    background_finish(m, a, g, cs2a, xe, gp.bcast(ev, 0), gp.bcast(ev, 1));
+  }
 }
 
 // conformal Hubble rate only (start time)
@@ -326,7 +377,7 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
   const double k = m.k, k2 = m.k2;
   const double itau = 1.0 / tau;
   Bg<S> g;
-  background<S>(c, m, make_var<S>(w.v(vin, 0)), g);
+  background_grp<S, G>(gp, c, m, make_var<S>(w.v(vin, 0)), g);
   if (gout) {
     gout->a = val(g.a); gout->ia = val(g.ia); gout->ia2 = val(g.ia2); gout->a2 = val(g.a2); gout->la = val(g.la);
     gout->cs2 = val(g.cs2); gout->xe = val(g.xe); gout->rhonu = val(g.rhonu); gout->rhoQ = val(g.rhoQ);
@@ -709,6 +760,15 @@ HD void factor_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab&
     w.m(M_SCAL + S_IDAH) = 1.0 / (d + g.aH);
   }
   gp.sync();
+  // explicit inverse of the core from its LU factors, one column per lane,
+  // so each stage's core solve is an 8-lane matrix-vector product
+  for (int col = gp.lane; col < 8; col += G) {
+    double r[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    r[col] = 1.0;
+    small_solve<8, G>(w, M_CORE, M_CPIV, r);
+    for (int i = 0; i < 8; ++i) w.m(M_CINV8 + i * 8 + col) = r[i];
+  }
+  gp.sync();
 }
 
 // z = M^{-1} r on indices >= 2, in place on vector vr.  Expects vr synced.
@@ -768,11 +828,16 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>
     }
   }
   gp.sync();
-  if (gp.lead()) {
-    double r[8] = {w.v(vr, 5), w.v(vr, 6), w.v(vr, 7), w.v(vr, 8), w.v(vr, 9), w.v(vr, igp), w.v(vr, igp + 1), w.v(vr, igp + 2)};
-    small_solve<8, G>(w, M_CORE, M_CPIV, r);
-    w.v(vr, 5) = r[0]; w.v(vr, 6) = r[1]; w.v(vr, 7) = r[2]; w.v(vr, 8) = r[3]; w.v(vr, 9) = r[4];
-    w.v(vr, igp) = r[5]; w.v(vr, igp + 1) = r[6]; w.v(vr, igp + 2) = r[7];
+  {
+    const int cidx[8] = {5, 6, 7, 8, 9, igp, igp + 1, igp + 2};
+    double r[8];
+    for (int j = 0; j < 8; ++j) r[j] = w.v(vr, cidx[j]);
+    gp.sync();
+    for (int row = gp.lane; row < 8; row += G) {
+      double z = 0.0;
+      for (int j = 0; j < 8; ++j) z += w.m(M_CINV8 + row * 8 + j) * r[j];
+      w.v(vr, cidx[row]) = z;
+    }
   }
   gp.sync();
   for (int t = gp.lane; t < 2; t += G) {

@@ -11,7 +11,9 @@ the C side of the layout is ``include/discoeb_gb300.h``):
   (``spline_interpolation.py:112-113`` fields ``_x_``, ``_y_``, ``_S_full_``)
   in the order of :data:`SPLINE_KEYS`;
 * the ``nq`` momentum nodes q and kernel weights w of
-  ``get_neutrino_momentum_bins`` (``background.py:13-44``).
+  ``get_neutrino_momentum_bins`` (``background.py:13-44``);
+* a derived section (offset in header slot 29): for each spline its
+  per-interval polynomial coefficients and its knots rounded to FP32.
 
 Splines are read duck-typed through ``_x_``, ``_y_``, ``_S_full_`` so a
 ``param`` produced by the reference's own ``evolve_background`` packs the
@@ -42,8 +44,36 @@ def _arr(x):
     return np.asarray(x, dtype=np.float64)
 
 
+H_DERIVED = 29   # offset of the derived section (polynomial coefficients, FP32 knots)
+
+
 def blob_length(spline_sizes, nq: int) -> int:
-    return HDR_LEN + 3 * int(sum(spline_sizes)) + 2 * nq
+    return HDR_LEN + 3 * int(sum(spline_sizes)) + 2 * nq + derived_length(spline_sizes)
+
+
+def derived_length(spline_sizes) -> int:
+    """Per spline: 4 (n-1) polynomial coefficients + n FP32 knots packed in ceil(n/2) doubles."""
+    return int(sum(4 * (n - 1) + (n + 1) // 2 for n in spline_sizes))
+
+
+def spline_derived(x, y, S):
+    """Per-interval coefficients of p(u) = c0 + u (c1 + u (c2 + u c3)), u = x - x_i.
+
+    The same natural cubic as the A/B form of spline_interpolation.py:150-152
+    (c0 = y_i, c1 = (y_{i+1}-y_i)/h - h (S_{i+1} + 2 S_i)/6, c2 = S_i/2,
+    c3 = (S_{i+1}-S_i)/(6h), spline_interpolation.py:94-101), so evaluation
+    needs no division; plus the knots rounded to FP32 for a fast search.
+    """
+    h = x[1:] - x[:-1]
+    c = np.empty((x.shape[0] - 1, 4))
+    c[:, 0] = y[:-1]
+    c[:, 1] = (y[1:] - y[:-1]) / h - h * (S[1:] + 2.0 * S[:-1]) / 6.0
+    c[:, 2] = S[:-1] / 2.0
+    c[:, 3] = (S[1:] - S[:-1]) / (6.0 * h)
+    xf = x.astype(np.float32)
+    if xf.shape[0] % 2:
+        xf = np.concatenate([xf, np.array([np.inf], dtype=np.float32)])
+    return c.ravel(), xf.view(np.float64)
 
 
 def pack_cosmology(param: dict, nqmax: int) -> np.ndarray:
@@ -83,6 +113,15 @@ def pack_cosmology(param: dict, nqmax: int) -> np.ndarray:
         p += 3 * n
     b[p:p + nqmax] = q
     b[p + nqmax:p + 2 * nqmax] = w
+    p += 2 * nqmax
+    b[H_DERIVED] = p
+    for (x, y, S) in splines:
+        cf, xf = spline_derived(x, y, S)
+        b[p:p + cf.shape[0]] = cf
+        p += cf.shape[0]
+        b[p:p + xf.shape[0]] = xf
+        p += xf.shape[0]
+    assert p == L
     return b
 
 

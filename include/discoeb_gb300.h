@@ -20,11 +20,15 @@
  * Table blob (FP64, one per cosmology, all blobs of one call the same length)
  *   [0..31]   header: Omegam, Omegab, OmegaDE, Omegak, grhom, grhog, grhor,
  *             Neff, Nmnu, amnu, w_DE_0, w_DE_a, cs2_DE, YHe, H0, taumin, A_s,
- *             n_s, k_p, nq, n_spline[7], blob_len, magic (20231103), 0, 0, 0
+ *             n_s, k_p, nq, n_spline[7], blob_len, magic (20231103),
+ *             derived_offset, 0, 0
  *   splines   7 x (x[n], y[n], S[n]) in the order xe(log a), c_s^2 a(log a),
  *             log rho_nu(log a), log p_nu(log a), a(tau), tau(a), xe(tau)
  *             (fields _x_, _y_, _S_full_ of spline_interpolation.py:112-113)
  *   nodes     q[nq], w[nq] of get_neutrino_momentum_bins (background.py:13-44)
+ *   derived   7 x (c[4(n-1)] polynomial coefficients of each interval,
+ *             p(u) = c0 + u (c1 + u (c2 + u c3)), u = x - x_i; then the
+ *             n knots as FP32, packed into ceil(n/2) doubles)
  */
 #ifndef DISCOEB_GB300_H
 #define DISCOEB_GB300_H

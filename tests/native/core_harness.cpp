@@ -76,6 +76,14 @@ int h_start(const double* blob, int blob_len, const int* dims, double k, double*
   return 0;
 }
 
+// spline evaluation as the kernel does it (FP32 search + FP64 fix-up, polynomial form)
+int h_spline(const double* blob, int blob_len, int which, const double* x, int nx, double* out, int* idx) {
+  Cosmo c; if (!load_cosmo(blob, blob_len, c)) return -2;
+  if (which < 0 || which >= NSPL) return -3;
+  for (int i = 0; i < nx; ++i) { out[i] = spl_eval(c.sp[which], x[i]); idx[i] = spl_locate(c.sp[which], x[i]); }
+  return 0;
+}
+
 // full per-mode solve with the kernel's driver, sequential over modes
 int h_solve(const double* tables, int ncosmo, int blob_len, const double* kmodes, const int* cosmo, int nmode,
             const double* tau_out, int nout, const int* dims, const double* cfg, int max_steps, int return_full,

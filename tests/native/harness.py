@@ -23,6 +23,7 @@ def lib():
         L = ctypes.CDLL(_LIB)
         L.h_rhs.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, ctypes.c_double, dp, dp, dp]
         L.h_solve_W.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, ctypes.c_double, dp, ctypes.c_double, dp, dp, ctypes.c_int]
+        L.h_spline.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, dp, ip]
         L.h_start.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, dp, dp]
         L.h_solve.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp, ip, ctypes.c_int, dp, ctypes.c_int, ip, dp, ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, dp, ip]
@@ -74,3 +75,12 @@ def solve(tables, kmodes, tau_out, *, cosmo_of_mode=None, lmaxg=11, lmaxgp=11, l
                        _p(st, ctypes.c_int))
     assert rc == 0, rc
     return y, st
+
+
+def spline(blob, which, x):
+    x = np.ascontiguousarray(np.atleast_1d(x), dtype=np.float64)
+    out = np.empty_like(x)
+    idx = np.empty(x.shape, dtype=np.int32)
+    rc = lib().h_spline(_p(blob), blob.shape[0], int(which), _p(x), x.shape[0], _p(out), _p(idx, ctypes.c_int))
+    assert rc == 0, rc
+    return out, idx

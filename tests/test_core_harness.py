@@ -94,3 +94,21 @@ def test_both_converge_to_tight_solution(lcdm, rtol):
     yh, _ = H.solve(blob, k, tau, rtol=rtol, atol=rtol * 1e-3, max_steps=400000, **LCDM)
     err = np.abs(yh[:, 0, 4] ** 2 / ref[:, 0, 4] ** 2 - 1).max()
     assert err < 100 * rtol
+
+
+def test_kernel_spline_matches_reference_form(fid):
+    """FP32 search + FP64 fix-up gives the left-searchsorted interval exactly,
+    and the polynomial form agrees with the A/B form of
+    spline_interpolation.py:150-152 at knots, interior points and outside."""
+    blob = tb.pack_cosmology(fid, 15)
+    for which, key in enumerate(tb.SPLINE_KEYS):
+        sp = fid[key]
+        x0 = sp._x_
+        x = np.concatenate([x0, x0[:-1] + 0.5 * np.diff(x0), np.nextafter(x0, np.inf), np.nextafter(x0, -np.inf),
+                            [x0[0] - 1.0, x0[-1] + 1.0]])
+        val, idx = H.spline(blob, which, x)
+        ref_idx = np.clip(np.searchsorted(x0, x, side="left") - 1, 0, x0.shape[0] - 2)
+        assert (idx == ref_idx).all(), key
+        ref = sp.evaluate(x)
+        scale = np.maximum(np.abs(sp._y_).max(), np.abs(ref))   # far extrapolation grows cubically
+        assert (np.abs(val - ref) <= 1e-13 * scale).all(), key
