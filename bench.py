@@ -1,15 +1,21 @@
 """Benchmark of the perturbation hot path on GB300.
 
-Workload (default): 64 cosmologies drawn uniformly over Omegam [.25,.35],
-Omegab [.04,.055], h [.6,.75], n_s [.92,1], ln(1e10 A_s) [2.9,3.2],
-m_nu [.06,.3] eV, w0 [-1.2,-.8], wa [-.3,.3] (w(a) = -1 crossings redrawn),
-each with 512 log-spaced k in [1e-4, 10] /Mpc, lmaxg=lmaxgp=12, lmaxr=17,
-lmaxnu=17, nqmax=15 (nvar 323), output at a=1, rtol=atol=1e-5: 32768 modes
-in one persistent launch.  A "step" is one full solve of that batch plus the
-P(k) assembly.  ``value`` is cosmologies (full k-grids) per second with the
-inputs resident on the device; ``e2e`` is the same through the public call
-with host inputs (tables, k-grid, output times copied in, all 20 output
-fields copied out, every step).
+Default workload (P(k) + d P / d theta): 8 cosmologies drawn uniformly over
+Omegam [.25,.35], Omegab [.04,.055], h [.6,.75], n_s [.92,1],
+ln(1e10 A_s) [2.9,3.2], m_nu [.06,.3] eV, w0 [-1.2,-.8], wa [-.3,.3]
+(w(a) = -1 crossings redrawn), each with 512 log-spaced k in [1e-4, 10] /Mpc,
+lmaxg=lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15 (nvar 323), output at a=1,
+rtol=atol=1e-5.  A "step" is one nominal solve of the 4096 modes (recording
+the accepted steps), one replay launch of the 12 perturbed table sets per
+cosmology (6 ODE parameters x +-eps, 49152 work items) and the P(k) /
+d log P / d theta assembly for theta = (Omegam, Omegab, h, n_s, A_s, m_nu,
+w0, wa).  ``value`` is cosmologies (full k-grid, P(k) and its 8-parameter
+gradient) per second with the inputs resident on the device; ``e2e`` is the
+same through the public call with host inputs (13 table sets per cosmology,
+k-grid, output times in; P(k) and the gradient out, every step).
+
+``--workload batched_64cosmo_512k_n323_rtol1e-5`` times the forward P(k)
+solve alone on 64 cosmologies (32768 modes).
 
 ``--impl reference`` times the CPU restatement of the reference algorithm
 (``oracle/``: Rodas5 + PID + dense forward-mode Jacobian + dense LU, FP64,
@@ -33,12 +39,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    # name: (ncosmo, num_k, kmin, kmax, dims, rtol, atol)
+    # name: (ncosmo, num_k, kmin, kmax, dims, rtol, atol); names ending in _grad include d P / d theta
+    "batched_8cosmo_512k_n323_rtol1e-5_grad": (8, 512, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
     "batched_64cosmo_512k_n323_rtol1e-5": (64, 512, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
     "batched_8cosmo_512k_n323_rtol1e-5": (8, 512, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
     "single_1cosmo_256k_n323_rtol1e-5": (1, 256, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
 }
-DEFAULT_WORKLOAD = "batched_64cosmo_512k_n323_rtol1e-5"
+DEFAULT_WORKLOAD = "batched_8cosmo_512k_n323_rtol1e-5_grad"
 
 
 def _dist():
@@ -50,19 +57,34 @@ def _dist():
 
 def make_inputs(name, rank=0, world=1, seed=1234):
     from discoeb_gb300 import background, tables
+    from discoeb_gb300.gradient import evolve_backgrounds, perturbed_params
     from discoeb_gb300.workloads import sample_cosmologies
 
     ncosmo, num_k, kmin, kmax, dims, rtol, atol = WORKLOADS[name]
+    grad = name.endswith("_grad")
     params, rejected = sample_cosmologies(ncosmo * world, seed=seed)
     mine = params[rank * ncosmo:(rank + 1) * ncosmo]
-    ps = [background.evolve_background(param=p) for p in mine]
+    pert, bgs = None, None
+    if grad:
+        pert = [perturbed_params(p) for p in mine]
+        flat = []
+        for p, pp in zip(mine, pert):
+            flat.append(p)
+            for (_, _, a, b) in pp:
+                flat += [a, b]
+        ev = evolve_backgrounds(flat)
+        nset1 = 1 + 2 * len(pert[0])
+        bgs = [ev[i * nset1:(i + 1) * nset1] for i in range(len(mine))]
+        ps = [b[0] for b in bgs]
+    else:
+        ps = [background.evolve_background(param=p) for p in mine]
     tabs = tables.pack_batch(ps, dims["nqmax"])
     tau = np.stack([tables.tau_of_a(p, [1.0]) for p in ps])
     k = np.geomspace(kmin, kmax, num_k)
     kk = np.tile(k, ncosmo)
     com = np.repeat(np.arange(ncosmo, dtype=np.int32), num_k)
     return dict(ps=ps, tables=tabs, tau=tau, k=kk, cosmo=com, dims=dims, rtol=rtol, atol=atol, ncosmo=ncosmo,
-                num_k=num_k, rejected=rejected)
+                num_k=num_k, rejected=rejected, grad=grad, params=mine, pert=pert, bgs=bgs, kgrid=k)
 
 
 class ClockSampler:
@@ -133,8 +155,10 @@ def cpu_baseline(inp, seconds=20.0, threads=0):
             break
         stride = max(1, stride // 2)
     per_mode = t_used / done_modes
-    return {"value": 1.0 / (per_mode * num_k), "unit": "cosmology solves/s", "cores": threads, "kind": "port",
-            "sample": f"{done_modes} modes of cosmology 0 (k strided over the 512-point grid), {t_used:.1f} s"}
+    solves = 13 if inp.get("grad") else 1   # nominal + 6 parameters x +-eps by central differences
+    return {"value": 1.0 / (per_mode * num_k * solves), "unit": "cosmology solves/s", "cores": threads, "kind": "port",
+            "sample": f"{done_modes} modes of cosmology 0 (k strided over the 512-point grid), {t_used:.1f} s"
+                      + (", x13 solves per cosmology for the 6 ODE gradients (+-eps) and the nominal P(k)" if solves > 1 else "")}
 
 
 def algorithmic_flops_per_step(dims, nq):
@@ -166,6 +190,8 @@ def run_ours(args):
 
     inp = make_inputs(args.workload, rank, world)
     dims = inp["dims"]
+    if inp["grad"]:
+        return run_gradient(args, inp, world, rank, local)
     prob = deb.DeviceProblem(inp["tables"], inp["k"], inp["tau"], inp["cosmo"], exec_mode=args.exec_mode, **dims)
     cfg = pt._cfg(inp["rtol"], inp["atol"], 0.25, 0.80, 0.0, 20.0, 0.3, args.max_steps)
     stream = torch.cuda.current_stream()
@@ -252,6 +278,96 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_gradient(args, inp, world, rank, local):
+    """P(k) + 8-parameter gradient per cosmology: record + replay launches."""
+    import torch
+
+    import discoeb_gb300 as deb
+    from discoeb_gb300 import _native
+    from discoeb_gb300.gradient import GradientProblem
+
+    dims = inp["dims"]
+    gp = GradientProblem(inp["params"], inp["bgs"], inp["pert"], inp["kgrid"], [1.0], rtol=inp["rtol"],
+                         atol=inp["atol"], max_steps=args.max_steps, **dims)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        gp.run(stream)
+    torch.cuda.synchronize()
+    gp.check()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            gp.run(stream, evs[i])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if world > 1:
+        torch.distributed.barrier()
+    rec_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    rep_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    t_step = wall / args.steps
+    if world > 1:
+        tt = torch.tensor([t_step], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(tt.item())
+    total_cosmo = inp["ncosmo"] * world
+    value = total_cosmo / t_step
+
+    # end to end through the public call from host buffers (tables for theta and theta +- eps)
+    e2e_steps = max(1, min(args.steps, 2))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        P, D, _ = deb.evolve_perturbations_grad(params=inp["params"], aexp_out=[1.0], kmin=inp["kgrid"][0],
+                                                kmax=inp["kgrid"][-1], num_k=inp["num_k"], rtol=inp["rtol"],
+                                                atol=inp["atol"], max_steps=args.max_steps, backgrounds=inp["bgs"],
+                                                **dims)
+    torch.cuda.synchronize()
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    h2d = (gp.host_tab0.nbytes + gp.host_tabs.nbytes + gp.host_tau0.nbytes + gp.host_taus.nbytes + gp.host_k.nbytes
+           + gp.host_com.nbytes)
+    d2h = int(P.nbytes + D.nbytes) + 4 * (gp.nmode * (1 + gp.nset))
+
+    peak = _native.measure_fp64_peak(stream.cuda_stream)
+    att = int(gp.d_steps.sum().item())
+    rep = int(gp.d_nrec.sum().item()) * gp.nset
+    flops = algorithmic_flops_per_step(dims, dims["nqmax"]) * (att + rep)
+    kern_s = (statistics.median(rec_ms) + statistics.median(rep_ms)) * 1e-3
+    achieved = flops / kern_s
+    out = {
+        "metric": "P(k)+dP/dtheta solves/s on 1 GB300, batched FP64 (8 parameters; structured Rodas5, frozen-step tangents)",
+        "value": value, "unit": "cosmology solves/s (P(k) + 8-parameter gradient)", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded cosmology sample, host RECFAST tables for theta and theta +- 1e-4 theta)",
+        "config": {"workload": args.workload, "ncosmo_per_gpu": inp["ncosmo"], "num_k": inp["num_k"],
+                   "modes_per_step": gp.nmode, "replay_items_per_step": gp.nmode * gp.nset, "nvar": 323,
+                   "rtol": inp["rtol"], "theta": list(gp.theta), "gradient": "central differences on the frozen step sequence",
+                   "l2": "per-mode state in shared memory; tables %.1f MB read per step" % ((gp.host_tab0.nbytes + gp.host_tabs.nbytes) / 1e6),
+                   "redrawn_cosmologies": inp["rejected"]},
+        "e2e": {"value": total_cosmo / t_e2e if world == 1 else None, "unit": "cosmology solves/s (P(k) + 8-parameter gradient)",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "note": "FP64-pipe bound (state in shared memory); peak = FP64 FMA microkernel measured in this run; "
+                             "achieved = algorithmic FLOPs of the structured Rodas5 step x (attempted + replayed steps)"},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk.summary(),
+        "forward_value": total_cosmo / (statistics.median(rec_ms) * 1e-3),
+        "record_ms_median": statistics.median(rec_ms), "replay_ms_median": statistics.median(rep_ms),
+        "attempted_steps_per_launch": att, "replayed_steps_per_launch": rep,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(inp, seconds=args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def run_reference(args):
     world, rank, local = _dist()
     if rank != 0:
@@ -264,8 +380,11 @@ def run_reference(args):
         if i >= args.warmup:
             vals.append(cb["value"])
     v = statistics.median(vals)
-    out = {"impl": "reference", "metric": "P(k) forward solves/s on 1 GB300, batched FP64 structured Rodas5 (gradient not included)",
-           "value": v * 1.0, "unit": "cosmology solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+    metric = ("P(k)+dP/dtheta solves/s on 1 GB300, batched FP64 (8 parameters; structured Rodas5, frozen-step tangents)"
+              if inp["grad"] else "P(k) forward solves/s on 1 GB300, batched FP64 structured Rodas5 (gradient not included)")
+    out = {"impl": "reference", "metric": metric,
+           "value": v * 1.0, "unit": "cosmology solves/s" + (" (P(k) + 8-parameter gradient)" if inp["grad"] else ""),
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded cosmology sample, host RECFAST tables)",
            "config": {"workload": args.workload, "ncosmo_per_gpu": inp["ncosmo"], "num_k": inp["num_k"]},

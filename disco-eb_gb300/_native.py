@@ -31,7 +31,8 @@ class DebSolverCfg(ctypes.Structure):
 
 
 _lib = None
-EXPORTS = ("deb_nvar", "deb_plan_create", "deb_plan_workspace_bytes", "deb_forward", "deb_forward_static", "deb_get_power",
+EXPORTS = ("deb_nvar", "deb_plan_create", "deb_plan_workspace_bytes", "deb_forward", "deb_forward_static",
+           "deb_forward_record", "deb_replay", "deb_get_power",
            "deb_plan_destroy", "deb_measure_fp64_peak", "deb_error_string", "deb_version")
 
 
@@ -53,6 +54,10 @@ def load(path: str | None = None):
                               ctypes.POINTER(DebSolverCfg), vp, vp, vp, vp]
     L.deb_forward_static.argtypes = [ctypes.POINTER(DebDims), vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp,
                                      ctypes.POINTER(DebSolverCfg), vp, vp, vp, vp]
+    L.deb_forward_record.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp,
+                                     ctypes.POINTER(DebSolverCfg), vp, vp, vp, vp, ctypes.c_int, vp, vp]
+    L.deb_replay.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp,
+                             ctypes.POINTER(DebSolverCfg), vp, ctypes.c_int, vp, vp, vp, vp]
     L.deb_get_power.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
                                 ctypes.c_int, vp, vp]
     L.deb_plan_destroy.argtypes = [vp]

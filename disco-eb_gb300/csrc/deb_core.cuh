@@ -1100,12 +1100,17 @@ HD void dense_solve(const Grp<G>& gp, const Dims& D, const WS<G>& w, int vb) {
 struct Ctl {
   double rtol, atol, b1, b2, b3, safety, fmin, fmax;
   int max_steps, hist_on_reject, dense, return_full, nout;
+  int record;   // store tau_start and every accepted step's end time
+  int replay;   // take the stored step times instead of controlling the step
 };
 
 // Integration state; every lane of a group holds an identical copy.
+// rec: [tau_start, t_1, ..., t_nrec] of the nominal run (record / replay).
 struct Run {
   double t0, t1, T1, prev_inv, prev_prev_inv;
   int vy, vy1, steps, acc, rej, status;
+  double* rec;
+  int rec_cap, nrec;
 };
 
 // start a mode: start time, ICs, first step size (perturbations.py:742-756)
@@ -1114,12 +1119,23 @@ HD void mode_begin(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const D
                    const double* tau_out, Run& r) {
   double tmax = LDG(tau_out), tmin = tmax;
   for (int o = 1; o < ctl.nout; ++o) { const double t = LDG(tau_out + o); tmax = t > tmax ? t : tmax; tmin = t < tmin ? t : tmin; }
-  const double ts = start_time(c, m);
-  const double t0 = 0.99 * (tmin < ts ? tmin : ts);
+  double t0;
+  if (ctl.replay) {
+    t0 = r.rec[0];
+  } else {
+    const double ts = start_time(c, m);
+    t0 = 0.99 * (tmin < ts ? tmin : ts);
+  }
   initial_conditions<G>(gp, c, m, D, t0, w, V_Y);
   r.t0 = t0; r.T1 = tmax;
-  const double dt0 = (t0 / 4.0 < 0.5 * (tmax - t0)) ? t0 / 4.0 : 0.5 * (tmax - t0);
-  r.t1 = t0 + dt0 < tmax ? t0 + dt0 : tmax;
+  if (ctl.replay) {
+    const double tn = r.nrec > 1 ? LDG(r.rec + 1) : tmax;
+    r.t1 = (r.nrec <= 1 || tn >= tmax) ? tmax : tn;
+  } else {
+    const double dt0 = (t0 / 4.0 < 0.5 * (tmax - t0)) ? t0 / 4.0 : 0.5 * (tmax - t0);
+    r.t1 = t0 + dt0 < tmax ? t0 + dt0 : tmax;
+    if (ctl.record && gp.lead()) r.rec[0] = t0;
+  }
   r.prev_inv = 1.0; r.prev_prev_inv = 1.0;
   r.vy = V_Y; r.vy1 = V_Y1; r.steps = 0; r.acc = 0; r.rej = 0; r.status = ST_OK;
 }
@@ -1201,10 +1217,10 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
     const double sc = w.v(vk8, j) / (ctl.atol + (y0 > y1 ? y0 : y1) * ctl.rtol) * ew[q];
     ss += sc * sc;
   }
-  const double err = sqrt(ss / 6.0);
+  const double err = ctl.replay ? 0.0 : sqrt(ss / 6.0);
   ++r.steps;
-  if (!isfinite_(err)) { r.status = ST_NONFINITE; return false; }
-  const bool keep = err < 1.0;
+  if (!isfinite_(err) || (ctl.replay && bad)) { r.status = ST_NONFINITE; return false; }
+  const bool keep = ctl.replay ? true : err < 1.0;
   double inv = 1.0 / err;
   const double f1 = ctl.b1 == 0.0 ? 1.0 : pow(inv, ctl.b1);
   const double f2 = ctl.b2 == 0.0 ? 1.0 : pow(r.prev_inv, ctl.b2);
@@ -1237,6 +1253,16 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
     r.t0 = r.t1;
     r.prev_prev_inv = r.prev_inv;
     r.prev_inv = inv;
+    if (ctl.record && gp.lead() && r.acc < r.rec_cap) r.rec[r.acc] = r.t1;
+    if (ctl.replay) {
+      // next recorded end time; the run ends at this cosmology's own final
+      // output time (the recorded one is the nominal cosmology's)
+      if (r.t0 >= r.T1) return false;
+      double tn = r.acc + 1 < r.nrec ? LDG(r.rec + r.acc + 1) : r.T1;
+      if (r.acc + 1 >= r.nrec || tn >= r.T1) tn = r.T1;
+      r.t1 = tn;
+      return true;
+    }
   } else {
     ++r.rej;
     if (ctl.hist_on_reject) { r.prev_prev_inv = r.prev_inv; r.prev_inv = inv; }

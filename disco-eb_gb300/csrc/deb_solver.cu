@@ -45,29 +45,44 @@ struct KParams {
   long slot_len, dense_len;
   int smem;           // warp mode: slots live in dynamic shared memory
   int* queue;
+  // record / replay of the accepted step times (frozen-step tangents)
+  double* rec;        // [nmode, rec_len]
+  int rec_len;
+  int* nrec;          // [nmode]
+  int nset;           // replay: table sets per cosmology; work item = set * nmode + mode
   deb::Ctl ctl;
   deb::Dims D;
 };
 
-// Validate mode m and load its cosmology; fills NaN outputs.  Same on every lane.
-__device__ bool prepare_mode(const KParams& P, int m, deb::Cosmo& c, deb::ModeConst& mc, const double*& tau_out,
-                             double*& yout, int lane, int G) {
+// Validate work item w and load its cosmology; fills NaN outputs and the
+// run's record pointers.  Same on every lane.  Work item = mode, or in a
+// replay set * nmode + mode.
+__device__ bool prepare_mode(const KParams& P, int w, deb::Cosmo& c, deb::ModeConst& mc, const double*& tau_out,
+                             double*& yout, deb::Run& run, int lane, int G) {
   const int osz = P.ctl.return_full ? P.D.n : DEB_NOUT_FIELDS;
+  const int m = P.ctl.replay ? w % P.nmode : w;
+  const int set = P.ctl.replay ? w / P.nmode : 0;
   const int ci = P.cosmo ? P.cosmo[m] : 0;
   const double k = P.k[m];
-  double* dst = P.y_out + (long)m * P.ctl.nout * osz;
+  double* dst = P.y_out + (long)w * P.ctl.nout * osz;
   for (int i = lane; i < P.ctl.nout * osz; i += G) dst[i] = __longlong_as_double(0x7ff8000000000000LL);
   bool ok = ci >= 0 && ci < P.ncosmo && k > 0.0 && isfinite(k);
-  if (ok) ok = deb::load_cosmo(P.tables + (long)ci * P.blob_len, P.blob_len, c) && c.nq == P.D.nq;
+  const int ti = ci * P.nset + set;
+  if (ok) ok = deb::load_cosmo(P.tables + (long)ti * P.blob_len, P.blob_len, c) && c.nq == P.D.nq;
+  run.rec = P.rec ? P.rec + (long)m * P.rec_len : nullptr;
+  run.rec_cap = P.rec_len - 1;
+  run.nrec = (P.ctl.replay && P.nrec) ? P.nrec[m] : 0;
+  if (ok && P.ctl.replay) ok = run.nrec >= 1 && run.nrec <= run.rec_cap;
   if (!ok) {
     if (lane == 0) {
-      P.status[m] = deb::ST_BAD_INPUT;
-      if (P.steps) { P.steps[2 * m] = 0; P.steps[2 * m + 1] = 0; }
+      P.status[w] = deb::ST_BAD_INPUT;
+      if (P.steps) { P.steps[2 * w] = 0; P.steps[2 * w + 1] = 0; }
+      if (P.ctl.record && P.nrec) P.nrec[m] = 0;
     }
     return false;
   }
   deb::mode_const(c, k, mc);
-  tau_out = P.tau_out + (long)ci * P.ctl.nout;
+  tau_out = P.tau_out + (long)ti * P.ctl.nout;
   yout = dst;
   return true;
 }
@@ -92,9 +107,9 @@ __global__ void __launch_bounds__(kBlock) forward_lane_kernel(KParams P) {
   auto fetch = [&]() -> bool {
     for (;;) {
       const int m = atomicAdd(P.queue, 1);
-      if (m >= P.nmode) return false;
+      if (m >= P.nmode * P.nset) return false;
       mode = m;
-      if (!prepare_mode(P, m, c, mc, tau_out, yout, 0, 1)) continue;
+      if (!prepare_mode(P, m, c, mc, tau_out, yout, run, 0, 1)) continue;
       deb::mode_begin<1>(gp, c, mc, P.D, P.ctl, w, tau_out, run);
       return true;
     }
@@ -106,6 +121,7 @@ __global__ void __launch_bounds__(kBlock) forward_lane_kernel(KParams P) {
       if (!more) {
         P.status[mode] = run.status;
         if (P.steps) { P.steps[2 * mode] = run.acc; P.steps[2 * mode + 1] = run.rej; }
+        if (P.ctl.record && P.nrec) P.nrec[mode] = run.status == deb::ST_OK ? run.acc : 0;
         active = fetch();
       }
     }
@@ -132,13 +148,14 @@ __global__ void __launch_bounds__(32) forward_warp_kernel(KParams P) {
     int m = 0;
     if (lane == 0) m = atomicAdd(P.queue, 1);
     m = __shfl_sync(0xffffffffu, m, 0);
-    if (m >= P.nmode) break;
-    if (!prepare_mode(P, m, c, mc, tau_out, yout, lane, 32)) continue;
+    if (m >= P.nmode * P.nset) break;
+    if (!prepare_mode(P, m, c, mc, tau_out, yout, run, lane, 32)) continue;
     deb::mode_begin<32>(gp, c, mc, P.D, P.ctl, w, tau_out, run);
     while (deb::mode_step<32>(gp, c, mc, P.D, c_tab, c_rodas, P.ctl, w, tau_out, yout, 1, run)) {}
     if (lane == 0) {
       P.status[m] = run.status;
       if (P.steps) { P.steps[2 * m] = run.acc; P.steps[2 * m + 1] = run.rej; }
+      if (P.ctl.record && P.nrec) P.nrec[m] = run.status == deb::ST_OK ? run.acc : 0;
     }
     __syncwarp();
   }
@@ -320,20 +337,29 @@ void deb_plan_destroy(deb_plan* p) {
   delete p;
 }
 
-int deb_forward(deb_plan* p, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
-                const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
-                double* d_y_out, int* d_status, int* d_steps, void* stream) {
-  if (!p || !cfg || ncosmo <= 0 || nmode < 0 || blob_len <= deb::HDR_LEN) return DEB_ERR_INVALID;
+}  // extern "C"
+
+namespace {
+
+int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, int blob_len, const double* d_k,
+                   const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+                   double* d_y_out, int* d_status, int* d_steps, double* d_record, int rec_len, int* d_nrec,
+                   int record, int replay, void* stream) {
+  if (!p || !cfg || ncosmo <= 0 || nset <= 0 || nmode < 0 || blob_len <= deb::HDR_LEN) return DEB_ERR_INVALID;
   if (nmode == 0) return DEB_OK;
   if (!d_tables || !d_k || !d_tau_out || !d_y_out || !d_status) return DEB_ERR_INVALID;
-  if (nmode > p->max_modes) return DEB_ERR_CAPACITY;
+  if ((long)nmode * nset > p->max_modes) return DEB_ERR_CAPACITY;
   if (!(cfg->rtol >= 0.0) || !(cfg->atol >= 0.0) || cfg->max_steps <= 0 || !(cfg->error_order > 0.0)) return DEB_ERR_INVALID;
+  if ((record || replay) && (!d_record || !d_nrec || rec_len < 2)) return DEB_ERR_INVALID;
+  if (record && rec_len < cfg->max_steps + 1) return DEB_ERR_INVALID;
+  if (replay && p->exec_mode != DEB_EXEC_WARP) return DEB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   KParams P;
   P.tables = d_tables; P.ncosmo = ncosmo; P.blob_len = blob_len; P.k = d_k; P.cosmo = d_cosmo_of_mode;
   P.nmode = nmode; P.tau_out = d_tau_out; P.y_out = d_y_out; P.status = d_status; P.steps = d_steps;
   P.ws = p->ws; P.dws = p->dws; P.slot_len = p->slot_len; P.dense_len = p->dense_len; P.queue = p->queue; P.D = p->D;
   P.smem = p->warp_smem;
+  P.rec = d_record; P.rec_len = rec_len; P.nrec = d_nrec; P.nset = nset;
   P.ctl.rtol = cfg->rtol; P.ctl.atol = cfg->atol;
   P.ctl.b1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / cfg->error_order;
   P.ctl.b2 = -(cfg->pcoeff + 2.0 * cfg->dcoeff) / cfg->error_order;
@@ -341,20 +367,49 @@ int deb_forward(deb_plan* p, const double* d_tables, int ncosmo, int blob_len, c
   P.ctl.safety = cfg->safety; P.ctl.fmin = cfg->factormin; P.ctl.fmax = cfg->factormax;
   P.ctl.max_steps = cfg->max_steps; P.ctl.hist_on_reject = cfg->hist_on_reject;
   P.ctl.dense = p->dense; P.ctl.return_full = p->return_full; P.ctl.nout = p->nout;
+  P.ctl.record = record; P.ctl.replay = replay;
   if (cudaMemsetAsync(p->queue, 0, sizeof(int), s) != cudaSuccess) return DEB_ERR_CUDA;
+  const long items = (long)nmode * nset;
   if (p->exec_mode == DEB_EXEC_LANE) {
-    long need = ((long)nmode + kBlock - 1) / kBlock;
+    long need = (items + kBlock - 1) / kBlock;
     const int blocks = (int)(need < p->lane_blocks ? need : p->lane_blocks);
     forward_lane_kernel<<<blocks, kBlock, 0, s>>>(P);
   } else {
     const int wpb = p->warp_block_warps;
-    long need = ((long)nmode + wpb - 1) / wpb;
+    long need = (items + wpb - 1) / wpb;
     const int blocks = (int)(need < p->warp_blocks ? need : p->warp_blocks);
     const size_t smem = p->warp_smem ? (size_t)p->slot_len * 8 * wpb : 0;
     forward_warp_kernel<<<blocks, 32 * wpb, smem, s>>>(P);
   }
   if (cudaGetLastError() != cudaSuccess) return DEB_ERR_CUDA;
   return DEB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int deb_forward(deb_plan* p, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
+                const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+                double* d_y_out, int* d_status, int* d_steps, void* stream) {
+  return launch_forward(p, d_tables, ncosmo, 1, blob_len, d_k, d_cosmo_of_mode, nmode, d_tau_out, cfg, d_y_out,
+                        d_status, d_steps, nullptr, 0, nullptr, 0, 0, stream);
+}
+
+int deb_forward_record(deb_plan* p, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
+                       const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+                       double* d_y_out, int* d_status, int* d_steps, double* d_record, int rec_len, int* d_nrec,
+                       void* stream) {
+  return launch_forward(p, d_tables, ncosmo, 1, blob_len, d_k, d_cosmo_of_mode, nmode, d_tau_out, cfg, d_y_out,
+                        d_status, d_steps, d_record, rec_len, d_nrec, 1, 0, stream);
+}
+
+int deb_replay(deb_plan* p, const double* d_tables, int ncosmo, int nset, int blob_len, const double* d_k,
+               const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+               const double* d_record, int rec_len, const int* d_nrec, double* d_y_out, int* d_status, void* stream) {
+  return launch_forward(p, d_tables, ncosmo, nset, blob_len, d_k, d_cosmo_of_mode, nmode, d_tau_out, cfg, d_y_out,
+                        d_status, nullptr, const_cast<double*>(d_record), rec_len, const_cast<int*>(d_nrec), 0, 1,
+                        stream);
 }
 
 int deb_get_power(const double* d_tables, int ncosmo, int blob_len, const double* d_k, const int* d_cosmo_of_mode,
@@ -409,6 +464,7 @@ int deb_forward_static(const deb_dims* dims, const double* d_tables, int ncosmo,
   P.nmode = nmode; P.tau_out = d_tau_out; P.y_out = d_y_out; P.status = d_status; P.steps = d_steps;
   P.ws = base + 256 / sizeof(double); P.dws = nullptr; P.slot_len = slot_len; P.dense_len = 0;
   P.queue = (int*)base; P.D = D; P.smem = 0;
+  P.rec = nullptr; P.rec_len = 0; P.nrec = nullptr; P.nset = 1;
   P.ctl.rtol = cfg->rtol; P.ctl.atol = cfg->atol;
   P.ctl.b1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / cfg->error_order;
   P.ctl.b2 = -(cfg->pcoeff + 2.0 * cfg->dcoeff) / cfg->error_order;
@@ -416,6 +472,7 @@ int deb_forward_static(const deb_dims* dims, const double* d_tables, int ncosmo,
   P.ctl.safety = cfg->safety; P.ctl.fmin = cfg->factormin; P.ctl.fmax = cfg->factormax;
   P.ctl.max_steps = cfg->max_steps; P.ctl.hist_on_reject = cfg->hist_on_reject;
   P.ctl.dense = 0; P.ctl.return_full = dims->return_full; P.ctl.nout = dims->nout;
+  P.ctl.record = 0; P.ctl.replay = 0;
   long warps = (long)nsm * 8;
   if (warps > max_slots) warps = max_slots;
   if (warps > nmode) warps = nmode;

@@ -1,0 +1,237 @@
+"""d log P(k, a) / d theta on the GPU: frozen-step tangents.
+
+The reference obtains gradients with ``jax.jacfwd`` through
+``evolve_background`` and ``evolve_perturbations`` (notebooks'
+``compute_matter_power``; ``DirectAdjoint`` at ``perturbations.py:765``).
+diffrax's PID controller stops gradients through its step-size factor, so
+that derivative is the derivative of the solve on the nominal step sequence:
+the 7-step start-time bisection is piecewise constant in theta, every step
+time is fixed, and only the final step follows ``tau_out(theta)``.
+
+Here that quantity is computed by central differences of exactly that map:
+``deb_forward_record`` runs the nominal solve and stores every mode's
+accepted step times, then one ``deb_replay`` launch integrates all
+(mode, theta_p +- eps_p) pairs on those steps with the perturbed tables.
+The difference quotient equals the tangent of the frozen-step map to
+O(eps^2) (eps = 1e-4 relative by default); the map has no branch, so there
+is no step-selection noise.  ``A_s`` and ``n_s`` enter only ``get_power``
+(``perturbations.py:1123``): their derivatives are analytic.
+"""
+from __future__ import annotations
+
+import ctypes
+import multiprocessing as mp
+import os
+
+import numpy as np
+
+from . import _native
+from . import background as _bg
+from . import perturbations as _pt
+from . import tables as _tables
+
+THETA = ("Omegam", "Omegab", "h", "n_s", "A_s", "mnu", "w_DE_0", "w_DE_a")
+ANALYTIC = ("n_s", "A_s")
+
+
+def _get(param, name):
+    return param["H0"] / 100.0 if name == "h" else param[name]
+
+
+def _with(param, name, value):
+    q = dict(param)
+    if name == "h":
+        q["H0"] = 100.0 * value
+    else:
+        q[name] = value
+    return q
+
+
+def _evolve(param):
+    return _bg.evolve_background(param=param)
+
+
+def evolve_backgrounds(params, processes=None):
+    """Host table production for many parameter dicts (process pool, spawn)."""
+    processes = processes if processes is not None else min(len(params), os.cpu_count() or 1)
+    if processes <= 1 or len(params) <= 1:
+        return [_evolve(p) for p in params]
+    with mp.get_context("spawn").Pool(processes) as pool:
+        return pool.map(_evolve, params)
+
+
+def perturbed_params(cosmo, theta=THETA, rel_step=1e-4):
+    """[(name, eps, param_plus, param_minus)] for the ODE parameters of theta."""
+    out = []
+    for name in theta:
+        if name in ANALYTIC:
+            continue
+        v = float(_get(cosmo, name))
+        eps = rel_step * abs(v) if v != 0.0 else rel_step
+        out.append((name, eps, _with(cosmo, name, v + eps), _with(cosmo, name, v - eps)))
+    return out
+
+
+class GradientProblem:
+    """Device-resident inputs, buffers and plan of one gradient launch pair.
+
+    ``backgrounds``: per cosmology the evolved ``param`` dicts
+    [nominal, theta_1 + eps_1, theta_1 - eps_1, ...] (see
+    :func:`perturbed_params`).  :meth:`run` enqueues the recorded nominal
+    solve, the replay of every perturbed set, ``get_power`` and the
+    difference quotients on one stream, without synchronising.
+    """
+
+    def __init__(self, plist, backgrounds, pert, kmodes, aexp_out, *, lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, rtol, atol,
+                 pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, max_steps=2048, idx=4,
+                 theta=THETA):
+        import torch
+
+        self.theta = tuple(theta)
+        self.nc = len(plist)
+        self.kmodes = np.asarray(kmodes, dtype=np.float64)
+        self.num_k = self.kmodes.shape[0]
+        aexp_out = np.atleast_1d(np.asarray(aexp_out, dtype=np.float64))
+        self.nout = aexp_out.shape[0]
+        self.npar = len(pert[0])
+        self.nset = 2 * self.npar
+        self.idx = idx
+        nominal = [b[0] for b in backgrounds]
+        sets = [b[1:] for b in backgrounds]
+        self.host_tab0 = _tables.pack_batch(nominal, nqmax)
+        self.host_tau0 = np.stack([_tables.tau_of_a(b, aexp_out) for b in nominal])
+        self.host_tabs = _tables.pack_batch([q for st in sets for q in st], nqmax)
+        self.host_taus = np.stack([_tables.tau_of_a(q, aexp_out) for st in sets for q in st])
+        self.host_k = np.tile(self.kmodes, self.nc)
+        self.host_com = np.repeat(np.arange(self.nc, dtype=np.int32), self.num_k)
+        self.nmode = self.host_k.shape[0]
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
+        T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a)).to(dev, dt)
+        self.d_tab0, self.d_tabs = T(self.host_tab0), T(self.host_tabs)
+        self.d_k, self.d_com = T(self.host_k), T(self.host_com, torch.int32)
+        self.d_tau0, self.d_taus = T(self.host_tau0), T(self.host_taus)
+        self.rec_len = int(max_steps) + 1
+        nm, ns, no = self.nmode, self.nset, self.nout
+        self.d_rec = torch.empty((nm, self.rec_len), dtype=torch.float64, device=dev)
+        self.d_nrec = torch.empty((nm,), dtype=torch.int32, device=dev)
+        self.d_y0 = torch.empty((nm, no, 20), dtype=torch.float64, device=dev)
+        self.d_st0 = torch.empty((nm,), dtype=torch.int32, device=dev)
+        self.d_steps = torch.empty((nm, 2), dtype=torch.int32, device=dev)
+        self.d_ys = torch.empty((ns * nm, no, 20), dtype=torch.float64, device=dev)
+        self.d_sts = torch.empty((ns * nm,), dtype=torch.int32, device=dev)
+        self.d_P = torch.empty((nm, no), dtype=torch.float64, device=dev)
+        self.d_dl = torch.empty((nm, no, len(self.theta)), dtype=torch.float64, device=dev)
+        eps = torch.as_tensor([[e for (_, e, _, _) in pp] for pp in pert], dtype=torch.float64, device=dev)
+        self.eps_m = eps[self.d_com.long()].t().contiguous()[:, :, None]     # [npar, nmode, 1]
+        self.ode_names = [n for (n, _, _, _) in pert[0]]
+        kp = torch.as_tensor([p.get("k_p", 0.05) for p in plist], dtype=torch.float64, device=dev)[self.d_com.long()]
+        As = torch.as_tensor([p["A_s"] for p in plist], dtype=torch.float64, device=dev)[self.d_com.long()]
+        self.d_inv_As = (1.0 / As)[:, None]
+        self.d_lnk = torch.log(self.d_k / kp)[:, None]
+        dims = _pt._dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, no, False, "structured", "warp")
+        self.plan = _pt.get_plan(dims, ns * nm)
+        self.cfg = _pt._cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps)
+
+    def run(self, stream=None, events=None):
+        import torch
+
+        s = stream if stream is not None else torch.cuda.current_stream()
+        L = _native.load()
+        c = lambda t: ctypes.c_void_p(t.data_ptr())
+        sp = ctypes.c_void_p(s.cuda_stream)
+        if events:
+            events[0].record(s)
+        _native.check(L.deb_forward_record(self.plan.ptr, c(self.d_tab0), self.nc, self.host_tab0.shape[1], c(self.d_k),
+                                           c(self.d_com), self.nmode, c(self.d_tau0), ctypes.byref(self.cfg),
+                                           c(self.d_y0), c(self.d_st0), c(self.d_steps), c(self.d_rec), self.rec_len,
+                                           c(self.d_nrec), sp), "deb_forward_record")
+        if events:
+            events[1].record(s)
+        _native.check(L.deb_replay(self.plan.ptr, c(self.d_tabs), self.nc, self.nset, self.host_tabs.shape[1],
+                                   c(self.d_k), c(self.d_com), self.nmode, c(self.d_taus), ctypes.byref(self.cfg),
+                                   c(self.d_rec), self.rec_len, c(self.d_nrec), c(self.d_ys), c(self.d_sts), sp),
+                      "deb_replay")
+        if events:
+            events[2].record(s)
+        with torch.cuda.stream(s):
+            ys = self.d_ys[..., self.idx].reshape(self.nset, self.nmode, self.nout)
+            lp = torch.log(ys * ys)
+            dl_ode = (lp[0::2] - lp[1::2]) / (2.0 * self.eps_m)
+            for j, name in enumerate(self.theta):
+                if name == "A_s":
+                    self.d_dl[:, :, j] = self.d_inv_As
+                elif name == "n_s":
+                    self.d_dl[:, :, j] = self.d_lnk
+                else:
+                    self.d_dl[:, :, j] = dl_ode[self.ode_names.index(name)]
+        _native.check(L.deb_get_power(c(self.d_tab0), self.nc, self.host_tab0.shape[1], c(self.d_k), c(self.d_com),
+                                      self.nmode, self.nout, c(self.d_y0), 20, self.idx, c(self.d_P), sp),
+                      "deb_get_power")
+        return self.d_P, self.d_dl
+
+    def check(self):
+        st0 = self.d_st0.cpu().numpy()
+        sts = self.d_sts.cpu().numpy()
+        if (st0 != 0).any() or (sts != 0).any():
+            raise RuntimeError(f"{int((st0 != 0).sum())} nominal / {int((sts != 0).sum())} replayed mode(s) failed")
+
+
+def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num_k: int, lmaxg: int = 11,
+                              lmaxgp: int = 11, lmaxr: int = 11, lmaxnu: int = 8, nqmax: int = 3, rtol: float = 1e-4,
+                              atol: float = 1e-4, pcoeff: float = 0.25, icoeff: float = 0.80, dcoeff: float = 0.0,
+                              factormax: float = 20.0, factormin: float = 0.3, max_steps: int = 2048, idx: int = 4,
+                              theta=THETA, rel_step: float = 1e-4, dologk: bool = True, processes=None,
+                              backgrounds=None, throw: bool = True):
+    """P(k, a) and d log P / d theta for one or many cosmologies.
+
+    ``params``: input parameter dict(s) as given to ``evolve_background``
+    (Omegam, Omegab, H0, mnu, w_DE_0, w_DE_a, A_s, n_s, ...).  Returns
+    ``(P [ncosmo, num_k, nout], dlogP [ncosmo, num_k, nout, len(theta)],
+    kmodes)``; with a single dict the cosmology axis is dropped.
+    ``backgrounds`` may pass precomputed host tables: a list (per cosmology)
+    of [nominal, +eps_1, -eps_1, +eps_2, ...] evolved ``param`` dicts.
+    """
+    single = isinstance(params, dict)
+    plist = [params] if single else list(params)
+    nc = len(plist)
+    kmodes = np.geomspace(kmin, kmax, num_k) if dologk else np.linspace(kmin, kmax, num_k)
+    pert = [perturbed_params(p, theta, rel_step) for p in plist]
+    nset = 2 * len(pert[0])
+    if backgrounds is None:
+        flat = []
+        for p, pp in zip(plist, pert):
+            flat.append(p)
+            for (_, _, a, b) in pp:
+                flat += [a, b]
+        ev = evolve_backgrounds(flat, processes)
+        backgrounds = [ev[i * (nset + 1):(i + 1) * (nset + 1)] for i in range(nc)]
+    gp = GradientProblem(plist, backgrounds, pert, kmodes, aexp_out, lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr,
+                         lmaxnu=lmaxnu, nqmax=nqmax, rtol=rtol, atol=atol, pcoeff=pcoeff, icoeff=icoeff, dcoeff=dcoeff,
+                         factormax=factormax, factormin=factormin, max_steps=max_steps, idx=idx, theta=theta)
+    Pd, Dd = gp.run()
+    if throw:
+        gp.check()
+    nout = gp.nout
+    P = Pd.reshape(nc, num_k, nout).cpu().numpy()
+    D = Dd.reshape(nc, num_k, nout, len(theta)).cpu().numpy()
+    return (P[0], D[0], kmodes) if single else (P, D, kmodes)
+
+
+def fisher_matrix(kmodes, dlogP, volume_mpc3: float):
+    """F_ij = sum_{k,a} d_i lnP d_j lnP / sigma^2_lnP with sigma^2_lnP = 2 / N_k,
+    N_k = V k^2 dk / (2 pi^2) (diagonal Gaussian covariance, one volume V per
+    output time).  dlogP [num_k, nout, ntheta] -> [ntheta, ntheta]."""
+    import torch
+
+    k = np.asarray(kmodes, dtype=np.float64)
+    edges = np.sqrt(k[1:] * k[:-1])
+    dk = np.empty_like(k)
+    dk[1:-1] = edges[1:] - edges[:-1]
+    dk[0] = edges[0] - k[0] ** 2 / edges[0]
+    dk[-1] = k[-1] ** 2 / edges[-1] - edges[-1]
+    nk = volume_mpc3 * k**2 * dk / (2.0 * np.pi**2)
+    w = torch.as_tensor(nk / 2.0, dtype=torch.float64, device="cuda")
+    d = torch.as_tensor(np.asarray(dlogP, dtype=np.float64), device="cuda")
+    F = torch.einsum("k,kai,kaj->ij", w, d, d)
+    return F.cpu().numpy()

@@ -125,6 +125,31 @@ int deb_forward(deb_plan* plan, const double* d_tables, int ncosmo, int blob_len
                 double* d_y_out, int* d_status, int* d_steps, void* stream);
 
 /*
+ * Frozen-step tangents (the gradient path, a jax.jacfwd over the solve in
+ * the reference: notebooks' compute_matter_power, perturbations.py:765
+ * DirectAdjoint).  diffrax's PID controller stops gradients through its step
+ * factor, so jacfwd differentiates the solve on the nominal step sequence.
+ * deb_forward_record is deb_forward that also stores, per mode, tau_start and
+ * every accepted step's end time:
+ *   d_record [nmode, rec_len] (rec_len >= max_steps + 1), d_nrec [nmode]
+ *   (accepted steps, 0 for a failed mode).
+ * deb_replay integrates nset table sets per cosmology (e.g. theta +- eps per
+ * parameter) on those recorded steps, without step control, in one launch:
+ *   d_tables [ncosmo * nset, blob_len] (set s of cosmology c at row c*nset+s)
+ *   d_tau_out [ncosmo * nset, nout]
+ *   d_y_out [nset * nmode, nout, 20|nvar], d_status [nset * nmode]
+ * The last replayed step ends at the set's own final output time.  Needs a
+ * plan in DEB_EXEC_WARP (or AUTO) made for >= nset * nmode modes.
+ */
+int deb_forward_record(deb_plan* plan, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
+                       const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+                       double* d_y_out, int* d_status, int* d_steps, double* d_record, int rec_len, int* d_nrec,
+                       void* stream);
+int deb_replay(deb_plan* plan, const double* d_tables, int ncosmo, int nset, int blob_len, const double* d_k,
+               const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+               const double* d_record, int rec_len, const int* d_nrec, double* d_y_out, int* d_status, void* stream);
+
+/*
  * get_power (perturbations.py:1101-1123):
  *   P[m, o] = 2 pi^2 A_s (k_m/k_p)^(n_s-1) k_m^-3 y[m, o, idx]^2
  * with A_s, n_s, k_p read from the mode's cosmology blob.

@@ -84,6 +84,33 @@ int h_spline(const double* blob, int blob_len, int which, const double* x, int n
   return 0;
 }
 
+// record / replay, mirroring the kernel's work items (item = set * nmode + mode)
+int h_solve_rr(const double* tables, int ncosmo, int nset, int blob_len, const double* kmodes, const int* cosmo,
+               int nmode, const double* tau_out, int nout, const int* dims, const double* cfg, int max_steps,
+               double* rec, int rec_len, int* nrec, int record, int replay, double* y_out, int* stats) {
+  const Dims D = make_dims(dims[0], dims[1], dims[2], dims[3], dims[4]);
+  Ctl ctl;
+  ctl.rtol = cfg[0]; ctl.atol = cfg[1];
+  ctl.b1 = (cfg[3] + cfg[2] + cfg[4]) / cfg[7]; ctl.b2 = -(cfg[2] + 2.0 * cfg[4]) / cfg[7]; ctl.b3 = cfg[4] / cfg[7];
+  ctl.fmax = cfg[5]; ctl.fmin = cfg[6]; ctl.safety = cfg[8]; ctl.hist_on_reject = (int)cfg[9];
+  ctl.max_steps = max_steps; ctl.dense = 0; ctl.return_full = 0; ctl.nout = nout;
+  ctl.record = record; ctl.replay = replay;
+  for (int it = 0; it < nmode * nset; ++it) {
+    const int mi = it % nmode, set = it / nmode;
+    const int ci = (cosmo ? cosmo[mi] : 0) * nset + set;
+    Ctx x; if (!setup(x, tables + (long)ci * blob_len, blob_len, dims, kmodes[mi], false)) return -2;
+    double* dst = y_out + (long)it * nout * 20;
+    for (int i = 0; i < nout * 20; ++i) dst[i] = std::numeric_limits<double>::quiet_NaN();
+    Run r;
+    r.rec = rec + (long)mi * rec_len; r.rec_cap = rec_len - 1; r.nrec = replay ? nrec[mi] : 0;
+    mode_begin<1>(GP, x.c, x.m, x.D, ctl, x.w, tau_out + (long)ci * nout, r);
+    while (mode_step<1>(GP, x.c, x.m, x.D, x.T, x.R, ctl, x.w, tau_out + (long)ci * nout, dst, 1, r)) {}
+    stats[3 * it] = r.status; stats[3 * it + 1] = r.acc; stats[3 * it + 2] = r.rej;
+    if (record) nrec[mi] = r.status == ST_OK ? r.acc : 0;
+  }
+  return 0;
+}
+
 // full per-mode solve with the kernel's driver, sequential over modes
 int h_solve(const double* tables, int ncosmo, int blob_len, const double* kmodes, const int* cosmo, int nmode,
             const double* tau_out, int nout, const int* dims, const double* cfg, int max_steps, int return_full,
@@ -94,6 +121,7 @@ int h_solve(const double* tables, int ncosmo, int blob_len, const double* kmodes
   ctl.b1 = (cfg[3] + cfg[2] + cfg[4]) / cfg[7]; ctl.b2 = -(cfg[2] + 2.0 * cfg[4]) / cfg[7]; ctl.b3 = cfg[4] / cfg[7];
   ctl.fmax = cfg[5]; ctl.fmin = cfg[6]; ctl.safety = cfg[8]; ctl.hist_on_reject = (int)cfg[9];
   ctl.max_steps = max_steps; ctl.dense = dense; ctl.return_full = return_full; ctl.nout = nout;
+  ctl.record = 0; ctl.replay = 0;
   const int osz = return_full ? D.n : 20;
   for (int mi = 0; mi < nmode; ++mi) {
     const int ci = cosmo ? cosmo[mi] : 0;
@@ -101,6 +129,7 @@ int h_solve(const double* tables, int ncosmo, int blob_len, const double* kmodes
     double* dst = y_out + (long)mi * nout * osz;
     for (int i = 0; i < nout * osz; ++i) dst[i] = std::numeric_limits<double>::quiet_NaN();
     Run r;
+    r.rec = nullptr; r.rec_cap = 0; r.nrec = 0;
     mode_begin<1>(GP, x.c, x.m, x.D, ctl, x.w, tau_out + (long)ci * nout, r);
     while (mode_step<1>(GP, x.c, x.m, x.D, x.T, x.R, ctl, x.w, tau_out + (long)ci * nout, dst, 1, r)) {}
     stats[3 * mi] = r.status; stats[3 * mi + 1] = r.acc; stats[3 * mi + 2] = r.rej;

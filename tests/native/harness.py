@@ -24,6 +24,8 @@ def lib():
         L.h_rhs.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, ctypes.c_double, dp, dp, dp]
         L.h_solve_W.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, ctypes.c_double, dp, ctypes.c_double, dp, dp, ctypes.c_int]
         L.h_spline.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, dp, ip]
+        L.h_solve_rr.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, ip, ctypes.c_int, dp, ctypes.c_int, ip,
+                                 dp, ctypes.c_int, dp, ctypes.c_int, ip, ctypes.c_int, ctypes.c_int, dp, ip]
         L.h_start.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, dp, dp]
         L.h_solve.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp, ip, ctypes.c_int, dp, ctypes.c_int, ip, dp, ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, dp, ip]
@@ -84,3 +86,27 @@ def spline(blob, which, x):
     rc = lib().h_spline(_p(blob), blob.shape[0], int(which), _p(x), x.shape[0], _p(out), _p(idx, ctypes.c_int))
     assert rc == 0, rc
     return out, idx
+
+
+def solve_rr(tables, nset, kmodes, tau_out, *, rec=None, nrec=None, record=False, replay=False, cosmo_of_mode=None,
+             lmaxg=11, lmaxgp=11, lmaxr=11, lmaxnu=8, nqmax=3, rtol=1e-4, atol=1e-4, max_steps=2048):
+    """Record (nset = 1) or replay (nset table sets per cosmology) like the kernel."""
+    tables = np.ascontiguousarray(np.atleast_2d(tables), dtype=np.float64)
+    kmodes = np.ascontiguousarray(kmodes, dtype=np.float64)
+    tau_out = np.ascontiguousarray(np.atleast_2d(tau_out), dtype=np.float64)
+    nmode, nout = kmodes.shape[0], tau_out.shape[1]
+    ncosmo = tables.shape[0] // nset
+    com = np.ascontiguousarray(np.zeros(nmode) if cosmo_of_mode is None else cosmo_of_mode, dtype=np.int32)
+    dims = _d([lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax])
+    cfg = np.array([rtol, atol, 0.25, 0.80, 0.0, 20.0, 0.3, 5.0, 0.9, 0.0])
+    rec_len = max_steps + 1
+    if rec is None:
+        rec = np.zeros((nmode, rec_len))
+        nrec = np.zeros(nmode, dtype=np.int32)
+    y = np.empty((nset * nmode, nout, 20))
+    st = np.zeros((nset * nmode, 3), dtype=np.int32)
+    rc = lib().h_solve_rr(_p(tables), ncosmo, nset, tables.shape[1], _p(kmodes), _p(com, ctypes.c_int), nmode, _p(tau_out),
+                          nout, _p(dims, ctypes.c_int), _p(cfg), int(max_steps), _p(rec), rec_len,
+                          _p(nrec, ctypes.c_int), int(record), int(replay), _p(y), _p(st, ctypes.c_int))
+    assert rc == 0, rc
+    return y, st, rec, nrec

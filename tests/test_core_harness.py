@@ -112,3 +112,45 @@ def test_kernel_spline_matches_reference_form(fid):
         ref = sp.evaluate(x)
         scale = np.maximum(np.abs(sp._y_).max(), np.abs(ref))   # far extrapolation grows cubically
         assert (np.abs(val - ref) <= 1e-13 * scale).all(), key
+
+
+def test_replay_on_nominal_tables_reproduces_the_solve(fid):
+    """Recording the accepted steps and replaying them with the same tables
+    gives the nominal outputs bit for bit (the replay takes no decisions)."""
+    dims = dict(lmaxg=8, lmaxgp=8, lmaxr=10, lmaxnu=8, nqmax=3)
+    a_out = np.linspace(0.2, 1.0, 8)
+    k = np.geomspace(1e-3, 1.0, 5)
+    b0 = tb.pack_cosmology(bg.evolve_background(param=fiducial_mnu_param()), 3)
+    p0 = bg.evolve_background(param=fiducial_mnu_param())
+    tau0 = tb.tau_of_a(p0, a_out)
+    y0, s0, rec, nrec = H.solve_rr(b0, 1, k, tau0, record=True, rtol=1e-6, atol=1e-9, max_steps=20000, **dims)
+    assert (s0[:, 0] == 0).all() and (nrec == s0[:, 1]).all()
+    yr, sr, _, _ = H.solve_rr(b0, 1, k, tau0, rec=rec, nrec=nrec, replay=True, rtol=1e-6, atol=1e-9, max_steps=20000,
+                              **dims)
+    assert (sr[:, 0] == 0).all() and (sr[:, 1] == nrec).all()
+    assert np.array_equal(yr, y0)
+
+
+def test_frozen_step_gradient_at_end_time_matches_tight_differences():
+    """d log P(k, a=1) / d Omega_m from the frozen-step replay (rtol 1e-6)
+    against central differences of two independent rtol 1e-9 solves."""
+    from discoeb_gb300.workloads import fiducial_mnu_param as fp
+    dims = dict(lmaxg=8, lmaxgp=8, lmaxr=10, lmaxnu=8, nqmax=3)
+    base = fp()
+    k = np.geomspace(1e-3, 1.0, 5)
+    eps = 1e-4 * base["Omegam"]
+    p0 = bg.evolve_background(param=base)
+    pp = bg.evolve_background(param=dict(base, Omegam=base["Omegam"] + eps))
+    pm = bg.evolve_background(param=dict(base, Omegam=base["Omegam"] - eps))
+    b0 = tb.pack_cosmology(p0, 3)
+    _, s0, rec, nrec = H.solve_rr(b0, 1, k, tb.tau_of_a(p0, [1.0]), record=True, rtol=1e-6, atol=1e-9,
+                                  max_steps=20000, **dims)
+    tabs = np.stack([tb.pack_cosmology(pp, 3), tb.pack_cosmology(pm, 3)])
+    taus = np.stack([tb.tau_of_a(pp, [1.0]), tb.tau_of_a(pm, [1.0])])
+    ys, ss, _, _ = H.solve_rr(tabs, 2, k, taus, rec=rec, nrec=nrec, replay=True, rtol=1e-6, atol=1e-9, max_steps=20000,
+                              **dims)
+    g = (np.log(ys[:5, 0, 4] ** 2) - np.log(ys[5:, 0, 4] ** 2)) / (2 * eps)
+    ya, _ = H.solve(tabs[0], k, taus[0], rtol=1e-9, atol=1e-12, max_steps=2000000, **dims)
+    yb, _ = H.solve(tabs[1], k, taus[1], rtol=1e-9, atol=1e-12, max_steps=2000000, **dims)
+    gt = (np.log(ya[:, 0, 4] ** 2) - np.log(yb[:, 0, 4] ** 2)) / (2 * eps)
+    assert np.abs(g - gt).max() <= 1e-3 * np.abs(gt).max()

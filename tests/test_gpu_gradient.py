@@ -1,0 +1,82 @@
+"""GPU gradient d log P / d theta (frozen-step tangents) against the host.
+
+* interior and end-time outputs: the same frozen-step algorithm run by the
+  host build of the kernel core (record + replay), tolerance 1e-3 of each
+  parameter's largest |d log P / d theta| (the nominal step sequences of the
+  two runs can differ by a rounding-flipped decision, which moves the
+  derivative by the discretisation error);
+* end-time output: central differences of two independent tight-tolerance
+  oracle solves (rtol 1e-9), the same 1e-3 bar.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import discoeb_gb300 as deb
+import discoeb_gb300.tables as tb
+from discoeb_gb300.gradient import THETA, evolve_backgrounds, perturbed_params
+from discoeb_gb300.workloads import fiducial_mnu_param
+from native import harness as H
+
+pytestmark = pytest.mark.gpu
+
+DIMS = dict(lmaxg=8, lmaxgp=8, lmaxr=10, lmaxnu=8, nqmax=3)
+
+
+@pytest.fixture(scope="module")
+def setup():
+    base = fiducial_mnu_param()
+    pert = perturbed_params(base)
+    flat = [base] + [q for (_, _, a, b) in pert for q in (a, b)]
+    bgs = evolve_backgrounds(flat, processes=1)
+    return base, pert, bgs
+
+
+def test_gradient_matches_host_frozen_step_replay(setup):
+    base, pert, bgs = setup
+    a_out = np.linspace(0.2, 1.0, 8)
+    P, D, k = deb.evolve_perturbations_grad(params=base, aexp_out=a_out, kmin=1e-3, kmax=1.0, num_k=6, rtol=1e-6,
+                                            atol=1e-9, max_steps=20000, backgrounds=[bgs], **DIMS)
+    assert P.shape == (6, 8) and D.shape == (6, 8, len(THETA))
+    b0 = tb.pack_cosmology(bgs[0], 3)
+    _, s0, rec, nrec = H.solve_rr(b0, 1, k, tb.tau_of_a(bgs[0], a_out), record=True, rtol=1e-6, atol=1e-9,
+                                  max_steps=20000, **DIMS)
+    tabs = np.stack([tb.pack_cosmology(q, 3) for q in bgs[1:]])
+    taus = np.stack([tb.tau_of_a(q, a_out) for q in bgs[1:]])
+    ys, ss, _, _ = H.solve_rr(tabs, len(bgs) - 1, k, taus, rec=rec, nrec=nrec, replay=True, rtol=1e-6, atol=1e-9,
+                              max_steps=20000, **DIMS)
+    lp = np.log(ys[..., 4] ** 2).reshape(len(bgs) - 1, 6, 8)
+    for j, (name, eps, _, _) in enumerate(pert):
+        g = (lp[2 * j] - lp[2 * j + 1]) / (2 * eps)
+        col = THETA.index(name)
+        scale = np.abs(g).max()
+        assert np.abs(D[:, :, col] - g).max() <= 1e-3 * scale, name
+    # analytic parameters (perturbations.py:1123)
+    np.testing.assert_allclose(D[:, :, THETA.index("A_s")], 1.0 / base["A_s"])
+    np.testing.assert_allclose(D[:, :, THETA.index("n_s")], np.log(k / 0.05)[:, None] * np.ones((1, 8)))
+
+
+def test_end_time_gradient_matches_tight_oracle_differences(setup):
+    base, pert, bgs = setup
+    P, D, k = deb.evolve_perturbations_grad(params=base, aexp_out=[1.0], kmin=1e-3, kmax=1.0, num_k=5, rtol=1e-6,
+                                            atol=1e-9, max_steps=20000, backgrounds=[bgs], **DIMS)
+    for j, (name, eps, _, _) in enumerate(pert):
+        bp, bm = bgs[1 + 2 * j], bgs[2 + 2 * j]
+        yp, sp = oracle.solve(tb.pack_cosmology(bp, 3), k, tb.tau_of_a(bp, [1.0]), rtol=1e-9, atol=1e-12,
+                              max_steps=2000000, **DIMS)
+        ym, sm = oracle.solve(tb.pack_cosmology(bm, 3), k, tb.tau_of_a(bm, [1.0]), rtol=1e-9, atol=1e-12,
+                              max_steps=2000000, **DIMS)
+        assert (sp[:, 0] == 0).all() and (sm[:, 0] == 0).all()
+        gt = (np.log(yp[:, 0, 4] ** 2) - np.log(ym[:, 0, 4] ** 2)) / (2 * eps)
+        col = THETA.index(name)
+        assert np.abs(D[:, 0, col] - gt).max() <= 1e-3 * np.abs(gt).max(), name
+
+
+def test_fisher_matrix_is_symmetric_and_positive(setup):
+    base, pert, bgs = setup
+    P, D, k = deb.evolve_perturbations_grad(params=base, aexp_out=np.linspace(0.2, 1.0, 8), kmin=1e-3, kmax=1.0,
+                                            num_k=16, rtol=1e-5, atol=1e-8, max_steps=20000, backgrounds=[bgs], **DIMS)
+    F = deb.fisher_matrix(k, D, volume_mpc3=(1000.0 / 0.6774) ** 3)
+    assert F.shape == (8, 8) and np.isfinite(F).all()
+    np.testing.assert_allclose(F, F.T, rtol=1e-12)
+    assert np.linalg.eigvalsh(F).min() >= -1e-8 * np.abs(F).max()
