@@ -27,7 +27,7 @@ class DebSolverCfg(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double), ("pcoeff", ctypes.c_double),
                 ("icoeff", ctypes.c_double), ("dcoeff", ctypes.c_double), ("factormax", ctypes.c_double),
                 ("factormin", ctypes.c_double), ("safety", ctypes.c_double), ("error_order", ctypes.c_double),
-                ("max_steps", ctypes.c_int), ("hist_on_reject", ctypes.c_int)]
+                ("max_steps", ctypes.c_int), ("hist_on_reject", ctypes.c_int), ("step_to_outputs", ctypes.c_int)]
 
 
 _lib = None

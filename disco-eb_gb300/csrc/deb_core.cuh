@@ -1102,7 +1102,18 @@ struct Ctl {
   int max_steps, hist_on_reject, dense, return_full, nout;
   int record;   // store tau_start and every accepted step's end time
   int replay;   // take the stored step times instead of controlling the step
+  int step_ts;  // clip steps to land on every output time (diffrax PIDController(step_ts=ts))
 };
+
+// first output time strictly after t (or +inf)
+HD double next_output_after(const double* tau_out, int nout, double t) {
+  double best = 1e300;
+  for (int o = 0; o < nout; ++o) {
+    const double to = LDG(tau_out + o);
+    if (to > t && to < best) best = to;
+  }
+  return best;
+}
 
 // Integration state; every lane of a group holds an identical copy.
 // rec: [tau_start, t_1, ..., t_nrec] of the nominal run (record / replay).
@@ -1134,6 +1145,10 @@ HD void mode_begin(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const D
   } else {
     const double dt0 = (t0 / 4.0 < 0.5 * (tmax - t0)) ? t0 / 4.0 : 0.5 * (tmax - t0);
     r.t1 = t0 + dt0 < tmax ? t0 + dt0 : tmax;
+    if (ctl.step_ts) {
+      const double to = next_output_after(tau_out, ctl.nout, t0);
+      if (r.t1 > to) r.t1 = to;
+    }
     if (ctl.record && gp.lead()) r.rec[0] = t0;
   }
   r.prev_inv = 1.0; r.prev_prev_inv = 1.0;
@@ -1268,6 +1283,10 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
     if (ctl.hist_on_reject) { r.prev_prev_inv = r.prev_inv; r.prev_inv = inv; }
   }
   double tn = r.t0 + dtn;
+  if (ctl.step_ts) {
+    const double to = next_output_after(tau_out, ctl.nout, r.t0);
+    if (tn > to) tn = to;
+  }
   if (tn > r.T1 - 1e-10) tn = r.T1;
   if (!(tn > r.t0) && r.t0 < r.T1) { r.status = ST_DT_UNDERFLOW; return false; }
   r.t1 = tn;

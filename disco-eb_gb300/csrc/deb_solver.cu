@@ -367,7 +367,7 @@ int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, in
   P.ctl.safety = cfg->safety; P.ctl.fmin = cfg->factormin; P.ctl.fmax = cfg->factormax;
   P.ctl.max_steps = cfg->max_steps; P.ctl.hist_on_reject = cfg->hist_on_reject;
   P.ctl.dense = p->dense; P.ctl.return_full = p->return_full; P.ctl.nout = p->nout;
-  P.ctl.record = record; P.ctl.replay = replay;
+  P.ctl.record = record; P.ctl.replay = replay; P.ctl.step_ts = cfg->step_to_outputs;
   if (cudaMemsetAsync(p->queue, 0, sizeof(int), s) != cudaSuccess) return DEB_ERR_CUDA;
   const long items = (long)nmode * nset;
   if (p->exec_mode == DEB_EXEC_LANE) {
@@ -472,7 +472,7 @@ int deb_forward_static(const deb_dims* dims, const double* d_tables, int ncosmo,
   P.ctl.safety = cfg->safety; P.ctl.fmin = cfg->factormin; P.ctl.fmax = cfg->factormax;
   P.ctl.max_steps = cfg->max_steps; P.ctl.hist_on_reject = cfg->hist_on_reject;
   P.ctl.dense = 0; P.ctl.return_full = dims->return_full; P.ctl.nout = dims->nout;
-  P.ctl.record = 0; P.ctl.replay = 0;
+  P.ctl.record = 0; P.ctl.replay = 0; P.ctl.step_ts = cfg->step_to_outputs;
   long warps = (long)nsm * 8;
   if (warps > max_slots) warps = max_slots;
   if (warps > nmode) warps = nmode;

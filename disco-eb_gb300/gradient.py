@@ -84,7 +84,7 @@ class GradientProblem:
 
     def __init__(self, plist, backgrounds, pert, kmodes, aexp_out, *, lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, rtol, atol,
                  pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, max_steps=2048, idx=4,
-                 theta=THETA):
+                 theta=THETA, step_to_outputs=False):
         import torch
 
         self.theta = tuple(theta)
@@ -131,7 +131,8 @@ class GradientProblem:
         self.d_lnk = torch.log(self.d_k / kp)[:, None]
         dims = _pt._dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, no, False, "structured", "warp")
         self.plan = _pt.get_plan(dims, ns * nm)
-        self.cfg = _pt._cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps)
+        self.cfg = _pt._cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps,
+                            step_to_outputs=step_to_outputs)
 
     def run(self, stream=None, events=None):
         import torch
@@ -182,7 +183,7 @@ def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num
                               atol: float = 1e-4, pcoeff: float = 0.25, icoeff: float = 0.80, dcoeff: float = 0.0,
                               factormax: float = 20.0, factormin: float = 0.3, max_steps: int = 2048, idx: int = 4,
                               theta=THETA, rel_step: float = 1e-4, dologk: bool = True, processes=None,
-                              backgrounds=None, throw: bool = True):
+                              backgrounds=None, throw: bool = True, step_to_outputs: bool = False):
     """P(k, a) and d log P / d theta for one or many cosmologies.
 
     ``params``: input parameter dict(s) as given to ``evolve_background``
@@ -191,6 +192,9 @@ def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num
     kmodes)``; with a single dict the cosmology axis is dropped.
     ``backgrounds`` may pass precomputed host tables: a list (per cosmology)
     of [nominal, +eps_1, -eps_1, +eps_2, ...] evolved ``param`` dicts.
+    With the reference's output semantics (linear interpolation inside the
+    step) an interior output's derivative includes the slope of that
+    interpolant; ``step_to_outputs=True`` lands steps on the output times.
     """
     single = isinstance(params, dict)
     plist = [params] if single else list(params)
@@ -208,7 +212,8 @@ def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num
         backgrounds = [ev[i * (nset + 1):(i + 1) * (nset + 1)] for i in range(nc)]
     gp = GradientProblem(plist, backgrounds, pert, kmodes, aexp_out, lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr,
                          lmaxnu=lmaxnu, nqmax=nqmax, rtol=rtol, atol=atol, pcoeff=pcoeff, icoeff=icoeff, dcoeff=dcoeff,
-                         factormax=factormax, factormin=factormin, max_steps=max_steps, idx=idx, theta=theta)
+                         factormax=factormax, factormin=factormin, max_steps=max_steps, idx=idx, theta=theta,
+                         step_to_outputs=step_to_outputs)
     Pd, Dd = gp.run()
     if throw:
         gp.check()

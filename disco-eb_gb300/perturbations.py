@@ -47,9 +47,9 @@ def _dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, nout, return_full, linear_solver,
 
 
 def _cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps, safety=0.9, error_order=5.0,
-         hist_on_reject=False):
+         hist_on_reject=False, step_to_outputs=False):
     return _native.DebSolverCfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, safety, error_order,
-                                int(max_steps), 1 if hist_on_reject else 0)
+                                int(max_steps), 1 if hist_on_reject else 0, 1 if step_to_outputs else 0)
 
 
 def get_plan(dims: _native.DebDims, nmode: int) -> _native.Plan:
@@ -137,12 +137,13 @@ def _check_status(status: np.ndarray, kmodes: np.ndarray, throw: bool):
 def solve(tables, kmodes, tau_out, cosmo_of_mode=None, *, lmaxg=11, lmaxgp=11, lmaxr=11, lmaxnu=8, nqmax=3,
           rtol=1e-4, atol=1e-4, pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, max_steps=2048,
           return_full=False, linear_solver="structured", throw=True, return_stats=False, output="numpy",
-          error_order=5.0, safety=0.9, hist_on_reject=False, exec_mode="auto"):
+          error_order=5.0, safety=0.9, hist_on_reject=False, exec_mode="auto", step_to_outputs=False):
     """Integrate modes of packed cosmologies on the GPU; y [nmode, nout, 20|nvar]."""
     torch = _torch()
     prob = DeviceProblem(tables, kmodes, tau_out, cosmo_of_mode, lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr, lmaxnu=lmaxnu,
                          nqmax=nqmax, return_full=return_full, linear_solver=linear_solver, exec_mode=exec_mode)
-    cfg = _cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps, safety, error_order, hist_on_reject)
+    cfg = _cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps, safety, error_order, hist_on_reject,
+               step_to_outputs)
     prob.launch(cfg)
     status = prob.status.cpu().numpy()
     _check_status(status, np.asarray(kmodes if not torch.is_tensor(kmodes) else kmodes.cpu()), throw)

@@ -95,6 +95,10 @@ typedef struct deb_solver_cfg {
   double error_order;
   int max_steps;
   int hist_on_reject;  /* 1: a rejected step also shifts the error history */
+  int step_to_outputs; /* 0: outputs by linear interpolation inside the step (the
+                          reference's SaveAt(ts), perturbations.py:770); 1: steps
+                          are clipped to land on every output time (diffrax
+                          PIDController(step_ts=...)), outputs are step ends */
 } deb_solver_cfg;
 
 typedef struct deb_plan deb_plan;

@@ -64,7 +64,8 @@ def n_vars(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax) -> int:
 
 def solve(tables, kmodes, tau_out, *, cosmo_of_mode=None, lmaxg=11, lmaxgp=11, lmaxr=11, lmaxnu=8, nqmax=3,
           rtol=1e-4, atol=1e-4, pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3,
-          max_steps=2048, return_full=False, error_order=5.0, safety=0.9, hist_on_reject=False, nthreads=0):
+          max_steps=2048, return_full=False, error_order=5.0, safety=0.9, hist_on_reject=False, nthreads=0,
+          step_to_outputs=False):
     """Run the oracle.  Returns (y [nmode, nout, 20|n], stats [nmode, 3])."""
     tables = np.ascontiguousarray(np.atleast_2d(tables), dtype=np.float64)
     kmodes = np.ascontiguousarray(kmodes, dtype=np.float64)
@@ -77,7 +78,7 @@ def solve(tables, kmodes, tau_out, *, cosmo_of_mode=None, lmaxg=11, lmaxgp=11, l
     cosmo_of_mode = np.ascontiguousarray(cosmo_of_mode, dtype=np.int32)
     dims = np.array([lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax], dtype=np.int32)
     cfg = np.array([rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, error_order, safety,
-                    1.0 if hist_on_reject else 0.0], dtype=np.float64)
+                    1.0 if hist_on_reject else 0.0, 1.0 if step_to_outputs else 0.0], dtype=np.float64)
     n = n_vars(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax)
     osz = n if return_full else 20
     y = np.empty((nmode, nout, osz), dtype=np.float64)

@@ -385,7 +385,7 @@ const double R_d[8] = {0.19, -0.1823079225333714636, -0.319231832186874912, 0.34
 
 struct Cfg {
   double rtol, atol, pcoeff, icoeff, dcoeff, fmax, fmin, error_order, safety;
-  int max_steps, hist_on_reject;
+  int max_steps, hist_on_reject, step_ts;
 };
 
 enum { ST_OK = 0, ST_MAX_STEPS = 1, ST_DT_UNDERFLOW = 2, ST_NONFINITE = 3, ST_BAD_INPUT = 4 };
@@ -452,6 +452,13 @@ ModeResult solve_mode(const Cosmo& c, const Dims& D, double k, const double* tau
   int next_out = 0;
   const double T1 = tau_max;
   double t1 = std::min(t0 + std::min(t0 / 4.0, 0.5 * (T1 - t0)), T1);
+  // optional diffrax PIDController(step_ts=tau_out): never step across an output time
+  auto clip_ts = [&](double tstart, double tend) {
+    if (!cfg.step_ts) return tend;
+    for (int i = 0; i < nout; ++i) if (tau_out[i] > tstart && tau_out[i] < tend) tend = tau_out[i];
+    return tend;
+  };
+  t1 = clip_ts(t0, t1);
   double prev_inv = 1.0, prev_prev_inv = 1.0;
   const double beta1 = (cfg.icoeff + cfg.pcoeff + cfg.dcoeff) / cfg.error_order;
   const double beta2 = -(cfg.pcoeff + 2.0 * cfg.dcoeff) / cfg.error_order;
@@ -532,7 +539,7 @@ ModeResult solve_mode(const Cosmo& c, const Dims& D, double k, const double* tau
       ++R.rejected;
       if (cfg.hist_on_reject) { prev_prev_inv = prev_inv; prev_inv = inv; }
     }
-    double tn = t0 + dtn;
+    double tn = clip_ts(t0, t0 + dtn);
     if (tn > T1 - 1e-10) tn = T1;
     if (!(tn > t0)) { if (t0 < T1) { R.status = ST_DT_UNDERFLOW; break; } }
     t1 = tn;
@@ -548,7 +555,8 @@ int oracle_n_vars(int lg, int lgp, int lr, int lnu, int nq) { return make_dims(l
 
 // Solve nmode modes.  tables: [ncosmo, blob_len]; tau_out: [ncosmo, nout];
 // dims = {lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax}; cfg = {rtol, atol, pcoeff,
-// icoeff, dcoeff, factormax, factormin, error_order, safety, hist_on_reject};
+// icoeff, dcoeff, factormax, factormin, error_order, safety, hist_on_reject,
+// step_to_outputs};
 // y_out: [nmode, nout, 20 or n]; stats: [nmode, 3] = status, accepted, rejected.
 int oracle_solve(const double* tables, int ncosmo, int blob_len, const double* kmodes, const int* cosmo_of_mode,
                  int nmode, const double* tau_out, int nout, const int* dims, const double* cfgv, int max_steps,
@@ -559,7 +567,8 @@ int oracle_solve(const double* tables, int ncosmo, int blob_len, const double* k
   Dims D = make_dims(dims[0], dims[1], dims[2], dims[3], dims[4]);
   if (D.lg < 3 || D.lgp < 3 || D.lr < 3 || D.lnu < 3) return -3;
   for (int i = 0; i < ncosmo; ++i) if (cs[i].nq != D.nq) return -4;
-  Cfg cfg{cfgv[0], cfgv[1], cfgv[2], cfgv[3], cfgv[4], cfgv[5], cfgv[6], cfgv[7], cfgv[8], max_steps, (int)cfgv[9]};
+  Cfg cfg{cfgv[0], cfgv[1], cfgv[2], cfgv[3], cfgv[4], cfgv[5], cfgv[6], cfgv[7], cfgv[8], max_steps, (int)cfgv[9],
+          (int)cfgv[10]};
   const int osz = return_full ? D.n : 20;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);

@@ -94,7 +94,7 @@ int h_solve_rr(const double* tables, int ncosmo, int nset, int blob_len, const d
   ctl.b1 = (cfg[3] + cfg[2] + cfg[4]) / cfg[7]; ctl.b2 = -(cfg[2] + 2.0 * cfg[4]) / cfg[7]; ctl.b3 = cfg[4] / cfg[7];
   ctl.fmax = cfg[5]; ctl.fmin = cfg[6]; ctl.safety = cfg[8]; ctl.hist_on_reject = (int)cfg[9];
   ctl.max_steps = max_steps; ctl.dense = 0; ctl.return_full = 0; ctl.nout = nout;
-  ctl.record = record; ctl.replay = replay;
+  ctl.record = record; ctl.replay = replay; ctl.step_ts = (int)cfg[10];
   for (int it = 0; it < nmode * nset; ++it) {
     const int mi = it % nmode, set = it / nmode;
     const int ci = (cosmo ? cosmo[mi] : 0) * nset + set;
@@ -121,7 +121,7 @@ int h_solve(const double* tables, int ncosmo, int blob_len, const double* kmodes
   ctl.b1 = (cfg[3] + cfg[2] + cfg[4]) / cfg[7]; ctl.b2 = -(cfg[2] + 2.0 * cfg[4]) / cfg[7]; ctl.b3 = cfg[4] / cfg[7];
   ctl.fmax = cfg[5]; ctl.fmin = cfg[6]; ctl.safety = cfg[8]; ctl.hist_on_reject = (int)cfg[9];
   ctl.max_steps = max_steps; ctl.dense = dense; ctl.return_full = return_full; ctl.nout = nout;
-  ctl.record = 0; ctl.replay = 0;
+  ctl.record = 0; ctl.replay = 0; ctl.step_ts = (int)cfg[10];
   const int osz = return_full ? D.n : 20;
   for (int mi = 0; mi < nmode; ++mi) {
     const int ci = cosmo ? cosmo[mi] : 0;

@@ -60,7 +60,7 @@ def solve_W(blob, dims, k, tau, y, dt, b, dense=False):
 
 def solve(tables, kmodes, tau_out, *, cosmo_of_mode=None, lmaxg=11, lmaxgp=11, lmaxr=11, lmaxnu=8, nqmax=3, rtol=1e-4,
           atol=1e-4, pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, max_steps=2048,
-          return_full=False, error_order=5.0, safety=0.9, hist_on_reject=False, dense=False):
+          return_full=False, error_order=5.0, safety=0.9, hist_on_reject=False, dense=False, step_to_outputs=False):
     tables = np.ascontiguousarray(np.atleast_2d(tables), dtype=np.float64)
     kmodes = np.ascontiguousarray(kmodes, dtype=np.float64)
     tau_out = np.ascontiguousarray(np.atleast_2d(tau_out), dtype=np.float64)
@@ -68,7 +68,7 @@ def solve(tables, kmodes, tau_out, *, cosmo_of_mode=None, lmaxg=11, lmaxgp=11, l
     com = np.ascontiguousarray(np.zeros(nmode) if cosmo_of_mode is None else cosmo_of_mode, dtype=np.int32)
     dims = _d([lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax])
     cfg = np.array([rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, error_order, safety,
-                    1.0 if hist_on_reject else 0.0])
+                    1.0 if hist_on_reject else 0.0, 1.0 if step_to_outputs else 0.0])
     n = 7 + (lmaxg + 1) + (lmaxgp + 1) + (lmaxr + 1) + nqmax * (lmaxnu + 1) + 2
     y = np.empty((nmode, nout, n if return_full else 20))
     st = np.zeros((nmode, 3), dtype=np.int32)
@@ -89,7 +89,8 @@ def spline(blob, which, x):
 
 
 def solve_rr(tables, nset, kmodes, tau_out, *, rec=None, nrec=None, record=False, replay=False, cosmo_of_mode=None,
-             lmaxg=11, lmaxgp=11, lmaxr=11, lmaxnu=8, nqmax=3, rtol=1e-4, atol=1e-4, max_steps=2048):
+             lmaxg=11, lmaxgp=11, lmaxr=11, lmaxnu=8, nqmax=3, rtol=1e-4, atol=1e-4, max_steps=2048,
+             step_to_outputs=False):
     """Record (nset = 1) or replay (nset table sets per cosmology) like the kernel."""
     tables = np.ascontiguousarray(np.atleast_2d(tables), dtype=np.float64)
     kmodes = np.ascontiguousarray(kmodes, dtype=np.float64)
@@ -98,7 +99,7 @@ def solve_rr(tables, nset, kmodes, tau_out, *, rec=None, nrec=None, record=False
     ncosmo = tables.shape[0] // nset
     com = np.ascontiguousarray(np.zeros(nmode) if cosmo_of_mode is None else cosmo_of_mode, dtype=np.int32)
     dims = _d([lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax])
-    cfg = np.array([rtol, atol, 0.25, 0.80, 0.0, 20.0, 0.3, 5.0, 0.9, 0.0])
+    cfg = np.array([rtol, atol, 0.25, 0.80, 0.0, 20.0, 0.3, 5.0, 0.9, 0.0, 1.0 if step_to_outputs else 0.0])
     rec_len = max_steps + 1
     if rec is None:
         rec = np.zeros((nmode, rec_len))

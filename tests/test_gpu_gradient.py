@@ -1,10 +1,14 @@
 """GPU gradient d log P / d theta (frozen-step tangents) against the host.
 
-* interior and end-time outputs: the same frozen-step algorithm run by the
-  host build of the kernel core (record + replay), tolerance 1e-3 of each
-  parameter's largest |d log P / d theta| (the nominal step sequences of the
-  two runs can differ by a rounding-flipped decision, which moves the
-  derivative by the discretisation error);
+* all outputs, steps landing on the output times (step_to_outputs): the
+  same frozen-step algorithm run by the host build of the kernel core
+  (record + replay), tolerance 1e-3 of each parameter's largest
+  |d log P / d theta| (the nominal step sequences of the two runs can differ
+  by a rounding-flipped decision, which moves the derivative by the
+  discretisation error).  With the reference's default outputs (linear
+  interpolation inside a step) an interior output's derivative is the slope
+  of that interpolant, which depends on where the steps fall; only the end
+  time is compared then;
 * end-time output: central differences of two independent tight-tolerance
   oracle solves (rtol 1e-9), the same 1e-3 bar.
 """
@@ -36,15 +40,15 @@ def test_gradient_matches_host_frozen_step_replay(setup):
     base, pert, bgs = setup
     a_out = np.linspace(0.2, 1.0, 8)
     P, D, k = deb.evolve_perturbations_grad(params=base, aexp_out=a_out, kmin=1e-3, kmax=1.0, num_k=6, rtol=1e-6,
-                                            atol=1e-9, max_steps=20000, backgrounds=[bgs], **DIMS)
+                                            atol=1e-9, max_steps=20000, backgrounds=[bgs], step_to_outputs=True, **DIMS)
     assert P.shape == (6, 8) and D.shape == (6, 8, len(THETA))
     b0 = tb.pack_cosmology(bgs[0], 3)
     _, s0, rec, nrec = H.solve_rr(b0, 1, k, tb.tau_of_a(bgs[0], a_out), record=True, rtol=1e-6, atol=1e-9,
-                                  max_steps=20000, **DIMS)
+                                  max_steps=20000, step_to_outputs=True, **DIMS)
     tabs = np.stack([tb.pack_cosmology(q, 3) for q in bgs[1:]])
     taus = np.stack([tb.tau_of_a(q, a_out) for q in bgs[1:]])
     ys, ss, _, _ = H.solve_rr(tabs, len(bgs) - 1, k, taus, rec=rec, nrec=nrec, replay=True, rtol=1e-6, atol=1e-9,
-                              max_steps=20000, **DIMS)
+                              max_steps=20000, step_to_outputs=True, **DIMS)
     lp = np.log(ys[..., 4] ** 2).reshape(len(bgs) - 1, 6, 8)
     for j, (name, eps, _, _) in enumerate(pert):
         g = (lp[2 * j] - lp[2 * j + 1]) / (2 * eps)
@@ -54,6 +58,27 @@ def test_gradient_matches_host_frozen_step_replay(setup):
     # analytic parameters (perturbations.py:1123)
     np.testing.assert_allclose(D[:, :, THETA.index("A_s")], 1.0 / base["A_s"])
     np.testing.assert_allclose(D[:, :, THETA.index("n_s")], np.log(k / 0.05)[:, None] * np.ones((1, 8)))
+
+
+def test_default_output_semantics_end_time_matches_host(setup):
+    """Reference output semantics (interpolation inside the step): the end-time
+    derivative agrees with the host replay."""
+    base, pert, bgs = setup
+    a_out = np.linspace(0.2, 1.0, 8)
+    P, D, k = deb.evolve_perturbations_grad(params=base, aexp_out=a_out, kmin=1e-3, kmax=1.0, num_k=6, rtol=1e-6,
+                                            atol=1e-9, max_steps=20000, backgrounds=[bgs], **DIMS)
+    b0 = tb.pack_cosmology(bgs[0], 3)
+    _, s0, rec, nrec = H.solve_rr(b0, 1, k, tb.tau_of_a(bgs[0], a_out), record=True, rtol=1e-6, atol=1e-9,
+                                  max_steps=20000, **DIMS)
+    tabs = np.stack([tb.pack_cosmology(q, 3) for q in bgs[1:]])
+    taus = np.stack([tb.tau_of_a(q, a_out) for q in bgs[1:]])
+    ys, ss, _, _ = H.solve_rr(tabs, len(bgs) - 1, k, taus, rec=rec, nrec=nrec, replay=True, rtol=1e-6, atol=1e-9,
+                              max_steps=20000, **DIMS)
+    lp = np.log(ys[..., 4] ** 2).reshape(len(bgs) - 1, 6, 8)
+    for j, (name, eps, _, _) in enumerate(pert):
+        g = (lp[2 * j, :, -1] - lp[2 * j + 1, :, -1]) / (2 * eps)
+        col = THETA.index(name)
+        assert np.abs(D[:, -1, col] - g).max() <= 1e-3 * np.abs(g).max(), name
 
 
 def test_end_time_gradient_matches_tight_oracle_differences(setup):

@@ -192,3 +192,17 @@ def test_dense_path_both_modes(lcdm, exec_mode):
     yd = deb.solve(blob[None], k, tau[None], rtol=1e-4, atol=1e-7, max_steps=20000, exec_mode=exec_mode,
                    linear_solver="dense", **LCDM)
     np.testing.assert_allclose(ys[:, 0, 4], yd[:, 0, 4], rtol=1e-5)
+
+
+def test_step_to_outputs_interior_outputs_vs_oracle(fid):
+    """With steps landing on the output times, interior outputs are step ends
+    (no interpolation): P(k) at 8 scale factors agrees with the oracle run
+    the same way."""
+    a_out = np.linspace(0.2, 1.0, 8)
+    k = np.geomspace(1e-3, 1.0, 8)
+    blob = tb.pack_cosmology(fid, 15)
+    tau = tb.tau_of_a(fid, a_out)
+    y = deb.solve(blob[None], k, tau[None], rtol=1e-5, atol=1e-5, max_steps=20000, step_to_outputs=True, **FID)
+    yo, so = oracle.solve(blob, k, tau, rtol=1e-5, atol=1e-5, max_steps=20000, step_to_outputs=True, **FID)
+    assert (so[:, 0] == 0).all()
+    np.testing.assert_allclose(y[:, :, 4] ** 2, yo[:, :, 4] ** 2, rtol=1e-4)
