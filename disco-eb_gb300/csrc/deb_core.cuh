@@ -187,9 +187,12 @@ HD Dims make_dims(int lg, int lgp, int lr, int lnu, int nq) {
 }
 
 // ------------------------------------------------------------------ workspace
-// Per-mode scratch: NV vectors of length n plus a MISC block.  Element e of a
-// mode's scratch lives at p[e * stride] (stride 32 interleaves the 32 modes
-// of a warp so that every access of the warp is one coalesced transaction).
+// Per-mode scratch: NV vectors of length n plus a MISC block.  Slot layout:
+// [vectors 0 .. V_K0-1][MISC][stage vectors k1..k8]; element e of a slot lives
+// at base[e * stride] (stride 32 interleaves the 32 modes of a warp so that
+// every access of the warp is one coalesced transaction).  The warp-per-mode
+// kernel keeps the first two parts in shared memory and may keep the stage
+// vectors in global memory (kp).
 enum { V_Y = 0, V_Y1, V_U, V_F, V_JC0, V_LO, V_UP, V_PI, V_ZH, V_ZE, V_K0, NV = V_K0 + 8 };
 // MISC block offsets
 enum { M_CORE = 0,          // 8x8 core LU (row-major)           64
@@ -204,6 +207,8 @@ enum { S_D = 0, S_W00I, S_ID, S_IDAH, S_GH2, S_GH3, S_GH5, S_GH7, S_GHR0, S_GHQE
        S_GER1, S_GEQE, S_R13, S_R15, S_R17, S_R1R0, S_R1QE, S_R1QT, S_DTT, S_DTP, S_DTR };
 HD int misc_len(int nq) { return M_Q + NQARR * nq; }
 HD long slot_len(const Dims& D) { return (long)NV * D.n + misc_len(D.nq); }
+HD long hot_len(const Dims& D) { return (long)V_K0 * D.n + misc_len(D.nq); }     // vectors before k1 + MISC
+HD long stage_len(const Dims& D) { return (long)(NV - V_K0) * D.n; }             // k1..k8
 HD long dense_len(const Dims& D) { return (long)D.n * D.n + D.n; }
 
 // Element stride follows the group width: one thread per mode interleaves
@@ -211,11 +216,12 @@ HD long dense_len(const Dims& D) { return (long)D.n * D.n + D.n; }
 template <int G>
 struct WS {
   static constexpr int S = (G == 1) ? 32 : 1;
-  double* p;      // vectors + MISC
+  double* p;      // vectors 0 .. V_K0-1, then MISC at misc0 = V_K0 n
+  double* kp;     // stage vectors: element (s, j) of k_{s+1} at kp[(s n + j) S]
   int n;
   int misc0;
   double* dp;     // dense matrix + pivots (dense path only)
-  HD double& v(int vec, int j) const { return p[(vec * n + j) * S]; }
+  HD double& v(int vec, int j) const { return vec < V_K0 ? p[(vec * n + j) * S] : kp[((vec - V_K0) * n + j) * S]; }
   HD double& m(int off) const { return p[(misc0 + off) * S]; }
   HD double& e(int off) const { return dp[off * S]; }
 };

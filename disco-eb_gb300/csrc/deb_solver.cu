@@ -40,7 +40,9 @@ struct KParams {
   double* y_out;
   int* status;
   int* steps;
-  double* ws;         // lane mode: interleaved slots; warp mode: unused (shared memory) unless smem == 0
+  double* ws;         // lane mode: interleaved slots; warp mode: slots unless smem == 1
+  double* kws;        // warp mode with smem == 1 and stage vectors outside shared memory: [warps, 8 n]
+  long hot_len;       // warp mode: doubles of the slot in shared memory
   double* dws;        // dense matrices (dense path only)
   long slot_len, dense_len;
   int smem;           // warp mode: slots live in dynamic shared memory
@@ -95,7 +97,8 @@ __global__ void __launch_bounds__(kBlock) forward_lane_kernel(KParams P) {
   deb::WS<1> w;
   w.p = P.ws + warp * 32 * P.slot_len + lane;
   w.n = P.D.n;
-  w.misc0 = deb::NV * P.D.n;
+  w.misc0 = deb::V_K0 * P.D.n;
+  w.kp = w.p + (long)deb::hot_len(P.D) * 32;
   w.dp = P.dws ? P.dws + warp * 32 * P.dense_len + lane : nullptr;
   const deb::Grp<1> gp{0};
   int mode = -1;
@@ -136,7 +139,9 @@ __global__ void __launch_bounds__(32) forward_warp_kernel(KParams P) {
   deb::WS<32> w;
   w.p = P.smem ? smem : P.ws + gwarp * P.slot_len;
   w.n = P.D.n;
-  w.misc0 = deb::NV * P.D.n;
+  w.misc0 = deb::V_K0 * P.D.n;
+  // stage vectors after MISC in the same slot, or in their own global region
+  w.kp = (P.smem && P.kws) ? P.kws + gwarp * deb::stage_len(P.D) : w.p + deb::hot_len(P.D);
   w.dp = P.dws ? P.dws + gwarp * P.dense_len : nullptr;
   const deb::Grp<32> gp{lane};
   deb::Cosmo c;
@@ -213,7 +218,9 @@ struct deb_plan {
   // lane mode
   int lane_blocks, lane_slots;
   // warp mode
-  int warp_block_warps, warp_blocks, warp_smem;
+  int warp_block_warps, warp_blocks, warp_smem, warp_k_global;
+  long warp_smem_bytes;
+  double* kws;      // warp mode: stage vectors in global memory
   double* ws;       // lane slots (or warp slots when shared memory is too small)
   double* dws;      // dense matrices
   int* queue;
@@ -286,14 +293,22 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
     p->lane_slots = p->lane_blocks * kBlock;
     nslots = p->lane_slots;
   } else {
-    const long slot_bytes = p->slot_len * 8;
-    p->warp_smem = slot_bytes <= smem_optin;
+    // a mode's whole slot in shared memory when 8 modes fit per SM, else only
+    // the hot part (vectors before k1 + MISC) with k1..k8 in global memory
+    // (L2-resident, lane-strided coalesced access)
+    const long full_bytes = p->slot_len * 8, hot_bytes = deb::hot_len(p->D) * 8;
+    const long sm_bytes = 228L * 1024;
+    long smem_bytes;
+    if (sm_bytes / (full_bytes + 1024) >= 8) { smem_bytes = full_bytes; p->warp_k_global = 0; }
+    else { smem_bytes = hot_bytes; p->warp_k_global = 1; }
+    p->warp_smem = smem_bytes <= smem_optin;
+    if (!p->warp_smem) p->warp_k_global = 0;
     p->warp_block_warps = 1;
-    // blocks (= modes in flight) per SM limited by shared memory and by the
-    // 255-register budget of a 1-warp block (8 warps per SM)
-    int per_sm = 8;
+    // blocks (= modes in flight) per SM limited by shared memory and by
+    // registers (at most 12 one-warp blocks)
+    int per_sm = 12;
     if (p->warp_smem) {
-      const int by_smem = (int)((228L * 1024) / (slot_bytes + 1024));
+      const int by_smem = (int)(sm_bytes / (smem_bytes + 1024));
       if (by_smem < per_sm) per_sm = by_smem;
       if (per_sm < 1) per_sm = 1;
     }
@@ -303,8 +318,9 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
     long nw = want < cap_warps ? want : cap_warps;
     p->warp_blocks = (int)nw;
     nslots = nw;
+    p->warp_smem_bytes = smem_bytes;
     if (p->warp_smem) {
-      if (cudaFuncSetAttribute(forward_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)slot_bytes) != cudaSuccess) {
+      if (cudaFuncSetAttribute(forward_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes) != cudaSuccess) {
         delete p;
         return DEB_ERR_CUDA;
       }
@@ -314,7 +330,14 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
   p->ws_bytes = (size_t)nslots * (need_ws ? p->slot_len : 0) * sizeof(double) + (size_t)nslots * p->dense_len * sizeof(double);
   p->ws = nullptr;
   p->dws = nullptr;
+  p->kws = nullptr;
   if (need_ws && cudaMalloc(&p->ws, (size_t)nslots * p->slot_len * sizeof(double)) != cudaSuccess) { delete p; return DEB_ERR_NOMEM; }
+  if (mode == DEB_EXEC_WARP && p->warp_k_global) {
+    if (cudaMalloc(&p->kws, (size_t)nslots * deb::stage_len(p->D) * sizeof(double)) != cudaSuccess) {
+      cudaFree(p->ws); delete p; return DEB_ERR_NOMEM;
+    }
+    p->ws_bytes += (size_t)nslots * deb::stage_len(p->D) * sizeof(double);
+  }
   if (p->dense && cudaMalloc(&p->dws, (size_t)nslots * p->dense_len * sizeof(double)) != cudaSuccess) {
     cudaFree(p->ws); delete p; return DEB_ERR_NOMEM;
   }
@@ -333,6 +356,7 @@ void deb_plan_destroy(deb_plan* p) {
   if (!p) return;
   cudaFree(p->ws);
   cudaFree(p->dws);
+  cudaFree(p->kws);
   cudaFree(p->queue);
   delete p;
 }
@@ -359,6 +383,7 @@ int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, in
   P.nmode = nmode; P.tau_out = d_tau_out; P.y_out = d_y_out; P.status = d_status; P.steps = d_steps;
   P.ws = p->ws; P.dws = p->dws; P.slot_len = p->slot_len; P.dense_len = p->dense_len; P.queue = p->queue; P.D = p->D;
   P.smem = p->warp_smem;
+  P.kws = p->kws;
   P.rec = d_record; P.rec_len = rec_len; P.nrec = d_nrec; P.nset = nset;
   P.ctl.rtol = cfg->rtol; P.ctl.atol = cfg->atol;
   P.ctl.b1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / cfg->error_order;
@@ -378,7 +403,7 @@ int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, in
     const int wpb = p->warp_block_warps;
     long need = (items + wpb - 1) / wpb;
     const int blocks = (int)(need < p->warp_blocks ? need : p->warp_blocks);
-    const size_t smem = p->warp_smem ? (size_t)p->slot_len * 8 * wpb : 0;
+    const size_t smem = p->warp_smem ? (size_t)p->warp_smem_bytes * wpb : 0;
     forward_warp_kernel<<<blocks, 32 * wpb, smem, s>>>(P);
   }
   if (cudaGetLastError() != cudaSuccess) return DEB_ERR_CUDA;
@@ -464,7 +489,7 @@ int deb_forward_static(const deb_dims* dims, const double* d_tables, int ncosmo,
   P.nmode = nmode; P.tau_out = d_tau_out; P.y_out = d_y_out; P.status = d_status; P.steps = d_steps;
   P.ws = base + 256 / sizeof(double); P.dws = nullptr; P.slot_len = slot_len; P.dense_len = 0;
   P.queue = (int*)base; P.D = D; P.smem = 0;
-  P.rec = nullptr; P.rec_len = 0; P.nrec = nullptr; P.nset = 1;
+  P.rec = nullptr; P.rec_len = 0; P.nrec = nullptr; P.nset = 1; P.kws = nullptr;
   P.ctl.rtol = cfg->rtol; P.ctl.atol = cfg->atol;
   P.ctl.b1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / cfg->error_order;
   P.ctl.b2 = -(cfg->pcoeff + 2.0 * cfg->dcoeff) / cfg->error_order;

@@ -24,7 +24,8 @@ bool setup(Ctx& x, const double* blob, int blob_len, const int* dims, double k, 
   // the one-thread-per-mode layout interleaves 32 modes; lane 0 is used here
   x.buf.assign(slot_len(x.D) * 32, 0.0);
   x.dbuf.assign(dense ? dense_len(x.D) * 32 : 1, 0.0);
-  x.w.p = x.buf.data(); x.w.n = x.D.n; x.w.misc0 = NV * x.D.n;
+  x.w.p = x.buf.data(); x.w.n = x.D.n; x.w.misc0 = V_K0 * x.D.n;
+  x.w.kp = x.w.p + hot_len(x.D) * 32;
   x.w.dp = x.dbuf.data();
   for (int i = 0; i < x.D.nq; ++i) {
     double q = x.c.q[i];
