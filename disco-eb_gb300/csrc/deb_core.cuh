@@ -1111,24 +1111,35 @@ struct Ctl {
   int step_ts;  // clip steps to land on every output time (diffrax PIDController(step_ts=ts))
 };
 
-// first output time strictly after t (or +inf)
-HD double next_output_after(const double* tau_out, int nout, double t) {
+// first output time strictly after t (or +inf) and its index (or -1)
+HD double next_output_after(const double* tau_out, int nout, double t, int* which = nullptr) {
   double best = 1e300;
+  int bi = -1;
   for (int o = 0; o < nout; ++o) {
     const double to = LDG(tau_out + o);
-    if (to > t && to < best) best = to;
+    if (to > t && to < best) { best = to; bi = o; }
   }
+  if (which) *which = bi;
   return best;
 }
 
 // Integration state; every lane of a group holds an identical copy.
-// rec: [tau_start, t_1, ..., t_nrec] of the nominal run (record / replay).
+// rec: [tau_start, t_1, ..., t_nrec] of the nominal run (record / replay);
+// a step that was clipped to output time o is stored as -(o + 1).
 struct Run {
   double t0, t1, T1, prev_inv, prev_prev_inv;
   int vy, vy1, steps, acc, rej, status;
   double* rec;
   int rec_cap, nrec;
+  double scale;   // replay: tau_start / nominal tau_start
+  int t1_out;     // index of the output time the current step is clipped to, or -1
 };
+
+// replay: end time of recorded step j (1-based) for this table set
+HD double replay_time(const Run& r, const double* tau_out, int j) {
+  const double v = LDG(r.rec + j);
+  return v < 0.0 ? LDG(tau_out + (int)(-v) - 1) : v * r.scale;
+}
 
 // start a mode: start time, ICs, first step size (perturbations.py:742-756)
 template <int G>
@@ -1136,24 +1147,27 @@ HD void mode_begin(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const D
                    const double* tau_out, Run& r) {
   double tmax = LDG(tau_out), tmin = tmax;
   for (int o = 1; o < ctl.nout; ++o) { const double t = LDG(tau_out + o); tmax = t > tmax ? t : tmax; tmin = t < tmin ? t : tmin; }
-  double t0;
-  if (ctl.replay) {
-    t0 = r.rec[0];
-  } else {
-    const double ts = start_time(c, m);
-    t0 = 0.99 * (tmin < ts ? tmin : ts);
-  }
+  // start time of this table set.  In a replay the recorded step times are
+  // scaled by tau_start / nominal tau_start: with the step-size factors
+  // frozen every step length is proportional to dt0 = tau_start / 4, which
+  // is how jax.jacfwd sees the diffrax step sequence.
+  const double ts = start_time(c, m);
+  const double t0 = 0.99 * (tmin < ts ? tmin : ts);
   initial_conditions<G>(gp, c, m, D, t0, w, V_Y);
   r.t0 = t0; r.T1 = tmax;
+  r.t1_out = -1;
   if (ctl.replay) {
-    const double tn = r.nrec > 1 ? LDG(r.rec + 1) : tmax;
+    r.scale = t0 / LDG(r.rec);
+    const double tn = r.nrec > 1 ? replay_time(r, tau_out, 1) : tmax;
     r.t1 = (r.nrec <= 1 || tn >= tmax) ? tmax : tn;
   } else {
+    r.scale = 1.0;
     const double dt0 = (t0 / 4.0 < 0.5 * (tmax - t0)) ? t0 / 4.0 : 0.5 * (tmax - t0);
     r.t1 = t0 + dt0 < tmax ? t0 + dt0 : tmax;
     if (ctl.step_ts) {
-      const double to = next_output_after(tau_out, ctl.nout, t0);
-      if (r.t1 > to) r.t1 = to;
+      int o;
+      const double to = next_output_after(tau_out, ctl.nout, t0, &o);
+      if (r.t1 >= to) { r.t1 = to; r.t1_out = o; }
     }
     if (ctl.record && gp.lead()) r.rec[0] = t0;
   }
@@ -1274,12 +1288,12 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
     r.t0 = r.t1;
     r.prev_prev_inv = r.prev_inv;
     r.prev_inv = inv;
-    if (ctl.record && gp.lead() && r.acc < r.rec_cap) r.rec[r.acc] = r.t1;
+    if (ctl.record && gp.lead() && r.acc < r.rec_cap) r.rec[r.acc] = r.t1_out >= 0 ? -(r.t1_out + 1.0) : r.t1;
     if (ctl.replay) {
-      // next recorded end time; the run ends at this cosmology's own final
+      // next recorded end time; the run ends at this table set's own final
       // output time (the recorded one is the nominal cosmology's)
       if (r.t0 >= r.T1) return false;
-      double tn = r.acc + 1 < r.nrec ? LDG(r.rec + r.acc + 1) : r.T1;
+      double tn = r.acc + 1 < r.nrec ? replay_time(r, tau_out, r.acc + 1) : r.T1;
       if (r.acc + 1 >= r.nrec || tn >= r.T1) tn = r.T1;
       r.t1 = tn;
       return true;
@@ -1289,9 +1303,11 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
     if (ctl.hist_on_reject) { r.prev_prev_inv = r.prev_inv; r.prev_inv = inv; }
   }
   double tn = r.t0 + dtn;
+  r.t1_out = -1;
   if (ctl.step_ts) {
-    const double to = next_output_after(tau_out, ctl.nout, r.t0);
-    if (tn > to) tn = to;
+    int o;
+    const double to = next_output_after(tau_out, ctl.nout, r.t0, &o);
+    if (tn >= to) { tn = to; r.t1_out = o; }
   }
   if (tn > r.T1 - 1e-10) tn = r.T1;
   if (!(tn > r.t0) && r.t0 < r.T1) { r.status = ST_DT_UNDERFLOW; return false; }

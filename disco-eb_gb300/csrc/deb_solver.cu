@@ -293,13 +293,13 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
     p->lane_slots = p->lane_blocks * kBlock;
     nslots = p->lane_slots;
   } else {
-    // a mode's whole slot in shared memory when 8 modes fit per SM, else only
+    // a mode's whole slot in shared memory when 2 modes fit per SM, else only
     // the hot part (vectors before k1 + MISC) with k1..k8 in global memory
     // (L2-resident, lane-strided coalesced access)
     const long full_bytes = p->slot_len * 8, hot_bytes = deb::hot_len(p->D) * 8;
     const long sm_bytes = 228L * 1024;
     long smem_bytes;
-    if (sm_bytes / (full_bytes + 1024) >= 8) { smem_bytes = full_bytes; p->warp_k_global = 0; }
+    if (sm_bytes / (full_bytes + 1024) >= 2) { smem_bytes = full_bytes; p->warp_k_global = 0; }
     else { smem_bytes = hot_bytes; p->warp_k_global = 1; }
     p->warp_smem = smem_bytes <= smem_optin;
     if (!p->warp_smem) p->warp_k_global = 0;

@@ -132,8 +132,10 @@ def test_replay_on_nominal_tables_reproduces_the_solve(fid):
 
 
 def test_frozen_step_gradient_at_end_time_matches_tight_differences():
-    """d log P(k, a=1) / d Omega_m from the frozen-step replay (rtol 1e-6)
-    against central differences of two independent rtol 1e-9 solves."""
+    """d log P(k, a=1) / d Omega_m from the replay (rtol 1e-6; start time
+    recomputed per table set, recorded step times scaled with it, final step
+    at the set's own output time) against central differences of two
+    independent rtol 1e-9 solves."""
     from discoeb_gb300.workloads import fiducial_mnu_param as fp
     dims = dict(lmaxg=8, lmaxgp=8, lmaxr=10, lmaxnu=8, nqmax=3)
     base = fp()
@@ -153,4 +155,4 @@ def test_frozen_step_gradient_at_end_time_matches_tight_differences():
     ya, _ = H.solve(tabs[0], k, taus[0], rtol=1e-9, atol=1e-12, max_steps=2000000, **dims)
     yb, _ = H.solve(tabs[1], k, taus[1], rtol=1e-9, atol=1e-12, max_steps=2000000, **dims)
     gt = (np.log(ya[:, 0, 4] ** 2) - np.log(yb[:, 0, 4] ** 2)) / (2 * eps)
-    assert np.abs(g - gt).max() <= 1e-3 * np.abs(gt).max()
+    assert np.abs(g - gt).max() <= 1e-5 * np.abs(gt).max()

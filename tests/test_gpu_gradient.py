@@ -1,16 +1,18 @@
-"""GPU gradient d log P / d theta (frozen-step tangents) against the host.
+"""GPU gradient d log P / d theta (jacfwd-style tangents of the step sequence) against the host.
 
 * all outputs, steps landing on the output times (step_to_outputs): the
   same frozen-step algorithm run by the host build of the kernel core
-  (record + replay), tolerance 1e-3 of each parameter's largest
+  (record + replay), tolerance 1e-4 of each parameter's largest
   |d log P / d theta| (the nominal step sequences of the two runs can differ
-  by a rounding-flipped decision, which moves the derivative by the
-  discretisation error).  With the reference's default outputs (linear
+  by a rounding-flipped decision; the derivative itself is accurate to ~1e-6
+  at rtol 1e-6, so that barely moves it);  With the reference's default outputs (linear
   interpolation inside a step) an interior output's derivative is the slope
   of that interpolant, which depends on where the steps fall; only the end
   time is compared then;
-* end-time output: central differences of two independent tight-tolerance
-  oracle solves (rtol 1e-9), the same 1e-3 bar.
+* central differences of two independent tight-tolerance oracle solves
+  (rtol 1e-9): the end time with default outputs, and every output with
+  steps landing on the output times, 1e-4 of the parameter's largest
+  derivative (the required bar is 1e-3).
 """
 import numpy as np
 import pytest
@@ -54,7 +56,7 @@ def test_gradient_matches_host_frozen_step_replay(setup):
         g = (lp[2 * j] - lp[2 * j + 1]) / (2 * eps)
         col = THETA.index(name)
         scale = np.abs(g).max()
-        assert np.abs(D[:, :, col] - g).max() <= 1e-3 * scale, name
+        assert np.abs(D[:, :, col] - g).max() <= 1e-4 * scale, name
     # analytic parameters (perturbations.py:1123)
     np.testing.assert_allclose(D[:, :, THETA.index("A_s")], 1.0 / base["A_s"])
     np.testing.assert_allclose(D[:, :, THETA.index("n_s")], np.log(k / 0.05)[:, None] * np.ones((1, 8)))
@@ -78,7 +80,7 @@ def test_default_output_semantics_end_time_matches_host(setup):
     for j, (name, eps, _, _) in enumerate(pert):
         g = (lp[2 * j, :, -1] - lp[2 * j + 1, :, -1]) / (2 * eps)
         col = THETA.index(name)
-        assert np.abs(D[:, -1, col] - g).max() <= 1e-3 * np.abs(g).max(), name
+        assert np.abs(D[:, -1, col] - g).max() <= 1e-4 * np.abs(g).max(), name
 
 
 def test_end_time_gradient_matches_tight_oracle_differences(setup):
@@ -94,7 +96,27 @@ def test_end_time_gradient_matches_tight_oracle_differences(setup):
         assert (sp[:, 0] == 0).all() and (sm[:, 0] == 0).all()
         gt = (np.log(yp[:, 0, 4] ** 2) - np.log(ym[:, 0, 4] ** 2)) / (2 * eps)
         col = THETA.index(name)
-        assert np.abs(D[:, 0, col] - gt).max() <= 1e-3 * np.abs(gt).max(), name
+        assert np.abs(D[:, 0, col] - gt).max() <= 1e-4 * np.abs(gt).max(), name
+
+
+def test_interior_output_gradient_matches_tight_oracle_differences(setup):
+    """All 8 outputs in a = [0.2, 1] with steps landing on the output times:
+    GPU gradient (rtol 1e-6) against central differences of two rtol 1e-9
+    oracle solves run the same way."""
+    base, pert, bgs = setup
+    a_out = np.linspace(0.2, 1.0, 8)
+    P, D, k = deb.evolve_perturbations_grad(params=base, aexp_out=a_out, kmin=1e-3, kmax=1.0, num_k=4, rtol=1e-6,
+                                            atol=1e-9, max_steps=20000, backgrounds=[bgs], step_to_outputs=True, **DIMS)
+    for j, (name, eps, _, _) in enumerate(pert[:3]):
+        bp, bm = bgs[1 + 2 * j], bgs[2 + 2 * j]
+        yp, sp = oracle.solve(tb.pack_cosmology(bp, 3), k, tb.tau_of_a(bp, a_out), rtol=1e-9, atol=1e-12,
+                              max_steps=2000000, step_to_outputs=True, **DIMS)
+        ym, sm = oracle.solve(tb.pack_cosmology(bm, 3), k, tb.tau_of_a(bm, a_out), rtol=1e-9, atol=1e-12,
+                              max_steps=2000000, step_to_outputs=True, **DIMS)
+        assert (sp[:, 0] == 0).all() and (sm[:, 0] == 0).all()
+        gt = (np.log(yp[..., 4] ** 2) - np.log(ym[..., 4] ** 2)) / (2 * eps)
+        col = THETA.index(name)
+        assert np.abs(D[:, :, col] - gt).max() <= 1e-4 * np.abs(gt).max(), name
 
 
 def test_fisher_matrix_is_symmetric_and_positive(setup):
