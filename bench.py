@@ -49,10 +49,9 @@ DEFAULT_WORKLOAD = "batched_8cosmo_512k_n323_rtol1e-5_grad"
 
 
 def _dist():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from discoeb_gb300.sharding import dist_env
+
+    return dist_env()
 
 
 def make_inputs(name, rank=0, world=1, seed=1234):
@@ -62,8 +61,10 @@ def make_inputs(name, rank=0, world=1, seed=1234):
 
     ncosmo, num_k, kmin, kmax, dims, rtol, atol = WORKLOADS[name]
     grad = name.endswith("_grad")
+    from discoeb_gb300.sharding import shard
+
     params, rejected = sample_cosmologies(ncosmo * world, seed=seed)
-    mine = params[rank * ncosmo:(rank + 1) * ncosmo]
+    mine = [params[i] for i in shard(ncosmo, world, rank)]
     pert, bgs = None, None
     if grad:
         pert = [perturbed_params(p) for p in mine]
@@ -222,11 +223,9 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
     kern_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
-    t_step = wall / args.steps
-    if world > 1:
-        tt = torch.tensor([t_step], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(tt.item())
+    from discoeb_gb300.sharding import max_over_ranks
+
+    t_step = max_over_ranks(wall / args.steps, device="cuda")
     total_cosmo = inp["ncosmo"] * world
     value = total_cosmo / t_step
 
@@ -308,11 +307,9 @@ def run_gradient(args, inp, world, rank, local):
         torch.distributed.barrier()
     rec_ms = [e[0].elapsed_time(e[1]) for e in evs]
     rep_ms = [e[1].elapsed_time(e[2]) for e in evs]
-    t_step = wall / args.steps
-    if world > 1:
-        tt = torch.tensor([t_step], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(tt.item())
+    from discoeb_gb300.sharding import max_over_ranks
+
+    t_step = max_over_ranks(wall / args.steps, device="cuda")
     total_cosmo = inp["ncosmo"] * world
     value = total_cosmo / t_step
 
