@@ -54,6 +54,29 @@ HD bool isfinite_(double x) { return std::isfinite(x); }
 HD bool isfinite_(double x) { return isfinite(x); }
 #endif
 
+// Reciprocal for positive, normal arguments whose reciprocal is normal (all
+// uses here: pivots >= 1/(gamma h), a, tau, aH, error scales).  Device: the
+// PTX approximate reciprocal as seed, then two Newton-Raphson steps
+// y <- y + y (1 - x y), each doubling the correct bits; about 1 ulp.  One
+// FP64 division costs several times as many FP64 instructions.
+HD double rcp(double x) {
+#ifdef __CUDA_ARCH__
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+#else
+  return 1.0 / x;
+#endif
+}
+#ifdef __CUDACC__
+HD double rsqrt_(double x) { return rsqrt(x); }
+#else
+HD double rsqrt_(double x) { return 1.0 / std::sqrt(x); }
+#endif
+
 // ------------------------------------------------------------------ blob layout
 enum { H_OMEGAM = 0, H_OMEGAB, H_OMEGADE, H_OMEGAK, H_GRHOM, H_GRHOG, H_GRHOR, H_NEFF, H_NMNU,
        H_AMNU, H_W0, H_WA, H_CS2DE, H_YHE, H_H0, H_TAUMIN, H_AS, H_NS, H_KP, H_NQ,
@@ -77,7 +100,7 @@ HD Dual operator+(Dual a, Dual b) { return Dual(a.v + b.v, a.d + b.d); }
 HD Dual operator-(Dual a, Dual b) { return Dual(a.v - b.v, a.d - b.d); }
 HD Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
 HD Dual operator*(Dual a, Dual b) { return Dual(a.v * b.v, a.d * b.v + a.v * b.d); }
-HD Dual operator/(Dual a, Dual b) { double r = 1.0 / b.v; double q = a.v * r; return Dual(a.v / b.v, (a.d - q * b.d) * r); }
+HD Dual operator/(Dual a, Dual b) { double r = rcp(b.v); double q = a.v * r; return Dual(q, (a.d - q * b.d) * r); }
 HD Dual operator+(Dual a, double b) { return Dual(a.v + b, a.d); }
 HD Dual operator+(double a, Dual b) { return Dual(a + b.v, b.d); }
 HD Dual operator-(Dual a, double b) { return Dual(a.v - b, a.d); }
@@ -85,13 +108,17 @@ HD Dual operator-(double a, Dual b) { return Dual(a - b.v, -b.d); }
 HD Dual operator*(Dual a, double b) { return Dual(a.v * b, a.d * b); }
 HD Dual operator*(double a, Dual b) { return Dual(a * b.v, a * b.d); }
 HD Dual operator/(Dual a, double b) { return Dual(a.v / b, a.d / b); }
-HD Dual operator/(double a, Dual b) { double r = 1.0 / b.v; return Dual(a / b.v, -a * b.d * r * r); }
+HD Dual operator/(double a, Dual b) { double r = rcp(b.v); double q = a * r; return Dual(q, -q * b.d * r); }
 HD Dual dexp(Dual a) { double e = exp(a.v); return Dual(e, e * a.d); }
 HD Dual dlog(Dual a) { return Dual(log(a.v), a.d / a.v); }
 HD Dual dsqrt(Dual a) { double s = sqrt(a.v); return Dual(s, 0.5 * a.d / s); }
 HD double dexp(double a) { return exp(a); }
 HD double dlog(double a) { return log(a); }
 HD double dsqrt(double a) { return sqrt(a); }
+HD Dual drsqrt(Dual a) { double r = rsqrt_(a.v); return Dual(r, -0.5 * r * r * r * a.d); }
+HD double drsqrt(double a) { return rsqrt_(a); }
+HD Dual drcp(Dual a) { double r = rcp(a.v); return Dual(r, -r * r * a.d); }
+HD double drcp(double a) { return rcp(a); }
 HD double val(double x) { return x; }
 HD double val(Dual x) { return x.v; }
 HD double der(double) { return 0.0; }
@@ -187,24 +214,28 @@ HD Dims make_dims(int lg, int lgp, int lr, int lnu, int nq) {
 }
 
 // ------------------------------------------------------------------ workspace
-// Per-mode scratch: NV vectors of length n plus a MISC block.  Slot layout:
+// Per-mode scratch: NV vectors of length n plus a MISC block.  Two state
+// vectors swap roles on every accepted step: y0, and the stage state that
+// ends the step holding y1.  The RHS writes straight into the stage vector
+// it feeds.  Slot layout:
 // [vectors 0 .. V_K0-1][MISC][stage vectors k1..k8]; element e of a slot lives
 // at base[e * stride] (stride 32 interleaves the 32 modes of a warp so that
 // every access of the warp is one coalesced transaction).  The warp-per-mode
 // kernel keeps the first two parts in shared memory and may keep the stage
 // vectors in global memory (kp).
-enum { V_Y = 0, V_Y1, V_U, V_F, V_JC0, V_LO, V_UP, V_PI, V_ZH, V_ZE, V_K0, NV = V_K0 + 8 };
+enum { V_Y = 0, V_U, V_JC0, V_LO, V_UP, V_PI, V_ZH, V_ZE, V_K0, NV = V_K0 + 8 };
 // MISC block offsets
 enum { M_CORE = 0,          // 8x8 core LU (row-major)           64
        M_CPIV = 64,         // core pivots                         8
        M_DE = 72,           // DE 2x2 LU + pivot flag              5
        M_CINV = 77,         // Woodbury capacitance inverse        4
-       M_SCAL = 81,         // cached per-step scalars            24
-       M_CINV8 = 105,       // explicit inverse of the 8x8 core    64
-       M_Q = 169 };         // per-q arrays: v, dv/da, dlfdlq, ghq, geq, r1q, dTq  (7 nq)
-enum { Q_V = 0, Q_DV, Q_DLF, Q_GH, Q_GE, Q_R1, Q_DT, NQARR };
+       M_SCAL = 81,         // cached per-step scalars            32
+       M_CINV8 = 113,       // explicit inverse of the 8x8 core    64
+       M_Q = 177 };         // per-q arrays: v, dv/da, dlfdlq, ghq, geq, r1q, dTq, m_nu/q  (8 nq)
+enum { Q_V = 0, Q_DV, Q_DLF, Q_GH, Q_GE, Q_R1, Q_DT, Q_AMQ, NQARR };
 enum { S_D = 0, S_W00I, S_ID, S_IDAH, S_GH2, S_GH3, S_GH5, S_GH7, S_GHR0, S_GHQE, S_GE4, S_GE6, S_GE8,
-       S_GER1, S_GEQE, S_R13, S_R15, S_R17, S_R1R0, S_R1QE, S_R1QT, S_DTT, S_DTP, S_DTR };
+       S_GER1, S_GEQE, S_R13, S_R15, S_R17, S_R1R0, S_R1QE, S_R1QT, S_DTT, S_DTP, S_DTR,
+       S_FT, S_FP };   // folds of the photon T / P tails into the core diagonal
 HD int misc_len(int nq) { return M_Q + NQARR * nq; }
 HD long slot_len(const Dims& D) { return (long)NV * D.n + misc_len(D.nq); }
 HD long hot_len(const Dims& D) { return (long)V_K0 * D.n + misc_len(D.nq); }     // vectors before k1 + MISC
@@ -318,11 +349,12 @@ HD void background_finish(const ModeConst& m, S a, Bg<S>& g, S cs2a, S xe, S rho
   g.rhoQ = rhoQ;
   S grho = m.grhom * m.Om * g.ia + (m.grhog + m.grhor * (m.Neff + m.Nmnu * g.rhonu)) * g.ia2 +
            m.grhom * m.ODE * g.rhoQ * g.a2 + m.grhom * m.Ok;
-  g.aH = dsqrt(grho * (1.0 / 3.0));
-  g.iaH = 1.0 / g.aH;
+  const S g3 = grho * (1.0 / 3.0);
+  g.iaH = drsqrt(g3);
+  g.aH = g3 * g.iaH;
   g.wQ = m.w0 + m.wa * (1.0 - a);
   S wQp = -m.wa * g.aH * a;
-  g.ca2 = g.wQ - wQp / 3.0 / ((1.0 + g.wQ) + 1e-6) * g.iaH;
+  g.ca2 = g.wQ - wQp * (1.0 / 3.0) * drcp((1.0 + g.wQ) + 1e-6) * g.iaH;
   g.opac = g.xe * m.akthom * g.ia2;
   g.pb43 = (4.0 / 3.0) * m.photbar0 * g.ia;
 }
@@ -330,7 +362,7 @@ HD void background_finish(const ModeConst& m, S a, Bg<S>& g, S cs2a, S xe, S rho
 template <class S>
 HD void background_start(S a, Bg<S>& g) {
   g.a = a;
-  g.ia = 1.0 / a;
+  g.ia = drcp(a);
   g.ia2 = g.ia * g.ia;
   g.a2 = a * a;
   g.la = dlog(a);
@@ -381,7 +413,7 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
   const int n = D.n, nq = D.nq, iq0 = D.iq0, iq1 = iq0 + nq, iq2 = iq1 + nq, iq3 = iq2 + nq;
   const int igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
   const double k = m.k, k2 = m.k2;
-  const double itau = 1.0 / tau;
+  const double itau = rcp(tau);
   Bg<S> g;
   background_grp<S, G>(gp, c, m, make_var<S>(w.v(vin, 0)), g);
   if (gout) {
@@ -398,13 +430,13 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
   // massive neutrino momentum sums (nu_perturb, perturbations.py:22-50)
   S drhonu = 0.0, dpnu = 0.0, fnu = 0.0;
   for (int i = gp.lane; i < nq; i += G) {
-    const double amq = m.amnu / LDG(c.q + i);
-    S aq = g.a * amq;
-    S v = 1.0 / dsqrt(1.0 + aq * aq);
+    S aq = g.a * w.m(M_Q + Q_AMQ * nq + i);
+    const S s2 = 1.0 + aq * aq;
+    S v = drsqrt(s2);                           // v = 1 / sqrt(1 + (a m / q)^2)
     const double wq = LDG(c.w + i);
-    const double p0 = Y(iq0 + i);
-    drhonu = drhonu + wq * p0 / v;
-    dpnu = dpnu + wq * p0 * v;
+    const double wp0 = wq * Y(iq0 + i);
+    drhonu = drhonu + wp0 * (s2 * v);
+    dpnu = dpnu + wp0 * v;
     fnu = fnu + wq * Y(iq1 + i);
     w.m(M_Q + Q_V * nq + i) = val(v);         // v_q and d v_q / d a for the element loop
     if constexpr (kDual) w.m(M_Q + Q_DV * nq + i) = der(v);
@@ -427,6 +459,7 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
   if (gp.lead()) {
     S dgpres = (m.grhog * dg + m.grhor * m.Neff * dr) * g.ia2 * (1.0 / 3.0) + m.grhor * m.Nmnu * dpnu * g.ia2 +
                (m.cs2Q * m.grhom * m.ODE * dq * g.rhoQ * g.a2 + (m.cs2Q - g.ca2) * (3.0 * g.aH * rptQ * m.ik2));
+    const S i1w = drcp(1.0 + g.wQ);
     S alpha = (hp + 6.0 * etap) * 0.5 * m.ik2;
     put(0, g.aH * g.a);
     put(1, -(dgrho + 3.0 * dgpres) * g.a);
@@ -454,38 +487,37 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
     // dark-energy fluid (BL10 3.5, 3.6)
     put(n - 2, -(1.0 + g.wQ) * (tq + 0.5 * hp) - 3.0 * (m.cs2Q - g.wQ) * g.aH * dq -
                    9.0 * (1.0 + g.wQ) * (m.cs2Q - g.ca2) * g.aH * g.aH * m.ik2 * tq);
-    put(n - 1, -(1.0 - 3.0 * m.cs2Q) * g.aH * tq + m.cs2Q / (1.0 + g.wQ) * k2 * dq);
+    put(n - 1, -(1.0 - 3.0 * m.cs2Q) * g.aH * tq + m.cs2Q * i1w * k2 * dq);
   }
   for (int l = 3 + gp.lane; l < lg; l += G)
     put(7 + l, k * (T.lo[l] * Y(6 + l) - T.up[l] * Y(8 + l)) - g.opac * Y(7 + l));
   for (int l = 3 + gp.lane; l < lgp; l += G)
     put(igp + l, k * (T.lo[l] * Y(igp + l - 1) - T.up[l] * Y(igp + l + 1)) - g.opac * Y(igp + l));
   for (int l = 3 + gp.lane; l < lr; l += G) put(ir + l, S(k * (T.lo[l] * Y(ir + l - 1) - T.up[l] * Y(ir + l + 1))));
-  // massive neutrinos, l-major [l][q]; element e = l nq + i walked with
-  // incremental (l, i) so the loop needs no integer division
-  const int nmass = nq * (lnu + 1);
-  const int dl = G / nq, di = G - dl * nq;
-  int l = gp.lane / nq, i = gp.lane - l * nq;
+  // massive neutrinos, l-major [l][q].  l = 0, 1, 2 and lmax in one pass over
+  // q, then 3 <= l < lmax with element e = (l - 3) nq + i walked as
+  // incremental (l, i): every lane of a pass evaluates the same formula.
   const S hp6 = hp * (1.0 / 6.0);
   const S hp_eta = hp * (1.0 / 15.0) + 0.4 * etap;
-  for (int e = gp.lane; e < nmass; e += G) {
-    S v;
-    if constexpr (kDual) v = mk<S>(w.m(M_Q + Q_V * nq + i), w.m(M_Q + Q_DV * nq + i));
-    else v = w.m(M_Q + Q_V * nq + i);
-    S kv = k * v;
-    S f;
-    if (l == 0) {
-      f = -kv * Y(iq1 + i) + hp6 * w.m(M_Q + Q_DLF * nq + i);
-    } else if (l == 1) {
-      f = kv * (Y(iq0 + i) - 2.0 * Y(iq2 + i)) * (1.0 / 3.0);
-    } else if (l == 2) {
-      f = kv * (2.0 * Y(iq1 + i) - 3.0 * Y(iq3 + i)) * 0.2 - hp_eta * w.m(M_Q + Q_DLF * nq + i);
-    } else if (l < lnu) {
-      f = kv * (T.lo[l] * Y(iq0 + (l - 1) * nq + i) - T.up[l] * Y(iq0 + (l + 1) * nq + i));
-    } else {
-      f = kv * Y(iq0 + (lnu - 1) * nq + i) - (lnu + 1.0) * itau * Y(iq0 + lnu * nq + i);
-    }
-    put(iq0 + e, f);
+  auto vq = [&](int i) -> S {
+    if constexpr (kDual) return mk<S>(w.m(M_Q + Q_V * nq + i), w.m(M_Q + Q_DV * nq + i));
+    else return w.m(M_Q + Q_V * nq + i);
+  };
+  for (int i = gp.lane; i < nq; i += G) {
+    const S kv = k * vq(i);
+    const double dlf = w.m(M_Q + Q_DLF * nq + i);
+    const int jt = iq0 + lnu * nq + i;
+    put(iq0 + i, -kv * Y(iq1 + i) + hp6 * dlf);
+    put(iq1 + i, kv * (Y(iq0 + i) - 2.0 * Y(iq2 + i)) * (1.0 / 3.0));
+    put(iq2 + i, kv * (2.0 * Y(iq1 + i) - 3.0 * Y(iq3 + i)) * 0.2 - hp_eta * dlf);
+    put(jt, kv * Y(jt - nq) - (lnu + 1.0) * itau * Y(jt));
+  }
+  const int ngen = (lnu - 3) * nq;
+  const int dl = G / nq, di = G - dl * nq;
+  int l = 3 + gp.lane / nq, i = gp.lane - (l - 3) * nq;
+  for (int e = gp.lane; e < ngen; e += G) {
+    const int j = iq3 + e;
+    put(j, k * vq(i) * (T.lo[l] * Y(j - nq) - T.up[l] * Y(j + nq)));
     l += dl;
     i += di;
     if (i >= nq) { i -= nq; ++l; }
@@ -592,6 +624,7 @@ HD void initial_conditions(const Grp<G>& gp, const Cosmo& c, const ModeConst& m,
     w.v(vout, iq1 + i) = -dlf * tr / v / k / 3.0;
     w.v(vout, iq2 + i) = -0.5 * dlf * sr;
     w.m(M_Q + Q_DLF * nq + i) = dlf;
+    w.m(M_Q + Q_AMQ * nq + i) = m.amnu / q;
   }
   gp.sync();
 }
@@ -631,58 +664,75 @@ HD double start_time(const Cosmo& c, const ModeConst& m) {
 
 // ------------------------------------------------------------------ structured factorization
 // Chains of M = d I - B (see file header).  A chain is the list of indices
-// start, start+stride, ... ; LO[i] = M[i, prev], UP[i] = M[i, next].
-// Bottom-up elimination: p_last = M_ii, p_i = M_ii - UP_i LO_next / p_next,
-// PI = 1/p.  Every chain pivot is >= d > 0: UP_i LO_next < 0 for every
-// free-streaming hierarchy and the diagonal damping (opacity, truncation
-// (l+1)/tau) is non-negative.
+// start, start + stride, ...; its raw entries are lo = M[i, prev] and
+// up = M[i, next].  Bottom-up elimination: p_last = M_ii,
+// p_i = M_ii - up_i lo_next / p_next.  Every chain pivot is >= d > 0:
+// up_i lo_next < 0 for every free-streaming hierarchy and the diagonal
+// damping (opacity, truncation (l+1)/tau) is non-negative.  Stored per
+// element: PI = 1/p, UP = up / p_next (forward-sweep multiplier) and
+// LO = lo / p (back-substitution multiplier), so each sweep step is one
+// FMA on the dependency chain.
 // Chain numbering: 0 massless nu, 1..nq massive nu q-1, nq+1 photon T tail
 // (l >= 3, attached to T2 = index 9), nq+2 photon P tail (attached to P2).
+struct Chain { int start, stride, cnt, attach, lmax, l0; double kv; };
+
 template <int G>
-HD void chain_pivots(const WS<G>& w, int start, int stride, int cnt, double d_last, double d_rest) {
-  int i = start + (cnt - 1) * stride;
-  double pinv = 1.0 / d_last;
-  w.v(V_PI, i) = pinv;
-  for (int j = cnt - 2; j >= 0; --j) {
-    const int ii = start + j * stride;
-    const double p = d_rest - w.v(V_UP, ii) * w.v(V_LO, ii + stride) * pinv;
-    pinv = 1.0 / p;
-    w.v(V_PI, ii) = pinv;
+HD Chain chain_of(const ModeConst& m, const Dims& D, const WS<G>& w, int ch) {
+  Chain c;
+  c.kv = m.k;
+  if (ch == 0) { c.start = D.ir; c.stride = 1; c.cnt = D.lr + 1; c.attach = -1; c.lmax = D.lr; c.l0 = 0; }
+  else if (ch <= D.nq) {
+    c.start = D.iq0 + ch - 1; c.stride = D.nq; c.cnt = D.lnu + 1; c.attach = -1; c.lmax = D.lnu; c.l0 = 0;
+    c.kv = m.k * w.m(M_Q + Q_V * D.nq + ch - 1);
+  } else if (ch == D.nq + 1) { c.start = 10; c.stride = 1; c.cnt = D.lg - 2; c.attach = 9; c.lmax = D.lg; c.l0 = 3; }
+  else { c.start = D.igp + 3; c.stride = 1; c.cnt = D.lgp - 2; c.attach = D.igp + 2; c.lmax = D.lgp; c.l0 = 3; }
+  return c;
+}
+
+// raw entries of the chain element with multipole l (l = 2: a tail's attach
+// row).  Massless nu l = 0..2 follow the fluid equations of the RHS.
+HD void chain_entry(const ModeConst& m, const Tab& T, int ch, const Chain& c, int l, double& lo, double& up) {
+  if (ch == 0 && l <= 2) {
+    lo = l == 1 ? -0.25 * m.k2 : (l == 2 ? -8.0 / 15.0 : 0.0);
+    up = l == 0 ? 4.0 / 3.0 : (l == 1 ? 0.5 * m.k2 : 0.6 * m.k);
+  } else if (l == c.lmax) {
+    lo = -c.kv; up = 0.0;
+  } else if (c.attach >= 0 && l == 2) {
+    lo = 0.0; up = 0.6 * m.k;
+  } else {
+    lo = -c.kv * T.lo[l]; up = c.kv * T.up[l];
   }
 }
 
+// Factor chain ch (one lane).  A tail also stores its attach multiplier and
+// the fold up_attach lo_start / p_start of its elimination into the core.
 template <int G>
-HD void chain_fill_factor(const ModeConst& m, const Dims& D, const Tab& T, const WS<G>& w, double d, double itau, double op,
-                          int ch) {
-  const int nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
-  const double k = m.k, k2 = m.k2;
-  if (ch == 0) {
-    w.v(V_UP, ir) = 4.0 / 3.0;
-    w.v(V_LO, ir + 1) = -0.25 * k2; w.v(V_UP, ir + 1) = 0.5 * k2;
-    w.v(V_LO, ir + 2) = -8.0 / 15.0; w.v(V_UP, ir + 2) = 0.6 * k;
-    for (int l = 3; l < lr; ++l) { w.v(V_LO, ir + l) = -k * T.lo[l]; w.v(V_UP, ir + l) = k * T.up[l]; }
-    w.v(V_LO, ir + lr) = -k;
-    chain_pivots<G>(w, ir, 1, lr + 1, d + (lr + 1.0) * itau, d);
-  } else if (ch <= nq) {
-    const int i = ch - 1;
-    const double kv = k * w.m(M_Q + Q_V * nq + i);
-    for (int l = 0; l < lnu; ++l) {
-      const int e = iq0 + l * nq + i;
-      if (l > 0) w.v(V_LO, e) = -kv * T.lo[l];
-      w.v(V_UP, e) = kv * T.up[l];
-    }
-    w.v(V_LO, iq0 + lnu * nq + i) = -kv;
-    chain_pivots<G>(w, iq0 + i, nq, lnu + 1, d + (lnu + 1.0) * itau, d);
-  } else if (ch == nq + 1) {
-    w.v(V_UP, 9) = 0.6 * k;
-    for (int l = 3; l < lg; ++l) { w.v(V_LO, 7 + l) = -k * T.lo[l]; w.v(V_UP, 7 + l) = k * T.up[l]; }
-    w.v(V_LO, 7 + lg) = -k;
-    chain_pivots<G>(w, 10, 1, lg - 2, d + op + (lg + 1.0) * itau, d + op);
-  } else {
-    w.v(V_UP, igp + 2) = 0.6 * k;
-    for (int l = 3; l < lgp; ++l) { w.v(V_LO, igp + l) = -k * T.lo[l]; w.v(V_UP, igp + l) = k * T.up[l]; }
-    w.v(V_LO, igp + lgp) = -k;
-    chain_pivots<G>(w, igp + 3, 1, lgp - 2, d + op + (lgp + 1.0) * itau, d + op);
+HD void chain_factor(const ModeConst& m, const Dims& D, const Tab& T, const WS<G>& w, double d, double itau, double op,
+                     int ch) {
+  const Chain c = chain_of<G>(m, D, w, ch);
+  const double d_rest = c.attach >= 0 ? d + op : d;
+  int i = c.start + (c.cnt - 1) * c.stride;
+  double lo, up;
+  chain_entry(m, T, ch, c, c.l0 + c.cnt - 1, lo, up);
+  double pinv = rcp(d_rest + (c.lmax + 1.0) * itau);
+  w.v(V_PI, i) = pinv;
+  w.v(V_LO, i) = lo * pinv;
+  double lo_next = lo;
+  for (int j = c.cnt - 2; j >= 0; --j) {
+    i -= c.stride;
+    chain_entry(m, T, ch, c, c.l0 + j, lo, up);
+    const double qf = up * pinv;
+    pinv = rcp(d_rest - qf * lo_next);
+    w.v(V_UP, i) = qf;
+    w.v(V_PI, i) = pinv;
+    w.v(V_LO, i) = lo * pinv;
+    lo_next = lo;
+  }
+  if (c.attach >= 0) {
+    chain_entry(m, T, ch, c, 2, lo, up);
+    const double qa = up * pinv;
+    w.v(V_UP, c.attach) = qa;
+    w.m(M_SCAL + (ch == D.nq + 1 ? S_FT : S_FP)) = qa * lo_next;
   }
 }
 
@@ -699,7 +749,7 @@ HD void small_lu(const WS<G>& w, int off, int pivoff) {
     w.m(pivoff + kk) = (double)p;
     if (p != kk)
       for (int j = 0; j < N; ++j) { double t = w.m(off + kk * N + j); w.m(off + kk * N + j) = w.m(off + p * N + j); w.m(off + p * N + j) = t; }
-    const double inv = 1.0 / w.m(off + kk * N + kk);
+    const double inv = rcp(w.m(off + kk * N + kk));
     for (int i = kk + 1; i < N; ++i) {
       const double l = w.m(off + i * N + kk) * inv;
       w.m(off + i * N + kk) = l;
@@ -735,7 +785,7 @@ HD void core_entries(const ModeConst& m, const Tab& T, const Bg<double>& g, doub
   core[60] = -0.1 * op; core[61] = -0.1 * op; core[62] = -k * T.lo[2]; core[63] = d + 0.9 * op;
   de[0] = d + 3.0 * (m.cs2Q - g.wQ) * g.aH;
   de[1] = (1.0 + g.wQ) + 9.0 * (1.0 + g.wQ) * (m.cs2Q - g.ca2) * g.aH * g.aH * m.ik2;
-  de[2] = -m.cs2Q / (1.0 + g.wQ) * k2;
+  de[2] = -m.cs2Q * rcp(1.0 + g.wQ) * k2;
   de[3] = d + (1.0 - 3.0 * m.cs2Q) * g.aH;
 }
 
@@ -744,15 +794,15 @@ HD void core_entries(const ModeConst& m, const Tab& T, const Bg<double>& g, doub
 template <int G>
 HD void factor_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab& T, const WS<G>& w, double d, double tau,
                  const Bg<double>& g) {
-  const int nq = D.nq, igp = D.igp;
-  const double itau = 1.0 / tau, op = g.opac;
-  for (int ch = gp.lane; ch < nq + 3; ch += G) chain_fill_factor<G>(m, D, T, w, d, itau, op, ch);
+  const int nq = D.nq;
+  const double itau = rcp(tau), op = g.opac;
+  for (int ch = gp.lane; ch < nq + 3; ch += G) chain_factor<G>(m, D, T, w, d, itau, op, ch);
   gp.sync();
   if (gp.lead()) {
     double core[64], de[4];
     core_entries(m, T, g, d, core, de);
-    core[36] -= w.v(V_UP, 9) * w.v(V_LO, 10) * w.v(V_PI, 10);
-    core[63] -= w.v(V_UP, igp + 2) * w.v(V_LO, igp + 3) * w.v(V_PI, igp + 3);
+    core[36] -= w.m(M_SCAL + S_FT);
+    core[63] -= w.m(M_SCAL + S_FP);
     for (int i = 0; i < 64; ++i) w.m(M_CORE + i) = core[i];
     small_lu<8, G>(w, M_CORE, M_CPIV);
     // dark energy 2x2 (rows n-2, n-1): LU with partial pivoting, M_DE+4 = 1 if swapped
@@ -760,10 +810,10 @@ HD void factor_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab&
     double sw = 0.0;
     if (fabs(a10) > fabs(a00)) { double t0_ = a00, t1_ = a01; a00 = a10; a01 = a11; a10 = t0_; a11 = t1_; sw = 1.0; }
     const double l = a10 / a00;
-    w.m(M_DE + 0) = 1.0 / a00; w.m(M_DE + 1) = a01; w.m(M_DE + 2) = l; w.m(M_DE + 3) = 1.0 / (a11 - l * a01);
+    w.m(M_DE + 0) = 1.0 / a00; w.m(M_DE + 1) = a01; w.m(M_DE + 2) = l; w.m(M_DE + 3) = 1.0 / (a11 - l * a01);   // signs vary: true division
     w.m(M_DE + 4) = sw;
-    w.m(M_SCAL + S_ID) = 1.0 / d;
-    w.m(M_SCAL + S_IDAH) = 1.0 / (d + g.aH);
+    w.m(M_SCAL + S_ID) = rcp(d);
+    w.m(M_SCAL + S_IDAH) = rcp(d + g.aH);
   }
   gp.sync();
   // explicit inverse of the core from its LU factors, one column per lane,
@@ -797,40 +847,29 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>
     w.v(vr, n - 2) = z0; w.v(vr, n - 1) = z1;
   }
   for (int ch = gp.lane; ch < nq + 3; ch += G) {
-    if (ch <= nq) {
-      // full chain: forward sweep from the top, then back substitution from l = 0
-      const int start = ch == 0 ? ir : iq0 + ch - 1;
-      const int stride = ch == 0 ? 1 : nq;
-      const int cnt = ch == 0 ? lr + 1 : lnu + 1;
-      int i = start + (cnt - 1) * stride;
-      double rn = w.v(vr, i), pn = w.v(V_PI, i);
-      for (int j = cnt - 2; j >= 0; --j) {
-        i -= stride;
-        rn = w.v(vr, i) - w.v(V_UP, i) * rn * pn;
-        pn = w.v(V_PI, i);
-        w.v(vr, i) = rn;
-      }
-      double z = rn * pn;
+    // forward sweep from the top, r_i -= (up_i / p_next) r_next; a full chain
+    // then back-substitutes from l = 0, a tail folds into its attach row
+    const bool tail = ch > nq;
+    const int start = ch == 0 ? ir : (!tail ? iq0 + ch - 1 : (ch == nq + 1 ? 10 : igp + 3));
+    const int stride = (ch == 0 || tail) ? 1 : nq;
+    const int cnt = ch == 0 ? lr + 1 : (!tail ? lnu + 1 : (ch == nq + 1 ? lg - 2 : lgp - 2));
+    int i = start + (cnt - 1) * stride;
+    double rn = w.v(vr, i);
+    for (int j = cnt - 2; j >= 0; --j) {
+      i -= stride;
+      rn = w.v(vr, i) - w.v(V_UP, i) * rn;
+      w.v(vr, i) = rn;
+    }
+    if (!tail) {
+      double z = rn * w.v(V_PI, start);
       w.v(vr, start) = z;
       for (int j = 1; j < cnt; ++j) {
-        const int i = start + j * stride;
-        z = (w.v(vr, i) - w.v(V_LO, i) * z) * w.v(V_PI, i);
+        i += stride;
+        z = w.v(vr, i) * w.v(V_PI, i) - w.v(V_LO, i) * z;
         w.v(vr, i) = z;
       }
     } else {
-      // tail forward sweep up to the attach point
-      const int start = ch == nq + 1 ? 10 : igp + 3;
-      const int cnt = ch == nq + 1 ? lg - 2 : lgp - 2;
-      const int attach = start - 1;
-      int i = start + cnt - 1;
-      double rn = w.v(vr, i), pn = w.v(V_PI, i);
-      for (int j = cnt - 2; j >= 0; --j) {
-        --i;
-        rn = w.v(vr, i) - w.v(V_UP, i) * rn * pn;
-        pn = w.v(V_PI, i);
-        w.v(vr, i) = rn;
-      }
-      w.v(vr, attach) -= w.v(V_UP, attach) * rn * pn;
+      w.v(vr, start - 1) -= w.v(V_UP, start - 1) * rn;
     }
   }
   gp.sync();
@@ -852,7 +891,7 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>
     double z = w.v(vr, start - 1);
     for (int j = 0; j < cnt; ++j) {
       const int i = start + j;
-      z = (w.v(vr, i) - w.v(V_LO, i) * z) * w.v(V_PI, i);
+      z = w.v(vr, i) * w.v(V_PI, i) - w.v(V_LO, i) * z;
       w.v(vr, i) = z;
     }
   }
@@ -912,9 +951,9 @@ HD void factor_W(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dim
   for (int i = gp.lane; i < nq; i += G) {
     const double v = w.m(M_Q + Q_V * nq + i);
     const double wq = LDG(c.w + i);
-    w.m(M_Q + Q_GH * nq + i) = m.grhor * m.Nmnu * wq / v * g.ia2 * iaH;
+    w.m(M_Q + Q_GH * nq + i) = m.grhor * m.Nmnu * wq * rcp(v) * g.ia2 * iaH;
     w.m(M_Q + Q_GE * nq + i) = m.Nmnu * m.grhor * m.k * wq * g.ia2 * h2;
-    w.m(M_Q + Q_R1 * nq + i) = -m.grhor * m.Nmnu * wq * (1.0 / v + v) * g.ia;
+    w.m(M_Q + Q_R1 * nq + i) = -m.grhor * m.Nmnu * wq * (rcp(v) + v) * g.ia;
   }
   for (int j = gp.lane; j < n; j += G) { w.v(V_ZH, j) = 0.0; w.v(V_ZE, j) = 0.0; }
   factor_M<G>(gp, m, D, T, w, d, tau, g);   // syncs
@@ -1009,7 +1048,7 @@ HD void visit_g(const Dims& D, const WS<G>& w, F f) {
 template <int G>
 HD void dense_factor(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab& T, const WS<G>& w, double d, double tau,
                      const Bg<double>& g) {
-  const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
+  const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir;
   auto A = [&](int i, int j) -> double& { return w.e(i * n + j); };
   const double itau = 1.0 / tau, op = g.opac;
   for (int i = gp.lane; i < n; i += G) {
@@ -1017,25 +1056,23 @@ HD void dense_factor(const Grp<G>& gp, const ModeConst& m, const Dims& D, const 
     A(i, 0) -= w.v(V_JC0, i);
   }
   gp.sync();
-  auto chain = [&](int start, int stride, int cnt, double damp, double damp_last, bool attach) {
-    for (int j = 0; j < cnt; ++j) {
-      const int i = start + j * stride;
-      if (j > 0 || attach) A(i, i - stride) = w.v(V_LO, i);
-      if (j < cnt - 1) A(i, i + stride) = w.v(V_UP, i);
-      A(i, i) = d + (j == cnt - 1 ? damp_last : damp);
-    }
-  };
   for (int ch = gp.lane; ch < nq + 3; ch += G) {
-    if (ch == 0) chain(ir, 1, lr + 1, 0.0, (lr + 1.0) * itau, false);
-    else if (ch <= nq) chain(iq0 + ch - 1, nq, lnu + 1, 0.0, (lnu + 1.0) * itau, false);
-    else if (ch == nq + 1) chain(10, 1, lg - 2, op, op + (lg + 1.0) * itau, true);
-    else chain(igp + 3, 1, lgp - 2, op, op + (lgp + 1.0) * itau, true);
+    const Chain cc = chain_of<G>(m, D, w, ch);
+    const double damp = cc.attach >= 0 ? op : 0.0;
+    for (int j = 0; j < cc.cnt; ++j) {
+      const int i = cc.start + j * cc.stride;
+      double lo, up;
+      chain_entry(m, T, ch, cc, cc.l0 + j, lo, up);
+      if (j > 0 || cc.attach >= 0) A(i, i - cc.stride) = lo;
+      if (j < cc.cnt - 1) A(i, i + cc.stride) = up;
+      A(i, i) = d + damp + (j == cc.cnt - 1 ? (cc.lmax + 1.0) * itau : 0.0);
+    }
   }
   gp.sync();
   if (gp.lead()) {
     A(3, 4) = 1.0; A(4, 4) = d + g.aH;
-    A(9, 10) = w.v(V_UP, 9);
-    A(igp + 2, igp + 3) = w.v(V_UP, igp + 2);
+    A(9, 10) = 0.6 * m.k;
+    A(igp + 2, igp + 3) = 0.6 * m.k;
     double core[64], de[4];
     core_entries(m, T, g, d, core, de);
     const int cidx[8] = {5, 6, 7, 8, 9, igp, igp + 1, igp + 2};
@@ -1127,8 +1164,8 @@ HD double next_output_after(const double* tau_out, int nout, double t, int* whic
 // rec: [tau_start, t_1, ..., t_nrec] of the nominal run (record / replay);
 // a step that was clipped to output time o is stored as -(o + 1).
 struct Run {
-  double t0, t1, T1, prev_inv, prev_prev_inv;
-  int vy, vy1, steps, acc, rej, status;
+  double t0, t1, T1, lprev, lprev_prev;   // logs of the previous two inverse errors
+  int vy, vu, steps, acc, rej, status;   // vector ids of y0 and of the stage state / y1
   double* rec;
   int rec_cap, nrec;
   double scale;   // replay: tau_start / nominal tau_start
@@ -1171,8 +1208,8 @@ HD void mode_begin(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const D
     }
     if (ctl.record && gp.lead()) r.rec[0] = t0;
   }
-  r.prev_inv = 1.0; r.prev_prev_inv = 1.0;
-  r.vy = V_Y; r.vy1 = V_Y1; r.steps = 0; r.acc = 0; r.rej = 0; r.status = ST_OK;
+  r.lprev = 0.0; r.lprev_prev = 0.0;
+  r.vy = V_Y; r.vu = V_U; r.steps = 0; r.acc = 0; r.rej = 0; r.status = ST_OK;
 }
 
 // One attempted Rodas5 step (ode_integrators_stiff.py:718-834) plus the PID
@@ -1184,20 +1221,20 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
   if (r.steps >= ctl.max_steps) { r.status = ST_MAX_STEPS; return false; }
   const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
   const double t0 = r.t0, dt = r.t1 - r.t0;
-  const int vy = r.vy;
-  // f(t0, y0) and d f / d a in one forward-mode pass
+  const int vy = r.vy, vu = r.vu;
+  // f(t0, y0) into k1 and d f / d a in one forward-mode pass
   Bg<double> g;
-  rhs<Dual, G>(gp, c, m, D, T, t0, w, vy, V_F, V_JC0, &g);
-  const double d = 1.0 / (dt * R.gamma);
+  rhs<Dual, G>(gp, c, m, D, T, t0, w, vy, V_K0, V_JC0, &g);
+  const double d = rcp(dt * R.gamma);
   factor_W<G>(gp, c, m, D, T, w, d, t0, g);
   if (ctl.dense) dense_factor<G>(gp, m, D, T, w, d, t0, g);
   // d f / d tau: only the (l+1)/tau truncation terms
-  const double it2 = 1.0 / (t0 * t0);
+  const double it2 = rcp(t0 * t0);
   const double dTT = (lg + 1.0) * it2 * w.v(vy, 7 + lg);
   const double dTP = (lgp + 1.0) * it2 * w.v(vy, igp + lgp);
   const double dTR = (lr + 1.0) * it2 * w.v(vy, ir + lr);
   for (int i = gp.lane; i < nq; i += G) w.m(M_Q + Q_DT * nq + i) = (lnu + 1.0) * it2 * w.v(vy, iq0 + lnu * nq + i);
-  const double idt = 1.0 / dt;
+  const double idt = rcp(dt);
   for (int s = 0; s < 8; ++s) {
     const int vk = V_K0 + s;
     if (s > 0) {
@@ -1205,20 +1242,20 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
         for (int j = gp.lane; j < n; j += G) {
           double acc = w.v(vy, j);
           for (int q = 0; q < s; ++q) acc += R.a[s][q] * w.v(V_K0 + q, j);
-          w.v(V_U, j) = acc;
+          w.v(vu, j) = acc;
         }
       } else {
-        for (int j = gp.lane; j < n; j += G) w.v(V_U, j) += w.v(V_K0 + s - 1, j);
+        for (int j = gp.lane; j < n; j += G) w.v(vu, j) += w.v(V_K0 + s - 1, j);
       }
       gp.sync();
-      rhs<double, G>(gp, c, m, D, T, t0 + R.c[s] * dt, w, V_U, V_F, -1);
+      rhs<double, G>(gp, c, m, D, T, t0 + R.c[s] * dt, w, vu, vk, -1);
+      for (int j = gp.lane; j < n; j += G) {
+        double acc = w.v(vk, j);
+        for (int q = 0; q < s; ++q) acc += (R.C[s][q] * idt) * w.v(V_K0 + q, j);
+        w.v(vk, j) = acc;
+      }
+      gp.sync();
     }
-    for (int j = gp.lane; j < n; j += G) {
-      double acc = w.v(V_F, j);
-      for (int q = 0; q < s; ++q) acc += (R.C[s][q] * idt) * w.v(V_K0 + q, j);
-      w.v(vk, j) = acc;
-    }
-    gp.sync();
     if (s <= 4) {
       const double dd = dt * R.d[s];
       if (gp.lead()) {
@@ -1232,11 +1269,11 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
     if (ctl.dense) dense_solve<G>(gp, D, w, vk);
     else solve_W<G>(gp, m, D, w, g.aH, vk);
   }
-  // y1 = u + k8 ; error estimate k8
-  const int vy1 = r.vy1, vk8 = V_K0 + 7;
+  // y1 = u + k8 in place of u; error estimate k8
+  const int vy1 = vu, vk8 = V_K0 + 7;
   bool bad = false;
   for (int j = gp.lane; j < n; j += G) {
-    const double v = w.v(V_U, j) + w.v(vk8, j);
+    const double v = w.v(vu, j) + w.v(vk8, j);
     w.v(vy1, j) = v;
     bad = bad || !isfinite_(v);
   }
@@ -1249,23 +1286,26 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
     const int j = eidx[q];
     const double y0 = fabs(w.v(vy, j));
     const double y1 = bad ? y0 : fabs(w.v(vy1, j));
-    const double sc = w.v(vk8, j) / (ctl.atol + (y0 > y1 ? y0 : y1) * ctl.rtol) * ew[q];
+    const double sc = w.v(vk8, j) * rcp(ctl.atol + (y0 > y1 ? y0 : y1) * ctl.rtol) * ew[q];
     ss += sc * sc;
   }
   const double err = ctl.replay ? 0.0 : sqrt(ss / 6.0);
   ++r.steps;
   if (!isfinite_(err) || (ctl.replay && bad)) { r.status = ST_NONFINITE; return false; }
   const bool keep = ctl.replay ? true : err < 1.0;
-  double inv = 1.0 / err;
-  const double f1 = ctl.b1 == 0.0 ? 1.0 : pow(inv, ctl.b1);
-  const double f2 = ctl.b2 == 0.0 ? 1.0 : pow(r.prev_inv, ctl.b2);
-  const double f3 = ctl.b3 == 0.0 ? 1.0 : pow(r.prev_prev_inv, ctl.b3);
-  double factor = ctl.safety * f1 * f2 * f3;
+  // PID factor safety inv^b1 prev^b2 prevprev^b3, as one exp of a sum of
+  // logs (the logs of the previous inverse errors are kept)
+  const double linv = -log(err);
+  double lf = 0.0;
+  if (ctl.b1 != 0.0) lf += ctl.b1 * linv;
+  if (ctl.b2 != 0.0) lf += ctl.b2 * r.lprev;
+  if (ctl.b3 != 0.0) lf += ctl.b3 * r.lprev_prev;
+  double factor = ctl.safety * exp(lf);
   const double fmin = keep ? 1.0 : ctl.fmin;
   factor = factor < fmin ? fmin : factor;
   factor = factor > ctl.fmax ? ctl.fmax : factor;
   const double dtn = dt * factor;
-  if (inv == 0.0 || !isfinite_(inv)) inv = 1.0;
+  const double linv_kept = isfinite_(linv) ? linv : 0.0;
   if (keep) {
     ++r.acc;
     // SaveAt(ts) with LocalLinearInterpolation between (t0, y0) and (t1, y1)
@@ -1277,17 +1317,18 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
         if (ctl.return_full) {
           for (int j = gp.lane; j < n; j += G) { const double y0 = w.v(vy, j); dst[(long)j * ostride] = y0 + cf * (w.v(vy1, j) - y0); }
         } else {
-          for (int j = gp.lane; j < n; j += G) { const double y0 = w.v(vy, j); w.v(V_U, j) = y0 + cf * (w.v(vy1, j) - y0); }
+          // interpolated state in k1 (free once the step is complete)
+          for (int j = gp.lane; j < n; j += G) { const double y0 = w.v(vy, j); w.v(V_K0, j) = y0 + cf * (w.v(vy1, j) - y0); }
           gp.sync();
-          if (gp.lead()) outputs<G>(c, m, D, w, V_U, dst, ostride);
+          if (gp.lead()) outputs<G>(c, m, D, w, V_K0, dst, ostride);
         }
         gp.sync();
       }
     }
-    r.vy = vy1; r.vy1 = vy;
+    r.vy = vy1; r.vu = vy;
     r.t0 = r.t1;
-    r.prev_prev_inv = r.prev_inv;
-    r.prev_inv = inv;
+    r.lprev_prev = r.lprev;
+    r.lprev = linv_kept;
     if (ctl.record && gp.lead() && r.acc < r.rec_cap) r.rec[r.acc] = r.t1_out >= 0 ? -(r.t1_out + 1.0) : r.t1;
     if (ctl.replay) {
       // next recorded end time; the run ends at this table set's own final
@@ -1300,7 +1341,7 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
     }
   } else {
     ++r.rej;
-    if (ctl.hist_on_reject) { r.prev_prev_inv = r.prev_inv; r.prev_inv = inv; }
+    if (ctl.hist_on_reject) { r.lprev_prev = r.lprev; r.lprev = linv_kept; }
   }
   double tn = r.t0 + dtn;
   r.t1_out = -1;

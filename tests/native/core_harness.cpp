@@ -30,6 +30,7 @@ bool setup(Ctx& x, const double* blob, int blob_len, const int* dims, double k, 
   for (int i = 0; i < x.D.nq; ++i) {
     double q = x.c.q[i];
     x.w.m(M_Q + Q_DLF * x.D.nq + i) = -q / (1.0 + std::exp(-q));
+    x.w.m(M_Q + Q_AMQ * x.D.nq + i) = x.m.amnu / q;
   }
   return true;
 }
@@ -41,8 +42,8 @@ extern "C" {
 int h_rhs(const double* blob, int blob_len, const int* dims, double k, double tau, const double* y, double* f, double* jc0) {
   Ctx x; if (!setup(x, blob, blob_len, dims, k, false)) return -2;
   for (int j = 0; j < x.D.n; ++j) x.w.v(V_Y, j) = y[j];
-  rhs<Dual, 1>(GP, x.c, x.m, x.D, x.T, tau, x.w, V_Y, V_F, V_JC0);
-  for (int j = 0; j < x.D.n; ++j) { f[j] = x.w.v(V_F, j); jc0[j] = x.w.v(V_JC0, j); }
+  rhs<Dual, 1>(GP, x.c, x.m, x.D, x.T, tau, x.w, V_Y, (V_K0 + 1), V_JC0);
+  for (int j = 0; j < x.D.n; ++j) { f[j] = x.w.v((V_K0 + 1), j); jc0[j] = x.w.v(V_JC0, j); }
   rhs<double, 1>(GP, x.c, x.m, x.D, x.T, tau, x.w, V_Y, V_U, -1);
   for (int j = 0; j < x.D.n; ++j) if (x.w.v(V_U, j) != f[j] && !(f[j] != f[j])) return -10;
   return 0;
@@ -54,7 +55,7 @@ int h_solve_W(const double* blob, int blob_len, const int* dims, double k, doubl
   Ctx x; if (!setup(x, blob, blob_len, dims, k, dense != 0)) return -2;
   const int n = x.D.n;
   for (int j = 0; j < n; ++j) x.w.v(V_Y, j) = y[j];
-  rhs<Dual, 1>(GP, x.c, x.m, x.D, x.T, tau, x.w, V_Y, V_F, V_JC0);
+  rhs<Dual, 1>(GP, x.c, x.m, x.D, x.T, tau, x.w, V_Y, (V_K0 + 1), V_JC0);
   Bg<double> g; background<double>(x.c, x.m, y[0], g);
   const double d = 1.0 / (dt * x.R.gamma);
   factor_W<1>(GP, x.c, x.m, x.D, x.T, x.w, d, tau, g);
