@@ -232,11 +232,27 @@ enum { M_CORE = 0,          // 8x8 core LU (row-major)           64
        M_SCAL = 81,         // cached per-step scalars            32
        M_CINV8 = 113,       // explicit inverse of the 8x8 core    64
        M_Q = 177 };         // per-q arrays: v, dv/da, dlfdlq, ghq, geq, r1q, dTq, m_nu/q  (8 nq)
-enum { Q_V = 0, Q_DV, Q_DLF, Q_GH, Q_GE, Q_R1, Q_DT, Q_AMQ, NQARR };
-enum { S_D = 0, S_W00I, S_ID, S_IDAH, S_GH2, S_GH3, S_GH5, S_GH7, S_GHR0, S_GHQE, S_GE4, S_GE6, S_GE8,
-       S_GER1, S_GEQE, S_R13, S_R15, S_R17, S_R1R0, S_R1QE, S_R1QT, S_DTT, S_DTP, S_DTR,
+enum { Q_V = 0, Q_DV, Q_DLF, Q_DT, Q_AMQ, NQARR };
+// After the per-q arrays: three gather lists of nq + 6 coefficients each --
+// the metric functionals h' and eta' as rows (d h'/d y, d eta'/d y) and row 1
+// of J -- over the elements gather_index() names, so that each product is
+// one lane-parallel FMA plus one reduction.
+enum { GL_H = 0, GL_E, GL_R1, NGL };
+enum { S_D = 0, S_W00I, S_ID, S_IDAH,
        S_FT, S_FP };   // folds of the photon T / P tails into the core diagonal
-HD int misc_len(int nq) { return M_Q + NQARR * nq; }
+HD int misc_len(int nq) { return M_Q + NQARR * nq + NGL * (nq + 6); }
+HD int gl_off(int nq, int list) { return M_Q + NQARR * nq + list * (nq + 6); }
+
+// element of the state read by entry t of gather list `list` (t < nq + 6):
+// the massive-neutrino l = 0 (h', row 1) or l = 1 (eta') moments first, then
+// six (five for eta', plus one zero entry) fluid / metric elements
+HD int gather_index(const Dims& D, int list, int t) {
+  if (t < D.nq) return D.iq0 + (list == GL_E ? D.nq : 0) + t;
+  const int u = t - D.nq;
+  if (list == GL_H) return u == 0 ? 2 : u == 1 ? 3 : u == 2 ? 5 : u == 3 ? 7 : u == 4 ? D.ir : D.n - 2;
+  if (list == GL_E) return u == 0 ? 4 : u == 1 ? 6 : u == 2 ? 8 : u == 3 ? D.ir + 1 : D.n - 1;
+  return u == 0 ? 3 : u == 1 ? 5 : u == 2 ? 7 : u == 3 ? D.ir : u == 4 ? D.n - 2 : D.n - 1;
+}
 HD long slot_len(const Dims& D) { return (long)NV * D.n + misc_len(D.nq); }
 HD long hot_len(const Dims& D) { return (long)V_K0 * D.n + misc_len(D.nq); }     // vectors before k1 + MISC
 HD long stage_len(const Dims& D) { return (long)(NV - V_K0) * D.n; }             // k1..k8
@@ -328,6 +344,8 @@ struct ModeConst {
   double k, k2, ik, ik2;
   double Om, Ob, Oc, ODE, Ok, grhom, grhog, grhor, Neff, Nmnu, amnu, w0, wa, cs2Q, YHe, H0;
   double akthom, pQ, photbar0;
+  // products of the constants above that the RHS uses every call
+  double gOm, gOc, gOb, gODE, gOk, grN, grM, grr, grMk, g43g, g43N, pb43c;
 };
 
 HD void mode_const(const Cosmo& c, double k, ModeConst& m) {
@@ -339,6 +357,9 @@ HD void mode_const(const Cosmo& c, double k, ModeConst& m) {
   m.akthom = 2.3038921003709498e-9 * (1.0 - m.YHe) * m.Ob * m.H0 * m.H0;
   m.pQ = -3.0 * (1.0 + m.w0 + m.wa);
   m.photbar0 = m.grhog / (m.grhom * m.Ob);
+  m.gOm = m.grhom * m.Om; m.gOc = m.grhom * m.Oc; m.gOb = m.grhom * m.Ob; m.gODE = m.grhom * m.ODE; m.gOk = m.grhom * m.Ok;
+  m.grN = m.grhor * m.Neff; m.grM = m.grhor * m.Nmnu; m.grr = m.grhog + m.grN; m.grMk = m.grM * k;
+  m.g43g = (4.0 / 3.0) * m.grhog; m.g43N = (4.0 / 3.0) * m.grN; m.pb43c = (4.0 / 3.0) * m.photbar0;
 }
 
 template <class S>
@@ -347,8 +368,7 @@ HD void background_finish(const ModeConst& m, S a, Bg<S>& g, S cs2a, S xe, S rho
   g.xe = xe;
   g.rhonu = rhonu;
   g.rhoQ = rhoQ;
-  S grho = m.grhom * m.Om * g.ia + (m.grhog + m.grhor * (m.Neff + m.Nmnu * g.rhonu)) * g.ia2 +
-           m.grhom * m.ODE * g.rhoQ * g.a2 + m.grhom * m.Ok;
+  S grho = m.gOm * g.ia + (m.grr + m.grM * g.rhonu) * g.ia2 + m.gODE * g.rhoQ * g.a2 + m.gOk;
   const S g3 = grho * (1.0 / 3.0);
   g.iaH = drsqrt(g3);
   g.aH = g3 * g.iaH;
@@ -356,7 +376,7 @@ HD void background_finish(const ModeConst& m, S a, Bg<S>& g, S cs2a, S xe, S rho
   S wQp = -m.wa * g.aH * a;
   g.ca2 = g.wQ - wQp * (1.0 / 3.0) * drcp((1.0 + g.wQ) + 1e-6) * g.iaH;
   g.opac = g.xe * m.akthom * g.ia2;
-  g.pb43 = (4.0 / 3.0) * m.photbar0 * g.ia;
+  g.pb43 = m.pb43c * g.ia;
 }
 
 template <class S>
@@ -405,8 +425,9 @@ HD double aprimeoa(const Cosmo& c, const ModeConst& m, double a) {
 // ------------------------------------------------------------------ RHS
 // f = model_synchronous(tau, y) (perturbations.py:84-371).  With S = Dual the
 // a-dependence is differentiated: vout receives f, vjc receives d f / d a.
-// Ends with a group sync; expects vin to be complete (synced) on entry.
-template <class S, int G>
+// With kAcc, f is added to vout instead.  Ends with a group sync; expects
+// vin to be complete (synced) on entry.
+template <class S, int G, bool kAcc = false>
 HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, double tau, const WS<G>& w,
             int vin, int vout, int vjc, Bg<double>* gout = nullptr) {
   constexpr bool kDual = !std::is_same<S, double>::value;
@@ -424,7 +445,8 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
   }
   auto Y = [&](int j) -> double { return w.v(vin, j); };
   auto put = [&](int j, S f) {
-    w.v(vout, j) = val(f);
+    if constexpr (kAcc) w.v(vout, j) += val(f);
+    else w.v(vout, j) = val(f);
     if constexpr (kDual) w.v(vjc, j) = der(f);
   };
   // massive neutrino momentum sums (nu_perturb, perturbations.py:22-50)
@@ -449,16 +471,15 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
   const double eta = Y(2), dc = Y(3), tc = Y(4), db = Y(5), tb = Y(6), dg = Y(7), tg = Y(8), y9 = Y(9);
   const double dr = Y(ir), tr = Y(ir + 1), y_r2 = Y(ir + 2);
   const double dq = Y(n - 2), tq = Y(n - 1);
-  S rptQ = (1.0 + g.wQ) * g.rhoQ * m.grhom * m.ODE * tq * g.a2;
-  S dgrho = m.grhom * (m.Oc * dc + m.Ob * db) * g.ia + (m.grhog * dg + m.grhor * (m.Neff * dr + m.Nmnu * drhonu)) * g.ia2 +
-            m.grhom * m.ODE * dq * g.rhoQ * g.a2;
+  const S rQ = m.gODE * g.rhoQ * g.a2;   // grhom Omega_DE rho_Q(a) a^2
+  S rptQ = (1.0 + g.wQ) * rQ * tq;
+  S dgrho = (m.gOc * dc + m.gOb * db) * g.ia + (m.grhog * dg + m.grN * dr + m.grM * drhonu) * g.ia2 + rQ * dq;
   S hp = (2.0 * k2 * eta + dgrho) * g.iaH;
-  S dgtheta = m.grhom * (m.Oc * tc + m.Ob * tb) * g.ia + (4.0 / 3.0) * (m.grhog * tg + m.Neff * m.grhor * tr) * g.ia2 +
-              m.Nmnu * m.grhor * k * fnu * g.ia2 + rptQ;
+  S dgtheta = (m.gOc * tc + m.gOb * tb) * g.ia + (m.g43g * tg + m.g43N * tr + m.grMk * fnu) * g.ia2 + rptQ;
   S etap = 0.5 * dgtheta * m.ik2;
   if (gp.lead()) {
-    S dgpres = (m.grhog * dg + m.grhor * m.Neff * dr) * g.ia2 * (1.0 / 3.0) + m.grhor * m.Nmnu * dpnu * g.ia2 +
-               (m.cs2Q * m.grhom * m.ODE * dq * g.rhoQ * g.a2 + (m.cs2Q - g.ca2) * (3.0 * g.aH * rptQ * m.ik2));
+    S dgpres = ((m.grhog * dg + m.grN * dr) * (1.0 / 3.0) + m.grM * dpnu) * g.ia2 +
+               (m.cs2Q * rQ * dq + (m.cs2Q - g.ca2) * (3.0 * g.aH * rptQ * m.ik2));
     const S i1w = drcp(1.0 + g.wQ);
     S alpha = (hp + 6.0 * etap) * 0.5 * m.ik2;
     put(0, g.aH * g.a);
@@ -901,17 +922,11 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>
 // g_h . v and g_e . v (the metric functionals h', eta' as rows); all lanes get the sums
 template <int G>
 HD void functionals(const Grp<G>& gp, const Dims& D, const WS<G>& w, int vr, double& sh, double& se) {
-  const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
+  const int nq = D.nq, oh = gl_off(nq, GL_H), oe = gl_off(nq, GL_E);
   double h = 0.0, e = 0.0;
-  if (gp.lead()) {
-    h = w.m(M_SCAL + S_GH2) * w.v(vr, 2) + w.m(M_SCAL + S_GH3) * w.v(vr, 3) + w.m(M_SCAL + S_GH5) * w.v(vr, 5) +
-        w.m(M_SCAL + S_GH7) * w.v(vr, 7) + w.m(M_SCAL + S_GHR0) * w.v(vr, ir) + w.m(M_SCAL + S_GHQE) * w.v(vr, n - 2);
-    e = w.m(M_SCAL + S_GE4) * w.v(vr, 4) + w.m(M_SCAL + S_GE6) * w.v(vr, 6) + w.m(M_SCAL + S_GE8) * w.v(vr, 8) +
-        w.m(M_SCAL + S_GER1) * w.v(vr, ir + 1) + w.m(M_SCAL + S_GEQE) * w.v(vr, n - 1);
-  }
-  for (int i = gp.lane; i < nq; i += G) {
-    h += w.m(M_Q + Q_GH * nq + i) * w.v(vr, iq0 + i);
-    e += w.m(M_Q + Q_GE * nq + i) * w.v(vr, iq0 + nq + i);
+  for (int t = gp.lane; t < nq + 6; t += G) {
+    h += w.m(oh + t) * w.v(vr, gather_index(D, GL_H, t));
+    e += w.m(oe + t) * w.v(vr, gather_index(D, GL_E, t));
   }
   sh = gp.sum(h);
   se = gp.sum(e);
@@ -928,32 +943,36 @@ HD void factor_W(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dim
   if (gp.lead()) {
     w.m(M_SCAL + S_D) = d;
     w.m(M_SCAL + S_W00I) = 1.0 / (d - w.v(V_JC0, 0));
-    // functional coefficients (d h'/d y and d eta'/d y)
-    w.m(M_SCAL + S_GH2) = 2.0 * m.k2 * iaH;
-    w.m(M_SCAL + S_GH3) = m.grhom * m.Oc * g.ia * iaH;
-    w.m(M_SCAL + S_GH5) = m.grhom * m.Ob * g.ia * iaH;
-    w.m(M_SCAL + S_GH7) = m.grhog * g.ia2 * iaH;
-    w.m(M_SCAL + S_GHR0) = m.grhor * m.Neff * g.ia2 * iaH;
-    w.m(M_SCAL + S_GHQE) = m.grhom * m.ODE * g.rhoQ * g.a2 * iaH;
-    w.m(M_SCAL + S_GE4) = m.grhom * m.Oc * g.ia * h2;
-    w.m(M_SCAL + S_GE6) = m.grhom * m.Ob * g.ia * h2;
-    w.m(M_SCAL + S_GE8) = (4.0 / 3.0) * m.grhog * g.ia2 * h2;
-    w.m(M_SCAL + S_GER1) = (4.0 / 3.0) * m.Neff * m.grhor * g.ia2 * h2;
-    w.m(M_SCAL + S_GEQE) = (1.0 + g.wQ) * g.rhoQ * m.grhom * m.ODE * g.a2 * h2;
-    // row 1: J[1, j] = -a (d dgrho/d y_j + 3 d dgpres/d y_j)
-    w.m(M_SCAL + S_R13) = -m.grhom * m.Oc;
-    w.m(M_SCAL + S_R15) = -m.grhom * m.Ob;
-    w.m(M_SCAL + S_R17) = -2.0 * m.grhog * g.ia;
-    w.m(M_SCAL + S_R1R0) = -2.0 * m.grhor * m.Neff * g.ia;
-    w.m(M_SCAL + S_R1QE) = -m.grhom * m.ODE * g.rhoQ * g.a2 * a * (1.0 + 3.0 * m.cs2Q);
-    w.m(M_SCAL + S_R1QT) = -9.0 * (m.cs2Q - g.ca2) * g.aH * (1.0 + g.wQ) * g.rhoQ * m.grhom * m.ODE * g.a2 * a * m.ik2;
+    // functional coefficients (d h'/d y and d eta'/d y) and row 1,
+    // J[1, j] = -a (d dgrho/d y_j + 3 d dgpres/d y_j); entries nq.. of the lists
+    const int oh = gl_off(nq, GL_H) + nq, oe = gl_off(nq, GL_E) + nq, o1 = gl_off(nq, GL_R1) + nq;
+    const double rQ = m.gODE * g.rhoQ * g.a2;
+    w.m(oh + 0) = 2.0 * m.k2 * iaH;
+    w.m(oh + 1) = m.gOc * g.ia * iaH;
+    w.m(oh + 2) = m.gOb * g.ia * iaH;
+    w.m(oh + 3) = m.grhog * g.ia2 * iaH;
+    w.m(oh + 4) = m.grN * g.ia2 * iaH;
+    w.m(oh + 5) = rQ * iaH;
+    w.m(oe + 0) = m.gOc * g.ia * h2;
+    w.m(oe + 1) = m.gOb * g.ia * h2;
+    w.m(oe + 2) = m.g43g * g.ia2 * h2;
+    w.m(oe + 3) = m.g43N * g.ia2 * h2;
+    w.m(oe + 4) = (1.0 + g.wQ) * rQ * h2;
+    w.m(oe + 5) = 0.0;
+    w.m(o1 + 0) = -m.gOc;
+    w.m(o1 + 1) = -m.gOb;
+    w.m(o1 + 2) = -2.0 * m.grhog * g.ia;
+    w.m(o1 + 3) = -2.0 * m.grN * g.ia;
+    w.m(o1 + 4) = -rQ * a * (1.0 + 3.0 * m.cs2Q);
+    w.m(o1 + 5) = -9.0 * (m.cs2Q - g.ca2) * g.aH * (1.0 + g.wQ) * rQ * a * m.ik2;
   }
   for (int i = gp.lane; i < nq; i += G) {
     const double v = w.m(M_Q + Q_V * nq + i);
+    const double iv = rcp(v);
     const double wq = LDG(c.w + i);
-    w.m(M_Q + Q_GH * nq + i) = m.grhor * m.Nmnu * wq * rcp(v) * g.ia2 * iaH;
-    w.m(M_Q + Q_GE * nq + i) = m.Nmnu * m.grhor * m.k * wq * g.ia2 * h2;
-    w.m(M_Q + Q_R1 * nq + i) = -m.grhor * m.Nmnu * wq * (rcp(v) + v) * g.ia;
+    w.m(gl_off(nq, GL_H) + i) = m.grM * wq * iv * g.ia2 * iaH;
+    w.m(gl_off(nq, GL_E) + i) = m.grMk * wq * g.ia2 * h2;
+    w.m(gl_off(nq, GL_R1) + i) = -m.grM * wq * (iv + v) * g.ia;
   }
   for (int j = gp.lane; j < n; j += G) { w.v(V_ZH, j) = 0.0; w.v(V_ZE, j) = 0.0; }
   factor_M<G>(gp, m, D, T, w, d, tau, g);   // syncs
@@ -988,7 +1007,7 @@ HD void factor_W(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dim
 // x = W^{-1} b in place on vector vb.  Expects vb synced; ends synced.
 template <int G>
 HD void solve_W(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>& w, double aH, int vb) {
-  const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
+  const int n = D.n, nq = D.nq;
   const double d = w.m(M_SCAL + S_D);
   const double x0 = w.v(vb, 0) * w.m(M_SCAL + S_W00I);
   gp.sync();
@@ -1004,10 +1023,8 @@ HD void solve_W(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>
   for (int j = 2 + gp.lane; j < n; j += G) w.v(vb, j) += w.v(V_ZH, j) * th + w.v(V_ZE, j) * te;
   gp.sync();
   double s1 = 0.0;
-  if (gp.lead())
-    s1 = w.m(M_SCAL + S_R13) * w.v(vb, 3) + w.m(M_SCAL + S_R15) * w.v(vb, 5) + w.m(M_SCAL + S_R17) * w.v(vb, 7) +
-         w.m(M_SCAL + S_R1R0) * w.v(vb, ir) + w.m(M_SCAL + S_R1QE) * w.v(vb, n - 2) + w.m(M_SCAL + S_R1QT) * w.v(vb, n - 1);
-  for (int i = gp.lane; i < nq; i += G) s1 += w.m(M_Q + Q_R1 * nq + i) * w.v(vb, iq0 + i);
+  const int o1 = gl_off(nq, GL_R1);
+  for (int t = gp.lane; t < nq + 6; t += G) s1 += w.m(o1 + t) * w.v(vb, gather_index(D, GL_R1, t));
   s1 = gp.sum(s1);
   if (gp.lead()) w.v(vb, 1) = (w.v(vb, 1) + s1) * w.m(M_SCAL + S_ID);
   gp.sync();
@@ -1032,14 +1049,10 @@ HD void visit_u(const Dims& D, const WS<G>& w, double wQ, F f) {
 
 template <int G, class F>
 HD void visit_g(const Dims& D, const WS<G>& w, F f) {
-  const int n = D.n, nq = D.nq, iq0 = D.iq0, ir = D.ir;
-  f(2, w.m(M_SCAL + S_GH2), 0.0); f(3, w.m(M_SCAL + S_GH3), 0.0); f(5, w.m(M_SCAL + S_GH5), 0.0);
-  f(7, w.m(M_SCAL + S_GH7), 0.0); f(ir, w.m(M_SCAL + S_GHR0), 0.0); f(n - 2, w.m(M_SCAL + S_GHQE), 0.0);
-  f(4, 0.0, w.m(M_SCAL + S_GE4)); f(6, 0.0, w.m(M_SCAL + S_GE6)); f(8, 0.0, w.m(M_SCAL + S_GE8));
-  f(ir + 1, 0.0, w.m(M_SCAL + S_GER1)); f(n - 1, 0.0, w.m(M_SCAL + S_GEQE));
-  for (int i = 0; i < nq; ++i) {
-    f(iq0 + i, w.m(M_Q + Q_GH * nq + i), 0.0);
-    f(iq0 + nq + i, 0.0, w.m(M_Q + Q_GE * nq + i));
+  const int nq = D.nq;
+  for (int t = 0; t < nq + 6; ++t) {
+    f(gather_index(D, GL_H, t), w.m(gl_off(nq, GL_H) + t), 0.0);
+    f(gather_index(D, GL_E, t), 0.0, w.m(gl_off(nq, GL_E) + t));
   }
 }
 
@@ -1048,7 +1061,7 @@ HD void visit_g(const Dims& D, const WS<G>& w, F f) {
 template <int G>
 HD void dense_factor(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab& T, const WS<G>& w, double d, double tau,
                      const Bg<double>& g) {
-  const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir;
+  const int n = D.n, nq = D.nq, igp = D.igp;
   auto A = [&](int i, int j) -> double& { return w.e(i * n + j); };
   const double itau = 1.0 / tau, op = g.opac;
   for (int i = gp.lane; i < n; i += G) {
@@ -1083,9 +1096,7 @@ HD void dense_factor(const Grp<G>& gp, const ModeConst& m, const Dims& D, const 
     });
     for (int j = 1; j < n; ++j) A(1, j) = (j == 1) ? d : 0.0;
     A(1, 0) = -w.v(V_JC0, 1);
-    A(1, 3) = -w.m(M_SCAL + S_R13); A(1, 5) = -w.m(M_SCAL + S_R15); A(1, 7) = -w.m(M_SCAL + S_R17);
-    A(1, ir) = -w.m(M_SCAL + S_R1R0); A(1, n - 2) = -w.m(M_SCAL + S_R1QE); A(1, n - 1) = -w.m(M_SCAL + S_R1QT);
-    for (int i = 0; i < nq; ++i) A(1, iq0 + i) = -w.m(M_Q + Q_R1 * nq + i);
+    for (int t = 0; t < nq + 6; ++t) A(1, gather_index(D, GL_R1, t)) = -w.m(gl_off(nq, GL_R1) + t);
   }
   gp.sync();
   // LU with partial pivoting (first maximal |pivot|), rows over lanes
@@ -1212,6 +1223,35 @@ HD void mode_begin(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const D
   r.vy = V_Y; r.vu = V_U; r.steps = 0; r.acc = 0; r.rej = 0; r.status = ST_OK;
 }
 
+// Stage S >= 1 before its RHS: u = y0 + sum_q a_Sq k_q (S <= 5) or
+// u += k_{S-1} (S >= 6), and k_S = sum_q (C_Sq / dt) k_q, to which the RHS
+// then adds f(u).  One pass reads every earlier stage vector once.
+template <int G, int S>
+HD void stage_prep(const Grp<G>& gp, const Rodas& R, const WS<G>& w, int n, int vy, int vu, double idt) {
+  double a[S], cc[S];
+#pragma unroll
+  for (int q = 0; q < S; ++q) { a[q] = R.a[S][q]; cc[q] = R.C[S][q] * idt; }
+#pragma unroll 2
+  for (int j = gp.lane; j < n; j += G) {
+    double kq[S];
+#pragma unroll
+    for (int q = 0; q < S; ++q) kq[q] = w.v(V_K0 + q, j);
+    double p = cc[0] * kq[0];
+#pragma unroll
+    for (int q = 1; q < S; ++q) p += cc[q] * kq[q];
+    double u;
+    if constexpr (S <= 5) {
+      u = w.v(vy, j);
+#pragma unroll
+      for (int q = 0; q < S; ++q) u += a[q] * kq[q];
+    } else {
+      u = w.v(vu, j) + kq[S - 1];
+    }
+    w.v(vu, j) = u;
+    w.v(V_K0 + S, j) = p;
+  }
+}
+
 // One attempted Rodas5 step (ode_integrators_stiff.py:718-834) plus the PID
 // decision.  Returns true while the mode still needs steps.
 template <int G>
@@ -1238,23 +1278,17 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
   for (int s = 0; s < 8; ++s) {
     const int vk = V_K0 + s;
     if (s > 0) {
-      if (s <= 5) {
-        for (int j = gp.lane; j < n; j += G) {
-          double acc = w.v(vy, j);
-          for (int q = 0; q < s; ++q) acc += R.a[s][q] * w.v(V_K0 + q, j);
-          w.v(vu, j) = acc;
-        }
-      } else {
-        for (int j = gp.lane; j < n; j += G) w.v(vu, j) += w.v(V_K0 + s - 1, j);
+      switch (s) {
+        case 1: stage_prep<G, 1>(gp, R, w, n, vy, vu, idt); break;
+        case 2: stage_prep<G, 2>(gp, R, w, n, vy, vu, idt); break;
+        case 3: stage_prep<G, 3>(gp, R, w, n, vy, vu, idt); break;
+        case 4: stage_prep<G, 4>(gp, R, w, n, vy, vu, idt); break;
+        case 5: stage_prep<G, 5>(gp, R, w, n, vy, vu, idt); break;
+        case 6: stage_prep<G, 6>(gp, R, w, n, vy, vu, idt); break;
+        default: stage_prep<G, 7>(gp, R, w, n, vy, vu, idt); break;
       }
       gp.sync();
-      rhs<double, G>(gp, c, m, D, T, t0 + R.c[s] * dt, w, vu, vk, -1);
-      for (int j = gp.lane; j < n; j += G) {
-        double acc = w.v(vk, j);
-        for (int q = 0; q < s; ++q) acc += (R.C[s][q] * idt) * w.v(V_K0 + q, j);
-        w.v(vk, j) = acc;
-      }
-      gp.sync();
+      rhs<double, G, true>(gp, c, m, D, T, t0 + R.c[s] * dt, w, vu, vk, -1);   // ends synced
     }
     if (s <= 4) {
       const double dd = dt * R.d[s];
