@@ -44,6 +44,8 @@ WORKLOADS = {
     "batched_64cosmo_512k_n323_rtol1e-5": (64, 512, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
     "batched_8cosmo_512k_n323_rtol1e-5": (8, 512, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
     "single_1cosmo_256k_n323_rtol1e-5": (1, 256, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
+    # profiling case: enough modes to fill every SM's slots, short enough for a counter capture
+    "batched_2cosmo_512k_n323_rtol1e-5": (2, 512, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
 }
 DEFAULT_WORKLOAD = "batched_8cosmo_512k_n323_rtol1e-5_grad"
 

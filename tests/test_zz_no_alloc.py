@@ -71,7 +71,8 @@ def test_static_entry_point_rejects_state_beyond_the_array():
     from discoeb_gb300 import perturbations as pt
 
     L = _native.load()
-    dims = pt._dims(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=100, nqmax=1200, nout=1, return_full=False,
+    # nvar = 202 053: 16 vectors of it alone are 25.9 MB > 16 MiB
+    dims = pt._dims(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=100, nqmax=2000, nout=1, return_full=False,
                     linear_solver="structured")
     cfg = pt._cfg(1e-3, 1e-6, 0.25, 0.80, 0.0, 20.0, 0.3, 2048)
     rc = L.deb_forward_static(ctypes.byref(dims), None, 1, 1000, None, None, 1, None, ctypes.byref(cfg), None, None,
