@@ -31,7 +31,8 @@ class DebSolverCfg(ctypes.Structure):
 
 
 _lib = None
-EXPORTS = ("deb_nvar", "deb_plan_create", "deb_plan_workspace_bytes", "deb_forward", "deb_forward_static",
+EXPORTS = ("deb_nvar", "deb_plan_create", "deb_plan_workspace_bytes", "deb_plan_set_order", "deb_forward",
+           "deb_forward_static",
            "deb_forward_record", "deb_replay", "deb_get_power",
            "deb_plan_destroy", "deb_measure_fp64_peak", "deb_error_string", "deb_version")
 
@@ -50,6 +51,7 @@ def load(path: str | None = None):
     L.deb_nvar.argtypes = [ctypes.POINTER(DebDims)]
     L.deb_plan_create.argtypes = [ctypes.POINTER(DebDims), ctypes.c_int, ctypes.POINTER(vp)]
     L.deb_plan_workspace_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
+    L.deb_plan_set_order.argtypes = [vp, vp, ctypes.c_int]
     L.deb_forward.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp,
                               ctypes.POINTER(DebSolverCfg), vp, vp, vp, vp]
     L.deb_forward_static.argtypes = [ctypes.POINTER(DebDims), vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp,

@@ -51,19 +51,31 @@ struct KParams {
   double* rec;        // [nmode, rec_len]
   int rec_len;
   int* nrec;          // [nmode]
-  int nset;           // replay: table sets per cosmology; work item = set * nmode + mode
+  int nset;           // replay: table sets per cosmology; output item = set * nmode + mode
+  // queue order: queue position q takes mode order[q] (forward) or mode
+  // order[q / nset], set q % nset (replay); null = index order
+  const int* order;
   deb::Ctl ctl;
   deb::Dims D;
 };
 
-// Validate work item w and load its cosmology; fills NaN outputs and the
-// run's record pointers.  Same on every lane.  Work item = mode, or in a
-// replay set * nmode + mode.
-__device__ bool prepare_mode(const KParams& P, int w, deb::Cosmo& c, deb::ModeConst& mc, const double*& tau_out,
-                             double*& yout, deb::Run& run, int lane, int G) {
+// Map queue position q to (mode m, table set, output item oi = set * nmode
+// + m), validate it and load its cosmology; fills NaN outputs and the run's
+// record pointers.  Same on every lane.  Returns false for an item to skip.
+__device__ bool prepare_mode(const KParams& P, int q, deb::Cosmo& c, deb::ModeConst& mc, const double*& tau_out,
+                             double*& yout, deb::Run& run, int& oi, int lane, int G) {
   const int osz = P.ctl.return_full ? P.D.n : DEB_NOUT_FIELDS;
-  const int m = P.ctl.replay ? w % P.nmode : w;
-  const int set = P.ctl.replay ? w / P.nmode : 0;
+  int m, set;
+  if (P.ctl.replay) {
+    if (P.order) { const int j = q / P.nset; set = q - j * P.nset; m = P.order[j]; }
+    else { m = q % P.nmode; set = q / P.nmode; }
+  } else {
+    set = 0;
+    m = P.order ? P.order[q] : q;
+  }
+  if (m < 0 || m >= P.nmode) return false;   // not a permutation: nothing to do for this position
+  const int w = set * P.nmode + m;
+  oi = w;
   const int ci = P.cosmo ? P.cosmo[m] : 0;
   const double k = P.k[m];
   double* dst = P.y_out + (long)w * P.ctl.nout * osz;
@@ -101,7 +113,7 @@ __global__ void __launch_bounds__(kBlock) forward_lane_kernel(KParams P) {
   w.kp = w.p + (long)deb::hot_len(P.D) * 32;
   w.dp = P.dws ? P.dws + warp * 32 * P.dense_len + lane : nullptr;
   const deb::Grp<1> gp{0};
-  int mode = -1;
+  int mode = -1;   // output item of the current mode
   deb::Cosmo c;
   deb::ModeConst mc;
   deb::Run run;
@@ -109,10 +121,9 @@ __global__ void __launch_bounds__(kBlock) forward_lane_kernel(KParams P) {
   double* yout = nullptr;
   auto fetch = [&]() -> bool {
     for (;;) {
-      const int m = atomicAdd(P.queue, 1);
-      if (m >= P.nmode * P.nset) return false;
-      mode = m;
-      if (!prepare_mode(P, m, c, mc, tau_out, yout, run, 0, 1)) continue;
+      const int q = atomicAdd(P.queue, 1);
+      if (q >= P.nmode * P.nset) return false;
+      if (!prepare_mode(P, q, c, mc, tau_out, yout, run, mode, 0, 1)) continue;
       deb::mode_begin<1>(gp, c, mc, P.D, P.ctl, w, tau_out, run);
       return true;
     }
@@ -124,7 +135,7 @@ __global__ void __launch_bounds__(kBlock) forward_lane_kernel(KParams P) {
       if (!more) {
         P.status[mode] = run.status;
         if (P.steps) { P.steps[2 * mode] = run.acc; P.steps[2 * mode + 1] = run.rej; }
-        if (P.ctl.record && P.nrec) P.nrec[mode] = run.status == deb::ST_OK ? run.acc : 0;
+        if (P.ctl.record && P.nrec) P.nrec[mode] = run.status == deb::ST_OK ? run.acc : 0;   // record: set 0, item = mode
         active = fetch();
       }
     }
@@ -150,11 +161,11 @@ __global__ void __launch_bounds__(32) forward_warp_kernel(KParams P) {
   const double* tau_out = nullptr;
   double* yout = nullptr;
   for (;;) {
-    int m = 0;
-    if (lane == 0) m = atomicAdd(P.queue, 1);
-    m = __shfl_sync(0xffffffffu, m, 0);
-    if (m >= P.nmode * P.nset) break;
-    if (!prepare_mode(P, m, c, mc, tau_out, yout, run, lane, 32)) continue;
+    int q = 0, m = 0;
+    if (lane == 0) q = atomicAdd(P.queue, 1);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    if (q >= P.nmode * P.nset) break;
+    if (!prepare_mode(P, q, c, mc, tau_out, yout, run, m, lane, 32)) continue;
     deb::mode_begin<32>(gp, c, mc, P.D, P.ctl, w, tau_out, run);
     while (deb::mode_step<32>(gp, c, mc, P.D, c_tab, c_rodas, P.ctl, w, tau_out, yout, 1, run)) {}
     if (lane == 0) {
@@ -179,6 +190,29 @@ __global__ void power_kernel(const double* tables, int ncosmo, int blob_len, con
   const double v = y[t * stride + idx];
   // get_power, perturbations.py:1123
   P[t] = 2.0 * M_PI * M_PI * As * pow(km / kp, ns - 1.0) * pow(km, -3.0) * v * v;
+}
+
+// order[rank(i)] = i with modes ranked by key descending, ties by index:
+// the replay hands the modes with the most recorded steps out first, so the
+// launch does not end on a long mode started last.  O(n^2) compares through
+// shared-memory tiles; n is a few ten thousand at most.
+__global__ void rank_desc_kernel(const int* key, int n, int* order) {
+  __shared__ int tile[256];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ki = i < n ? key[i] : 0;
+  int r = 0;
+  for (int base = 0; base < n; base += blockDim.x) {
+    const int j = base + (int)threadIdx.x;
+    tile[threadIdx.x] = j < n ? key[j] : 0;
+    __syncthreads();
+    const int lim = n - base < (int)blockDim.x ? n - base : (int)blockDim.x;
+    for (int t = 0; t < lim; ++t) {
+      const int kj = tile[t];
+      r += (kj > ki) || (kj == ki && base + t < i);
+    }
+    __syncthreads();
+  }
+  if (i < n) order[r] = i;
 }
 
 // Independent FMA chains: 8 per thread, long enough to be issue-bound.
@@ -224,6 +258,9 @@ struct deb_plan {
   double* ws;       // lane slots (or warp slots when shared memory is too small)
   double* dws;      // dense matrices
   int* queue;
+  int* order_dev;   // replay order (max_modes ints)
+  const int* user_order;   // deb_plan_set_order
+  int user_order_n;
   size_t ws_bytes;
 };
 
@@ -341,7 +378,12 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
   if (p->dense && cudaMalloc(&p->dws, (size_t)nslots * p->dense_len * sizeof(double)) != cudaSuccess) {
     cudaFree(p->ws); delete p; return DEB_ERR_NOMEM;
   }
-  if (cudaMalloc(&p->queue, sizeof(int) * 4) != cudaSuccess) { cudaFree(p->ws); cudaFree(p->dws); delete p; return DEB_ERR_NOMEM; }
+  if (cudaMalloc(&p->queue, sizeof(int) * 4) != cudaSuccess) { cudaFree(p->ws); cudaFree(p->dws); cudaFree(p->kws); delete p; return DEB_ERR_NOMEM; }
+  if (cudaMalloc(&p->order_dev, sizeof(int) * (size_t)max_modes) != cudaSuccess) {
+    cudaFree(p->ws); cudaFree(p->dws); cudaFree(p->kws); cudaFree(p->queue); delete p; return DEB_ERR_NOMEM;
+  }
+  p->user_order = nullptr;
+  p->user_order_n = 0;
   *out = p;
   return DEB_OK;
 }
@@ -358,7 +400,15 @@ void deb_plan_destroy(deb_plan* p) {
   cudaFree(p->dws);
   cudaFree(p->kws);
   cudaFree(p->queue);
+  cudaFree(p->order_dev);
   delete p;
+}
+
+int deb_plan_set_order(deb_plan* p, const int* d_order, int nmode) {
+  if (!p || (d_order && nmode <= 0)) return DEB_ERR_INVALID;
+  p->user_order = d_order;
+  p->user_order_n = d_order ? nmode : 0;
+  return DEB_OK;
 }
 
 }  // extern "C"
@@ -378,13 +428,14 @@ int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, in
   if (record && rec_len < cfg->max_steps + 1) return DEB_ERR_INVALID;
   if (replay && p->exec_mode != DEB_EXEC_WARP) return DEB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  KParams P;
+  KParams P{};
   P.tables = d_tables; P.ncosmo = ncosmo; P.blob_len = blob_len; P.k = d_k; P.cosmo = d_cosmo_of_mode;
   P.nmode = nmode; P.tau_out = d_tau_out; P.y_out = d_y_out; P.status = d_status; P.steps = d_steps;
   P.ws = p->ws; P.dws = p->dws; P.slot_len = p->slot_len; P.dense_len = p->dense_len; P.queue = p->queue; P.D = p->D;
   P.smem = p->warp_smem;
   P.kws = p->kws;
   P.rec = d_record; P.rec_len = rec_len; P.nrec = d_nrec; P.nset = nset;
+  P.order = (!replay && p->user_order && p->user_order_n == nmode) ? p->user_order : nullptr;
   P.ctl.rtol = cfg->rtol; P.ctl.atol = cfg->atol;
   P.ctl.b1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / cfg->error_order;
   P.ctl.b2 = -(cfg->pcoeff + 2.0 * cfg->dcoeff) / cfg->error_order;
@@ -394,6 +445,10 @@ int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, in
   P.ctl.dense = p->dense; P.ctl.return_full = p->return_full; P.ctl.nout = p->nout;
   P.ctl.record = record; P.ctl.replay = replay; P.ctl.step_ts = cfg->step_to_outputs;
   if (cudaMemsetAsync(p->queue, 0, sizeof(int), s) != cudaSuccess) return DEB_ERR_CUDA;
+  if (replay) {
+    rank_desc_kernel<<<(nmode + 255) / 256, 256, 0, s>>>(d_nrec, nmode, p->order_dev);
+    P.order = p->order_dev;
+  }
   const long items = (long)nmode * nset;
   if (p->exec_mode == DEB_EXEC_LANE) {
     long need = (items + kBlock - 1) / kBlock;
@@ -484,7 +539,7 @@ int deb_forward_static(const deb_dims* dims, const double* d_tables, int ncosmo,
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return DEB_ERR_CUDA;
   double* base = g_static_scratch_addr[dev];
   cudaStream_t s = (cudaStream_t)stream;
-  KParams P;
+  KParams P{};
   P.tables = d_tables; P.ncosmo = ncosmo; P.blob_len = blob_len; P.k = d_k; P.cosmo = d_cosmo_of_mode;
   P.nmode = nmode; P.tau_out = d_tau_out; P.y_out = d_y_out; P.status = d_status; P.steps = d_steps;
   P.ws = base + 256 / sizeof(double); P.dws = nullptr; P.slot_len = slot_len; P.dense_len = 0;

@@ -133,6 +133,7 @@ class GradientProblem:
         self.plan = _pt.get_plan(dims, ns * nm)
         self.cfg = _pt._cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps,
                             step_to_outputs=step_to_outputs)
+        self.order = T(_pt.schedule_order(self.host_k), torch.int32)
 
     def run(self, stream=None, events=None):
         import torch
@@ -143,10 +144,10 @@ class GradientProblem:
         sp = ctypes.c_void_p(s.cuda_stream)
         if events:
             events[0].record(s)
-        _native.check(L.deb_forward_record(self.plan.ptr, c(self.d_tab0), self.nc, self.host_tab0.shape[1], c(self.d_k),
-                                           c(self.d_com), self.nmode, c(self.d_tau0), ctypes.byref(self.cfg),
-                                           c(self.d_y0), c(self.d_st0), c(self.d_steps), c(self.d_rec), self.rec_len,
-                                           c(self.d_nrec), sp), "deb_forward_record")
+        _native.check(_pt.launch_ordered(self.plan, self.order, self.nmode, lambda: L.deb_forward_record(
+            self.plan.ptr, c(self.d_tab0), self.nc, self.host_tab0.shape[1], c(self.d_k), c(self.d_com), self.nmode,
+            c(self.d_tau0), ctypes.byref(self.cfg), c(self.d_y0), c(self.d_st0), c(self.d_steps), c(self.d_rec),
+            self.rec_len, c(self.d_nrec), sp)), "deb_forward_record")
         if events:
             events[1].record(s)
         _native.check(L.deb_replay(self.plan.ptr, c(self.d_tabs), self.nc, self.nset, self.host_tabs.shape[1],

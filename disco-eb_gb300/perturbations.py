@@ -52,6 +52,35 @@ def _cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps, sa
                                 int(max_steps), 1 if hist_on_reject else 0, 1 if step_to_outputs else 0)
 
 
+# Attempted steps per mode peak near k = 0.15 / Mpc (tens of steps at
+# k = 1e-4, ~1500 at the peak, a few hundred at k = 1-10 for the
+# fiducial-like cosmologies); the first launch of a problem hands modes out
+# in order of distance from that peak.
+K_STEP_PEAK = 0.15
+
+
+def schedule_order(kmodes: np.ndarray, cost=None) -> np.ndarray:
+    """Queue order (a permutation), most expensive modes first: by measured
+    cost (e.g. attempted steps of an earlier launch) when given, else by
+    |ln(k / K_STEP_PEAK)|."""
+    if cost is not None:
+        return np.argsort(-np.asarray(cost, dtype=np.float64), kind="stable").astype(np.int32)
+    return np.argsort(np.abs(np.log(np.asarray(kmodes, dtype=np.float64) / K_STEP_PEAK)), kind="stable").astype(np.int32)
+
+
+def launch_ordered(plan, order, nmode: int, fn):
+    """Run fn() (one launch on plan) with queue order ``order`` (device int32
+    tensor or None) set for that launch only."""
+    L = _native.load()
+    if order is not None:
+        _native.check(L.deb_plan_set_order(plan.ptr, ctypes.c_void_p(order.data_ptr()), int(nmode)), "deb_plan_set_order")
+    try:
+        return fn()
+    finally:
+        if order is not None:
+            L.deb_plan_set_order(plan.ptr, None, 0)
+
+
 def get_plan(dims: _native.DebDims, nmode: int) -> _native.Plan:
     """Cached plan for these hierarchy sizes with room for >= nmode modes."""
     torch = _torch()
@@ -100,17 +129,27 @@ class DeviceProblem:
         self.steps = torch.empty((self.nmode, 2), dtype=torch.int32, device=dev)
         self.plan = get_plan(self.dims, self.nmode)
         self.device = dev
+        host_k = self.k.cpu().numpy() if self.nmode else np.zeros(0)
+        self.order = torch.as_tensor(schedule_order(host_k)).to(dev) if self.nmode else None
+
+    def reorder_by_steps(self):
+        """Hand modes out longest-first by the attempted steps of the last
+        launch (synchronises; results do not depend on the order)."""
+        torch = _torch()
+        torch.cuda.synchronize()
+        st = self.steps.cpu().numpy()
+        self.order = torch.as_tensor(schedule_order(None, st[:, 0] + st[:, 1])).to(self.device)
+        torch.cuda.synchronize()
 
     def launch(self, cfg: _native.DebSolverCfg, stream=None):
         torch = _torch()
         s = stream if stream is not None else torch.cuda.current_stream()
         L = _native.load()
-        rc = L.deb_forward(self.plan.ptr, ctypes.c_void_p(self.tables.data_ptr()), self.ncosmo, self.blob_len,
-                           ctypes.c_void_p(self.k.data_ptr()),
-                           ctypes.c_void_p(self.cosmo.data_ptr() if self.cosmo is not None else 0), self.nmode,
-                           ctypes.c_void_p(self.tau_out.data_ptr()), ctypes.byref(cfg),
-                           ctypes.c_void_p(self.y.data_ptr()), ctypes.c_void_p(self.status.data_ptr()),
-                           ctypes.c_void_p(self.steps.data_ptr()), ctypes.c_void_p(s.cuda_stream))
+        rc = launch_ordered(self.plan, self.order, self.nmode, lambda: L.deb_forward(
+            self.plan.ptr, ctypes.c_void_p(self.tables.data_ptr()), self.ncosmo, self.blob_len,
+            ctypes.c_void_p(self.k.data_ptr()), ctypes.c_void_p(self.cosmo.data_ptr() if self.cosmo is not None else 0),
+            self.nmode, ctypes.c_void_p(self.tau_out.data_ptr()), ctypes.byref(cfg), ctypes.c_void_p(self.y.data_ptr()),
+            ctypes.c_void_p(self.status.data_ptr()), ctypes.c_void_p(self.steps.data_ptr()), ctypes.c_void_p(s.cuda_stream)))
         _native.check(rc, "deb_forward")
 
     def power(self, idx: int, stream=None):

@@ -114,6 +114,20 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** plan);
 int deb_plan_workspace_bytes(const deb_plan* plan, size_t* bytes);
 
 /*
+ * Scheduling hint, no reference counterpart.  The kernel hands modes to its
+ * warps through a device-side queue; a launch ends when its last mode ends,
+ * and step counts differ by 60x across k, so handing out the most expensive
+ * modes first shortens the tail.  d_order [nmode] (device) must be a
+ * permutation of 0 .. nmode-1: queue position q takes mode d_order[q].
+ * Results do not depend on it.  The plan keeps the pointer (the array must
+ * stay valid until every launch that reads it has finished) and applies it
+ * to deb_forward / deb_forward_record launches with this nmode; NULL
+ * restores index order.  deb_replay always orders its work by the recorded
+ * step counts, most steps first.
+ */
+int deb_plan_set_order(deb_plan* plan, const int* d_order, int nmode);
+
+/*
  * Integrate nmode k-modes (perturbations.py:980-987 for one cosmology; here
  * any number of cosmologies share one launch).
  *   d_tables        [ncosmo, blob_len] FP64 table blobs

@@ -206,3 +206,44 @@ def test_step_to_outputs_interior_outputs_vs_oracle(fid):
     yo, so = oracle.solve(blob, k, tau, rtol=1e-5, atol=1e-5, max_steps=20000, step_to_outputs=True, **FID)
     assert (so[:, 0] == 0).all()
     np.testing.assert_allclose(y[:, :, 4] ** 2, yo[:, :, 4] ** 2, rtol=1e-4)
+
+
+def test_queue_order_does_not_change_results(fid):
+    """Any permutation handed to deb_plan_set_order gives bit-identical outputs,
+    status and step counts (only which warp takes which mode changes)."""
+    import torch
+    from discoeb_gb300 import perturbations as pt
+
+    k = np.geomspace(1e-4, 10.0, 40)
+    blob = tb.pack_cosmology(fid, 15)
+    tau = tb.tau_of_a(fid, [0.5, 1.0])
+    prob = deb.DeviceProblem(blob[None], k, tau[None], **FID)
+    cfg = pt._cfg(1e-5, 1e-5, 0.25, 0.80, 0.0, 20.0, 0.3, 20000)
+    runs = []
+    for order in (None, np.random.default_rng(3).permutation(40).astype(np.int32), np.arange(40)[::-1].copy()):
+        prob.order = None if order is None else torch.as_tensor(order).cuda()
+        prob.launch(cfg)
+        torch.cuda.synchronize()
+        runs.append((prob.y.cpu().numpy().copy(), prob.status.cpu().numpy().copy(), prob.steps.cpu().numpy().copy()))
+    for y, st, sp in runs[1:]:
+        assert np.array_equal(y, runs[0][0]) and np.array_equal(st, runs[0][1]) and np.array_equal(sp, runs[0][2])
+    prob.reorder_by_steps()
+    prob.launch(cfg)
+    torch.cuda.synchronize()
+    assert np.array_equal(prob.y.cpu().numpy(), runs[0][0])
+
+
+def test_more_chains_and_gather_entries_than_lanes():
+    """nqmax 30: 33 chains and 36-entry gather lists exceed the 32 lanes of a
+    warp, so every lane-strided loop over them takes two passes; small lmax
+    keeps the oracle's dense LU quick (nvar 246).  Six modes at rtol 1e-6."""
+    p = bg.evolve_background(param=fiducial_mnu_param())
+    dims = dict(lmaxg=8, lmaxgp=8, lmaxr=8, lmaxnu=6, nqmax=30)
+    k = np.geomspace(1e-3, 1.0, 6)
+    blob = tb.pack_cosmology(p, 30)
+    tau = tb.tau_of_a(p, [1.0])
+    y, st = deb.solve(blob[None], k, tau[None], rtol=1e-6, atol=1e-6, return_stats=True, max_steps=20000, **dims)
+    yo, so = oracle.solve(blob, k, tau, rtol=1e-6, atol=1e-6, max_steps=20000, **dims)
+    assert (st["status"] == 0).all() and (so[:, 0] == 0).all()
+    np.testing.assert_allclose(y[:, 0, 4], yo[:, 0, 4], rtol=1e-5)
+    np.testing.assert_allclose(y[:, 0, 8], yo[:, 0, 8], rtol=1e-5, atol=1e-9 * np.abs(yo[:, 0, 8]).max())
