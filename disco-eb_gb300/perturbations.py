@@ -65,7 +65,11 @@ def schedule_order(kmodes: np.ndarray, cost=None) -> np.ndarray:
     |ln(k / K_STEP_PEAK)|."""
     if cost is not None:
         return np.argsort(-np.asarray(cost, dtype=np.float64), kind="stable").astype(np.int32)
-    return np.argsort(np.abs(np.log(np.asarray(kmodes, dtype=np.float64) / K_STEP_PEAK)), kind="stable").astype(np.int32)
+    k = np.asarray(kmodes, dtype=np.float64)
+    ok = np.isfinite(k) & (k > 0)
+    key = np.full(k.shape, np.inf)          # invalid k (rejected by the kernel) last
+    key[ok] = np.abs(np.log(k[ok] / K_STEP_PEAK))
+    return np.argsort(key, kind="stable").astype(np.int32)
 
 
 def launch_ordered(plan, order, nmode: int, fn):

@@ -16,3 +16,12 @@ def test_cost_order_is_longest_first_and_stable():
     cost = np.array([5, 900, 5, 40, 900, 1])
     o = schedule_order(None, cost)
     assert o.tolist() == [1, 4, 3, 0, 2, 5]
+
+
+def test_invalid_k_goes_last_without_warnings():
+    import warnings
+
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        o = schedule_order(np.array([0.1, -1.0, np.nan, 1.0, 0.0]))
+    assert o.tolist()[:2] == [0, 3] and sorted(o.tolist()[2:]) == [1, 2, 4]
