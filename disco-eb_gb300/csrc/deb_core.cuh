@@ -229,9 +229,9 @@ enum { M_CORE = 0,          // 8x8 core LU (row-major)           64
        M_CPIV = 64,         // core pivots                         8
        M_DE = 72,           // DE 2x2 LU + pivot flag              5
        M_CINV = 77,         // Woodbury capacitance inverse        4
-       M_SCAL = 81,         // cached per-step scalars            32
-       M_CINV8 = 113,       // explicit inverse of the 8x8 core    64
-       M_Q = 177 };         // per-q arrays: v, dv/da, dlfdlq, ghq, geq, r1q, dTq, m_nu/q  (8 nq)
+       M_SCAL = 81,         // cached per-step scalars            56
+       M_CINV8 = 137,       // explicit inverse of the 8x8 core    64
+       M_Q = 201 };         // per-q arrays: v, dv/da, dlfdlq, ghq, geq, r1q, dTq, m_nu/q  (8 nq)
 enum { Q_V = 0, Q_DV, Q_DLF, Q_DT, Q_AMQ, NQARR };
 // After the per-q arrays: three gather lists of nq + 6 coefficients each --
 // the metric functionals h' and eta' as rows (d h'/d y, d eta'/d y) and row 1
@@ -239,7 +239,9 @@ enum { Q_V = 0, Q_DV, Q_DLF, Q_DT, Q_AMQ, NQARR };
 // one lane-parallel FMA plus one reduction.
 enum { GL_H = 0, GL_E, GL_R1, NGL };
 enum { S_D = 0, S_W00I, S_ID, S_IDAH,
-       S_FT, S_FP };   // folds of the photon T / P tails into the core diagonal
+       S_FT, S_FP,     // folds of the photon T / P tails into the core diagonal
+       S_LEAD = 8,     // RHS lead rows: per-call scalars sigma[17], derived values [5] (22)
+       S_LEADD = 32 }; // and their d / d a (forward-mode RHS)                          (22)
 HD int misc_len(int nq) { return M_Q + NQARR * nq + NGL * (nq + 6); }
 HD int gl_off(int nq, int list) { return M_Q + NQARR * nq + list * (nq + 6); }
 
@@ -422,6 +424,123 @@ HD double aprimeoa(const Cosmo& c, const ModeConst& m, double a) {
   return sqrt(grho / 3.0);
 }
 
+// ------------------------------------------------------------------ RHS lead rows
+// The 21 RHS entries outside the hierarchy loops (metric, CDM, baryons,
+// photon l = 0..2 and truncations, massless nu l = 0..2 and truncation, DE
+// fluid), each written as a sum of at most six terms kappa * sigma * x:
+// kappa a number, sigma one of the per-call scalars below, x a state element
+// or a derived value.  One lane evaluates one row, so the whole block costs
+// six multiply-adds per lane instead of ~130 scalar operations on one lane.
+enum { SG_ONE = 0, SG_K, SG_K2, SG_OP, SG_AH, SG_A, SG_AHA, SG_KCS, SG_PBO, SG_ITG, SG_ITP, SG_ITR, SG_W1, SG_DE1,
+       SG_DE2, SG_DE3, SG_DE4, NSIG };
+enum { DV_HP = 0, DV_ETAP, DV_ALPHA, DV_P1, DV_ONE, NDV };
+// index bases: absolute, igp, ir, n, 7 + lg, igp + lgp, ir + lr, derived value
+enum { IB_ABS = 0, IB_IGP, IB_IR, IB_N, IB_LG7, IB_IGPL, IB_IRL, IB_DV };
+struct LeadTerm { double kap; int base, off, sig; };
+constexpr int NLEAD = 21, NLT = 6;
+#define DEB_LEAD_ROWS {                                                                                               \
+  /* a' = aH a */                                                                                                    \
+  {{1.0, IB_DV, DV_ONE, SG_AHA}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE},   \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* (a h')' = -(dgrho + 3 dgpres) a */                                                                              \
+  {{-1.0, IB_DV, DV_P1, SG_A}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE},    \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* eta' */                                                                                                         \
+  {{1.0, IB_DV, DV_ETAP, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}, \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* delta_c' = -theta_c - h'/2 */                                                                                   \
+  {{-1.0, IB_ABS, 4, SG_ONE}, {-0.5, IB_DV, DV_HP, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE},  \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* theta_c' = -aH theta_c */                                                                                       \
+  {{-1.0, IB_ABS, 4, SG_AH}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE},      \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* delta_b' = -theta_b - h'/2 */                                                                                   \
+  {{-1.0, IB_ABS, 6, SG_ONE}, {-0.5, IB_DV, DV_HP, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE},  \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* theta_b' = -aH theta_b + k^2 cs2 delta_b + R opac (theta_g - theta_b) */                                        \
+  {{-1.0, IB_ABS, 6, SG_AH}, {1.0, IB_ABS, 5, SG_KCS}, {1.0, IB_ABS, 8, SG_PBO}, {-1.0, IB_ABS, 6, SG_PBO},          \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* delta_g' = 4/3 (-theta_g - h'/2) */                                                                             \
+  {{-4.0 / 3.0, IB_ABS, 8, SG_ONE}, {-2.0 / 3.0, IB_DV, DV_HP, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE},                  \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                               \
+  /* theta_g' = k^2 (delta_g/4 - sigma_g) - opac (theta_g - theta_b) */                                              \
+  {{0.25, IB_ABS, 7, SG_K2}, {-0.5, IB_ABS, 9, SG_K2}, {-1.0, IB_ABS, 8, SG_OP}, {1.0, IB_ABS, 6, SG_OP},            \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* photon l = 2: 8/15 (theta_g + k^2 alpha) - 3/5 k F3 - opac (F2 - Pi / 10), Pi = F2 + G0 + G2 */                 \
+  {{8.0 / 15.0, IB_ABS, 8, SG_ONE}, {8.0 / 15.0, IB_DV, DV_ALPHA, SG_K2}, {-0.6, IB_ABS, 10, SG_K},                  \
+   {-0.9, IB_ABS, 9, SG_OP}, {0.1, IB_IGP, 0, SG_OP}, {0.1, IB_IGP, 2, SG_OP}},                                      \
+  /* photon l = lmax: k F_{l-1} - (l + 1) / tau F_l - opac F_l */                                                    \
+  {{1.0, IB_LG7, -1, SG_K}, {1.0, IB_LG7, 0, SG_ITG}, {-1.0, IB_LG7, 0, SG_OP}, {0, IB_DV, DV_ONE, SG_ONE},          \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* polarisation l = 0: -k G1 - opac G0 + opac Pi / 2 */                                                            \
+  {{-1.0, IB_IGP, 1, SG_K}, {-0.5, IB_IGP, 0, SG_OP}, {0.5, IB_ABS, 9, SG_OP}, {0.5, IB_IGP, 2, SG_OP},              \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* polarisation l = 1: k (G0 / 3 - 2 G2 / 3) - opac G1 */                                                          \
+  {{1.0 / 3.0, IB_IGP, 0, SG_K}, {-2.0 / 3.0, IB_IGP, 2, SG_K}, {-1.0, IB_IGP, 1, SG_OP}, {0, IB_DV, DV_ONE, SG_ONE}, \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* polarisation l = 2: k (2 G1 / 5 - 3 G3 / 5) - opac G2 + opac Pi / 10 */                                         \
+  {{0.4, IB_IGP, 1, SG_K}, {-0.6, IB_IGP, 3, SG_K}, {-0.9, IB_IGP, 2, SG_OP}, {0.1, IB_ABS, 9, SG_OP},               \
+   {0.1, IB_IGP, 0, SG_OP}, {0, IB_DV, DV_ONE, SG_ONE}},                                                              \
+  /* polarisation l = lmax */                                                                                        \
+  {{1.0, IB_IGPL, -1, SG_K}, {1.0, IB_IGPL, 0, SG_ITP}, {-1.0, IB_IGPL, 0, SG_OP}, {0, IB_DV, DV_ONE, SG_ONE},       \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* massless nu l = 0: 4/3 (-theta_r - h'/2) */                                                                     \
+  {{-4.0 / 3.0, IB_IR, 1, SG_ONE}, {-2.0 / 3.0, IB_DV, DV_HP, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE},                   \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                               \
+  /* l = 1: k^2 (delta_r / 4 - sigma_r) */                                                                           \
+  {{0.25, IB_IR, 0, SG_K2}, {-0.5, IB_IR, 2, SG_K2}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE},          \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* l = 2: 8/15 (theta_r + k^2 alpha) - 3/5 k F3 */                                                                 \
+  {{8.0 / 15.0, IB_IR, 1, SG_ONE}, {8.0 / 15.0, IB_DV, DV_ALPHA, SG_K2}, {-0.6, IB_IR, 3, SG_K},                     \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                               \
+  /* l = lmax */                                                                                                     \
+  {{1.0, IB_IRL, -1, SG_K}, {1.0, IB_IRL, 0, SG_ITR}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE},         \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* DE fluid delta: -(1+w)(theta + h'/2) - 3 (cs2 - w) aH delta - 9 (1+w)(cs2 - ca2) aH^2 theta / k^2 */             \
+  {{-1.0, IB_N, -1, SG_W1}, {-0.5, IB_DV, DV_HP, SG_W1}, {-1.0, IB_N, -2, SG_DE1}, {-1.0, IB_N, -1, SG_DE2},         \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}},                                                           \
+  /* DE fluid theta: -(1 - 3 cs2) aH theta + cs2 / (1+w) k^2 delta */                                                \
+  {{-1.0, IB_N, -1, SG_DE3}, {1.0, IB_N, -2, SG_DE4}, {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE},         \
+   {0, IB_DV, DV_ONE, SG_ONE}, {0, IB_DV, DV_ONE, SG_ONE}}}
+// row targets (base, offset), in the order above
+#define DEB_LEAD_TARGETS {{IB_ABS, 0}, {IB_ABS, 1}, {IB_ABS, 2}, {IB_ABS, 3}, {IB_ABS, 4}, {IB_ABS, 5}, {IB_ABS, 6},   \
+                          {IB_ABS, 7}, {IB_ABS, 8}, {IB_ABS, 9}, {IB_LG7, 0}, {IB_IGP, 0}, {IB_IGP, 1}, {IB_IGP, 2},  \
+                          {IB_IGPL, 0}, {IB_IR, 0}, {IB_IR, 1}, {IB_IR, 2}, {IB_IRL, 0}, {IB_N, -2}, {IB_N, -1}}
+#ifdef __CUDACC__
+__device__ const LeadTerm d_lead_rows[NLEAD][NLT] = DEB_LEAD_ROWS;
+__device__ const int d_lead_tgt[NLEAD][2] = DEB_LEAD_TARGETS;
+#endif
+static const LeadTerm h_lead_rows[NLEAD][NLT] = DEB_LEAD_ROWS;
+static const int h_lead_tgt[NLEAD][2] = DEB_LEAD_TARGETS;
+
+HD const LeadTerm& lead_term(int r, int t) {
+#ifdef __CUDA_ARCH__
+  return d_lead_rows[r][t];
+#else
+  return h_lead_rows[r][t];
+#endif
+}
+HD int lead_tgt(int r, int f) {
+#ifdef __CUDA_ARCH__
+  return d_lead_tgt[r][f];
+#else
+  return h_lead_tgt[r][f];
+#endif
+}
+// state index of (base, offset), or -1 - k for derived value k
+HD int lead_index(const Dims& D, int base, int off) {
+  switch (base) {
+    case IB_IGP: return D.igp + off;
+    case IB_IR: return D.ir + off;
+    case IB_N: return D.n + off;
+    case IB_LG7: return 7 + D.lg + off;
+    case IB_IGPL: return D.igp + D.lgp + off;
+    case IB_IRL: return D.ir + D.lr + off;
+    case IB_DV: return -1 - off;
+    default: return off;
+  }
+}
+
 // ------------------------------------------------------------------ RHS
 // f = model_synchronous(tau, y) (perturbations.py:84-371).  With S = Dual the
 // a-dependence is differentiated: vout receives f, vjc receives d f / d a.
@@ -477,44 +596,53 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
   S hp = (2.0 * k2 * eta + dgrho) * g.iaH;
   S dgtheta = (m.gOc * tc + m.gOb * tb) * g.ia + (m.g43g * tg + m.g43N * tr + m.grMk * fnu) * g.ia2 + rptQ;
   S etap = 0.5 * dgtheta * m.ik2;
+  // per-call scalars and derived values of the lead rows, through MISC
   if (gp.lead()) {
-    S dgpres = ((m.grhog * dg + m.grN * dr) * (1.0 / 3.0) + m.grM * dpnu) * g.ia2 +
-               (m.cs2Q * rQ * dq + (m.cs2Q - g.ca2) * (3.0 * g.aH * rptQ * m.ik2));
-    const S i1w = drcp(1.0 + g.wQ);
-    S alpha = (hp + 6.0 * etap) * 0.5 * m.ik2;
-    put(0, g.aH * g.a);
-    put(1, -(dgrho + 3.0 * dgpres) * g.a);
-    put(2, etap);
-    put(3, -tc - 0.5 * hp);
-    put(4, -g.aH * tc);
-    put(5, -tb - 0.5 * hp);
-    put(6, -g.aH * tb + k2 * g.cs2 * db + g.pb43 * g.opac * (tg - tb));
-    // photons, temperature (BLT11 2.4)
-    const double polter = y9 + Y(igp) + Y(igp + 2);
-    put(7, (4.0 / 3.0) * (-tg - 0.5 * hp));
-    put(8, k2 * (0.25 * dg - 0.5 * y9) - g.opac * (tg - tb));
-    put(9, (8.0 / 15.0) * (tg + k2 * alpha) - 0.6 * k * Y(10) - g.opac * (y9 - 0.1 * polter));
-    put(7 + lg, k * Y(6 + lg) - (lg + 1.0) * itau * Y(7 + lg) - g.opac * Y(7 + lg));
-    // photons, polarisation l = 0..2 and truncation
-    put(igp, -k * Y(igp + 1) - g.opac * Y(igp) + g.opac * polter * 0.5);
-    put(igp + 1, k * (T.lo[1] * Y(igp) - T.up[1] * Y(igp + 2)) - g.opac * Y(igp + 1));
-    put(igp + 2, k * (T.lo[2] * Y(igp + 1) - T.up[2] * Y(igp + 3)) - g.opac * Y(igp + 2) + g.opac * polter * 0.1);
-    put(igp + lgp, k * Y(igp + lgp - 1) - (lgp + 1.0) * itau * Y(igp + lgp) - g.opac * Y(igp + lgp));
-    // massless neutrinos l = 0..2 and truncation
-    put(ir, (4.0 / 3.0) * (-tr - 0.5 * hp));
-    put(ir + 1, k2 * (0.25 * dr - 0.5 * y_r2));
-    put(ir + 2, (8.0 / 15.0) * (tr + k2 * alpha) - 0.6 * k * Y(ir + 3));
-    put(ir + lr, S(k * Y(ir + lr - 1) - (lr + 1.0) * itau * Y(ir + lr)));
-    // dark-energy fluid (BL10 3.5, 3.6)
-    put(n - 2, -(1.0 + g.wQ) * (tq + 0.5 * hp) - 3.0 * (m.cs2Q - g.wQ) * g.aH * dq -
-                   9.0 * (1.0 + g.wQ) * (m.cs2Q - g.ca2) * g.aH * g.aH * m.ik2 * tq);
-    put(n - 1, -(1.0 - 3.0 * m.cs2Q) * g.aH * tq + m.cs2Q * i1w * k2 * dq);
+    const S dgpres = ((m.grhog * dg + m.grN * dr) * (1.0 / 3.0) + m.grM * dpnu) * g.ia2 +
+                     (m.cs2Q * rQ * dq + (m.cs2Q - g.ca2) * (3.0 * g.aH * rptQ * m.ik2));
+    const S w1 = 1.0 + g.wQ;
+    const S sg[NSIG] = {S(1.0), S(k), S(k2), g.opac, g.aH, g.a, g.aH * g.a, k2 * g.cs2, g.pb43 * g.opac,
+                        S(-(lg + 1.0) * itau), S(-(lgp + 1.0) * itau), S(-(lr + 1.0) * itau), w1,
+                        3.0 * (m.cs2Q - g.wQ) * g.aH, 9.0 * w1 * (m.cs2Q - g.ca2) * g.aH * g.aH * m.ik2,
+                        (1.0 - 3.0 * m.cs2Q) * g.aH, m.cs2Q * drcp(w1) * k2};
+    const S dv[NDV] = {hp, etap, (hp + 6.0 * etap) * 0.5 * m.ik2, dgrho + 3.0 * dgpres, S(1.0)};
+    for (int i = 0; i < NSIG; ++i) {
+      w.m(M_SCAL + S_LEAD + i) = val(sg[i]);
+      if constexpr (kDual) w.m(M_SCAL + S_LEADD + i) = der(sg[i]);
+    }
+    for (int i = 0; i < NDV; ++i) {
+      w.m(M_SCAL + S_LEAD + NSIG + i) = val(dv[i]);
+      if constexpr (kDual) w.m(M_SCAL + S_LEADD + NSIG + i) = der(dv[i]);
+    }
   }
-  for (int l = 3 + gp.lane; l < lg; l += G)
-    put(7 + l, k * (T.lo[l] * Y(6 + l) - T.up[l] * Y(8 + l)) - g.opac * Y(7 + l));
-  for (int l = 3 + gp.lane; l < lgp; l += G)
-    put(igp + l, k * (T.lo[l] * Y(igp + l - 1) - T.up[l] * Y(igp + l + 1)) - g.opac * Y(igp + l));
-  for (int l = 3 + gp.lane; l < lr; l += G) put(ir + l, S(k * (T.lo[l] * Y(ir + l - 1) - T.up[l] * Y(ir + l + 1))));
+  gp.sync();
+  auto scal = [&](int i) -> S {
+    if constexpr (kDual) return mk<S>(w.m(M_SCAL + S_LEAD + i), w.m(M_SCAL + S_LEADD + i));
+    else return w.m(M_SCAL + S_LEAD + i);
+  };
+  for (int r = gp.lane; r < NLEAD; r += G) {
+    S acc = 0.0;
+#pragma unroll
+    for (int t = 0; t < NLT; ++t) {
+      const LeadTerm& e = lead_term(r, t);
+      const int src = lead_index(D, e.base, e.off);
+      const S x = src >= 0 ? S(Y(src)) : scal(NSIG - 1 - src);
+      acc = acc + (e.kap * scal(e.sig)) * x;
+    }
+    put(lead_index(D, lead_tgt(r, 0), lead_tgt(r, 1)), acc);
+  }
+  // photon T and P and massless nu hierarchies, 3 <= l < lmax, in one pass:
+  // element e walks photon T, then P, then nu; only photons scatter
+  {
+    const int nt = lg - 3, np = lgp - 3, nr = lr - 3;
+    for (int e = gp.lane; e < nt + np + nr; e += G) {
+      const bool ph = e < nt + np;
+      const int l = 3 + (e < nt ? e : (ph ? e - nt : e - nt - np));
+      const int j = (e < nt ? 7 : (ph ? igp : ir)) + l;
+      const S damp = ph ? g.opac : S(0.0);
+      put(j, k * (T.lo[l] * Y(j - 1) - T.up[l] * Y(j + 1)) - damp * Y(j));
+    }
+  }
   // massive neutrinos, l-major [l][q].  l = 0, 1, 2 and lmax in one pass over
   // q, then 3 <= l < lmax with element e = (l - 3) nq + i walked as
   // incremental (l, i): every lane of a pass evaluates the same formula.
