@@ -28,6 +28,7 @@
 // The result equals the dense solution to rounding; the work is O(n).
 #pragma once
 
+#include <cstring>
 #include <type_traits>
 
 #ifdef __CUDACC__
@@ -54,21 +55,32 @@ HD bool isfinite_(double x) { return std::isfinite(x); }
 HD bool isfinite_(double x) { return isfinite(x); }
 #endif
 
-// Reciprocal for positive, normal arguments whose reciprocal is normal (all
-// uses here: pivots >= 1/(gamma h), a, tau, aH, error scales).  Device: the
-// PTX approximate reciprocal as seed, then two Newton-Raphson steps
-// y <- y + y (1 - x y), each doubling the correct bits; about 1 ulp.  One
-// FP64 division costs several times as many FP64 instructions.
+// Reciprocal for nonzero normal arguments whose reciprocal is normal (all
+// uses here: pivots, a, tau, aH, error scales).  Device: the
+// PTX approximate reciprocal as seed (relative error below 2^-19), then one
+// third-order Newton-Raphson step y <- y (1 + e + e^2), e = 1 - x y, whose
+// error e^3 < 2^-57 leaves at most 1 ulp; three FMAs where an FP64
+// division costs several times as many FP64 instructions.
 HD double rcp(double x) {
 #ifdef __CUDA_ARCH__
   double y;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-  double e = fma(-x, y, 1.0);
-  y = fma(y, e, y);
-  e = fma(-x, y, 1.0);
-  return fma(y, e, y);
+  const double e = fma(-x, y, 1.0);
+  return fma(y, fma(e, e, e), y);
 #else
   return 1.0 / x;
+#endif
+}
+// Ordering key of |x| from the high word of its bit pattern: integer
+// compares choose pivots without FP64 instructions (ties within 2^-20
+// relative are broken by index, harmless for partial pivoting).
+HD int abs_key(double x) {
+#ifdef __CUDA_ARCH__
+  return __double2hiint(x) & 0x7fffffff;
+#else
+  unsigned long long u;
+  std::memcpy(&u, &x, 8);
+  return (int)((u >> 32) & 0x7fffffffu);
 #endif
 }
 #ifdef __CUDACC__
@@ -226,7 +238,7 @@ HD Dims make_dims(int lg, int lgp, int lr, int lnu, int nq) {
 enum { V_Y = 0, V_U, V_JC0, V_LO, V_UP, V_PI, V_ZH, V_ZE, V_K0, NV = V_K0 + 8 };
 // MISC block offsets
 enum { M_CORE = 0,          // 8x8 core LU (row-major)           64
-       M_CPIV = 64,         // core pivots                         8
+       M_CPIV = 64,         // (unused)                             8
        M_DE = 72,           // DE 2x2 LU + pivot flag              5
        M_CINV = 77,         // Woodbury capacitance inverse        4
        M_SCAL = 81,         // cached per-step scalars            56
@@ -296,7 +308,43 @@ struct Grp {
 #endif
     return x;
   }
-  HD Dual sum(Dual x) const { return Dual(sum(x.v), sum(x.d)); }
+  HD Dual sum(Dual x) const { Dual r = x; sum2(r.v, r.d); return r; }
+  // Two or three sums at once.  Every FP64 add costs a full issue slot of the
+  // FP64 unit whatever the number of active lanes, so the first exchanges
+  // split the values over half- and quarter-warps: 5 adds for two sums and
+  // 6 for three instead of 10 and 15.
+  HD void sum2(double& a, double& b) const {
+#ifdef __CUDA_ARCH__
+    if (G == 32) {
+      const bool lo = lane < 16;
+      double k = (lo ? a : b) + __shfl_xor_sync(0xffffffffu, lo ? b : a, 16);
+      for (int o = 8; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+      a = __shfl_sync(0xffffffffu, k, 0);
+      b = __shfl_sync(0xffffffffu, k, 16);
+      return;
+    }
+#endif
+    a = sum(a);
+    b = sum(b);
+  }
+  HD void sum3(double& a, double& b, double& c) const {
+#ifdef __CUDA_ARCH__
+    if (G == 32) {
+      const bool lo = lane < 16, q = (lane & 8) == 0;
+      const double k1 = (lo ? a : b) + __shfl_xor_sync(0xffffffffu, lo ? b : a, 16);    // lo: a, hi: b
+      const double k2 = (lo ? c : 0.0) + __shfl_xor_sync(0xffffffffu, lo ? 0.0 : c, 16);  // lo: c, hi: 0
+      double k = (q ? k1 : k2) + __shfl_xor_sync(0xffffffffu, q ? k2 : k1, 8);
+      for (int o = 4; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+      a = __shfl_sync(0xffffffffu, k, 0);
+      c = __shfl_sync(0xffffffffu, k, 8);
+      b = __shfl_sync(0xffffffffu, k, 16);
+      return;
+    }
+#endif
+    a = sum(a);
+    b = sum(b);
+    c = sum(c);
+  }
   HD double bcast(double x, int src) const {
 #ifdef __CUDA_ARCH__
     if (G > 1) return __shfl_sync(0xffffffffu, x, src);
@@ -582,9 +630,12 @@ HD void rhs(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D,
     w.m(M_Q + Q_V * nq + i) = val(v);         // v_q and d v_q / d a for the element loop
     if constexpr (kDual) w.m(M_Q + Q_DV * nq + i) = der(v);
   }
-  drhonu = gp.sum(drhonu);
-  dpnu = gp.sum(dpnu);
-  fnu = gp.sum(fnu);
+  if constexpr (kDual) {
+    gp.sum3(drhonu.v, dpnu.v, fnu.v);
+    gp.sum3(drhonu.d, dpnu.d, fnu.d);
+  } else {
+    gp.sum3(drhonu, dpnu, fnu);
+  }
   gp.sync();
   dpnu = dpnu * (1.0 / 3.0);
   const double eta = Y(2), dc = Y(3), tc = Y(4), db = Y(5), tb = Y(6), dg = Y(7), tg = Y(8), y9 = Y(9);
@@ -885,38 +936,61 @@ HD void chain_factor(const ModeConst& m, const Dims& D, const Tab& T, const WS<G
   }
 }
 
-// small dense LU with partial pivoting in the MISC block (row-major, N <= 8)
-template <int N, int G>
-HD void small_lu(const WS<G>& w, int off, int pivoff) {
-  for (int kk = 0; kk < N; ++kk) {
-    int p = kk;
-    double mx = fabs(w.m(off + kk * N + kk));
-    for (int i = kk + 1; i < N; ++i) {
-      const double v = fabs(w.m(off + i * N + kk));
-      if (v > mx) { mx = v; p = i; }
+// 8x8 core: explicit inverse by Gauss-Jordan elimination with partial
+// pivoting, rows over lanes 0..7.  The matrix is in MISC column-major at
+// M_CORE (overwritten), the inverse goes column-major to M_CINV8.  A pivot
+// row stays unscaled until the end, so a step costs one reciprocal, one
+// multiply per row and one FMA per remaining entry; rows are permuted into
+// place with the final scaling.
+template <int G>
+HD void core_invert(const Grp<G>& gp, const WS<G>& w) {
+  auto A = [&](int i, int j) -> double& { return w.m(M_CORE + j * 8 + i); };
+  auto X = [&](int i, int j) -> double& { return w.m(M_CINV8 + j * 8 + i); };
+  for (int e = gp.lane; e < 64; e += G) X(e & 7, e >> 3) = ((e & 7) == (e >> 3)) ? 1.0 : 0.0;
+  gp.sync();
+  unsigned done = 0u;
+  int prow[8];
+  double pinv[8];
+#pragma unroll
+  for (int kk = 0; kk < 8; ++kk) {
+    int p = 0;
+#ifdef __CUDA_ARCH__
+    if (G == 32) {
+      int key = (gp.lane < 8 && !((done >> gp.lane) & 1u)) ? abs_key(A(gp.lane, kk)) : -1;
+      int idx = gp.lane;
+      for (int o = 4; o > 0; o >>= 1) {
+        const int ok = __shfl_xor_sync(0xffffffffu, key, o), oi = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (ok > key || (ok == key && oi < idx)) { key = ok; idx = oi; }
+      }
+      p = __shfl_sync(0xffffffffu, idx, 0);
+    } else
+#endif
+    {
+      int best = -1;
+      for (int i = 0; i < 8; ++i)
+        if (!((done >> i) & 1u) && abs_key(A(i, kk)) > best) { best = abs_key(A(i, kk)); p = i; }
     }
-    w.m(pivoff + kk) = (double)p;
-    if (p != kk)
-      for (int j = 0; j < N; ++j) { double t = w.m(off + kk * N + j); w.m(off + kk * N + j) = w.m(off + p * N + j); w.m(off + p * N + j) = t; }
-    const double inv = rcp(w.m(off + kk * N + kk));
-    for (int i = kk + 1; i < N; ++i) {
-      const double l = w.m(off + i * N + kk) * inv;
-      w.m(off + i * N + kk) = l;
-      if (l != 0.0)
-        for (int j = kk + 1; j < N; ++j) w.m(off + i * N + j) -= l * w.m(off + kk * N + j);
+    done |= 1u << p;
+    prow[kk] = p;
+    const double pi = rcp(A(p, kk));
+    pinv[kk] = pi;
+    for (int i = gp.lane; i < 8; i += G) {
+      if (i != p) {
+        const double f = A(i, kk) * pi;
+        for (int j = kk + 1; j < 8; ++j) A(i, j) -= f * A(p, j);
+        for (int j = 0; j < 8; ++j) X(i, j) -= f * X(p, j);
+      }
     }
-    w.m(off + kk * N + kk) = inv;   // U_kk is kept as its reciprocal
+    gp.sync();
   }
-}
-
-template <int N, int G>
-HD void small_solve(const WS<G>& w, int off, int pivoff, double* r) {
-  for (int kk = 0; kk < N; ++kk) {
-    const int p = (int)w.m(pivoff + kk);
-    if (p != kk) { double t = r[kk]; r[kk] = r[p]; r[p] = t; }
+  // row kk of the inverse = row prow[kk] / its pivot, through M_CORE
+  for (int e = gp.lane; e < 64; e += G) {
+    const int kk = e & 7, j = e >> 3;
+    A(kk, j) = X(prow[kk], j) * pinv[kk];
   }
-  for (int i = 1; i < N; ++i) { double s = r[i]; for (int j = 0; j < i; ++j) s -= w.m(off + i * N + j) * r[j]; r[i] = s; }
-  for (int i = N - 1; i >= 0; --i) { double s = r[i]; for (int j = i + 1; j < N; ++j) s -= w.m(off + i * N + j) * r[j]; r[i] = s * w.m(off + i * N + i); }
+  gp.sync();
+  for (int e = gp.lane; e < 64; e += G) X(e & 7, e >> 3) = A(e & 7, e >> 3);
+  gp.sync();
 }
 
 // entries of the 8x8 photon-baryon core of M (db, tb, dg, tg, T2, P0, P1, P2)
@@ -952,28 +1026,21 @@ HD void factor_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const Tab&
     core_entries(m, T, g, d, core, de);
     core[36] -= w.m(M_SCAL + S_FT);
     core[63] -= w.m(M_SCAL + S_FP);
-    for (int i = 0; i < 64; ++i) w.m(M_CORE + i) = core[i];
-    small_lu<8, G>(w, M_CORE, M_CPIV);
+    for (int i = 0; i < 64; ++i) w.m(M_CORE + (i & 7) * 8 + (i >> 3)) = core[i];   // column-major
     // dark energy 2x2 (rows n-2, n-1): LU with partial pivoting, M_DE+4 = 1 if swapped
     double a00 = de[0], a01 = de[1], a10 = de[2], a11 = de[3];
     double sw = 0.0;
     if (fabs(a10) > fabs(a00)) { double t0_ = a00, t1_ = a01; a00 = a10; a01 = a11; a10 = t0_; a11 = t1_; sw = 1.0; }
-    const double l = a10 / a00;
-    w.m(M_DE + 0) = 1.0 / a00; w.m(M_DE + 1) = a01; w.m(M_DE + 2) = l; w.m(M_DE + 3) = 1.0 / (a11 - l * a01);   // signs vary: true division
+    const double i00 = rcp(a00), l = a10 * i00;
+    w.m(M_DE + 0) = i00; w.m(M_DE + 1) = a01; w.m(M_DE + 2) = l; w.m(M_DE + 3) = rcp(a11 - l * a01);
     w.m(M_DE + 4) = sw;
     w.m(M_SCAL + S_ID) = rcp(d);
     w.m(M_SCAL + S_IDAH) = rcp(d + g.aH);
   }
   gp.sync();
-  // explicit inverse of the core from its LU factors, one column per lane,
-  // so each stage's core solve is an 8-lane matrix-vector product
-  for (int col = gp.lane; col < 8; col += G) {
-    double r[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    r[col] = 1.0;
-    small_solve<8, G>(w, M_CORE, M_CPIV, r);
-    for (int i = 0; i < 8; ++i) w.m(M_CINV8 + i * 8 + col) = r[i];
-  }
-  gp.sync();
+  // explicit inverse of the core, so each stage's core solve is an 8-lane
+  // matrix-vector product
+  core_invert<G>(gp, w);
 }
 
 // z = M^{-1} r on indices >= 2, in place on vector vr.  Expects vr synced.
@@ -1002,9 +1069,22 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>
     const int start = ch == 0 ? ir : (!tail ? iq0 + ch - 1 : (ch == nq + 1 ? 10 : igp + 3));
     const int stride = (ch == 0 || tail) ? 1 : nq;
     const int cnt = ch == 0 ? lr + 1 : (!tail ? lnu + 1 : (ch == nq + 1 ? lg - 2 : lgp - 2));
+    // groups of four elements load ahead of their dependent FMAs, so the
+    // shared-memory latency is paid once per group
     int i = start + (cnt - 1) * stride;
     double rn = w.v(vr, i);
-    for (int j = cnt - 2; j >= 0; --j) {
+    int j = cnt - 2;
+    for (; j >= 3; j -= 4) {
+      const int i0 = i - stride, i1 = i0 - stride, i2 = i1 - stride, i3 = i2 - stride;
+      const double r0 = w.v(vr, i0), r1 = w.v(vr, i1), r2 = w.v(vr, i2), r3 = w.v(vr, i3);
+      const double u0 = w.v(V_UP, i0), u1 = w.v(V_UP, i1), u2 = w.v(V_UP, i2), u3 = w.v(V_UP, i3);
+      rn = r0 - u0 * rn; w.v(vr, i0) = rn;
+      rn = r1 - u1 * rn; w.v(vr, i1) = rn;
+      rn = r2 - u2 * rn; w.v(vr, i2) = rn;
+      rn = r3 - u3 * rn; w.v(vr, i3) = rn;
+      i = i3;
+    }
+    for (; j >= 0; --j) {
       i -= stride;
       rn = w.v(vr, i) - w.v(V_UP, i) * rn;
       w.v(vr, i) = rn;
@@ -1012,7 +1092,19 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>
     if (!tail) {
       double z = rn * w.v(V_PI, start);
       w.v(vr, start) = z;
-      for (int j = 1; j < cnt; ++j) {
+      int jb = 1;
+      for (; jb + 3 < cnt; jb += 4) {
+        const int i0 = i + stride, i1 = i0 + stride, i2 = i1 + stride, i3 = i2 + stride;
+        const double s0 = w.v(vr, i0) * w.v(V_PI, i0), s1 = w.v(vr, i1) * w.v(V_PI, i1);
+        const double s2 = w.v(vr, i2) * w.v(V_PI, i2), s3 = w.v(vr, i3) * w.v(V_PI, i3);
+        const double l0 = w.v(V_LO, i0), l1 = w.v(V_LO, i1), l2 = w.v(V_LO, i2), l3 = w.v(V_LO, i3);
+        z = s0 - l0 * z; w.v(vr, i0) = z;
+        z = s1 - l1 * z; w.v(vr, i1) = z;
+        z = s2 - l2 * z; w.v(vr, i2) = z;
+        z = s3 - l3 * z; w.v(vr, i3) = z;
+        i = i3;
+      }
+      for (; jb < cnt; ++jb) {
         i += stride;
         z = w.v(vr, i) * w.v(V_PI, i) - w.v(V_LO, i) * z;
         w.v(vr, i) = z;
@@ -1029,7 +1121,7 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>
     gp.sync();
     for (int row = gp.lane; row < 8; row += G) {
       double z = 0.0;
-      for (int j = 0; j < 8; ++j) z += w.m(M_CINV8 + row * 8 + j) * r[j];
+      for (int j = 0; j < 8; ++j) z += w.m(M_CINV8 + j * 8 + row) * r[j];
       w.v(vr, cidx[row]) = z;
     }
   }
@@ -1056,8 +1148,9 @@ HD void functionals(const Grp<G>& gp, const Dims& D, const WS<G>& w, int vr, dou
     h += w.m(oh + t) * w.v(vr, gather_index(D, GL_H, t));
     e += w.m(oe + t) * w.v(vr, gather_index(D, GL_E, t));
   }
-  sh = gp.sum(h);
-  se = gp.sum(e);
+  gp.sum2(h, e);
+  sh = h;
+  se = e;
 }
 
 // Per-step factorization of W = d I - J at (t0, y0).  Needs JC0 (d f/d a),
