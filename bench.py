@@ -38,14 +38,29 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+_N323 = dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15)
+_N80 = dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=8, nqmax=3)
+# cosmo: "sample" (seeded draws over the batched ranges), "fiducial" (LCDM + 0.06 eV nu + w0 -0.9, wa 0.1)
+# or "lcdm" (flat LCDM, massless nu); names ending in _grad add the 8-parameter gradient
 WORKLOADS = {
-    # name: (ncosmo, num_k, kmin, kmax, dims, rtol, atol); names ending in _grad include d P / d theta
-    "batched_8cosmo_512k_n323_rtol1e-5_grad": (8, 512, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
-    "batched_64cosmo_512k_n323_rtol1e-5": (64, 512, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
-    "batched_8cosmo_512k_n323_rtol1e-5": (8, 512, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
-    "single_1cosmo_256k_n323_rtol1e-5": (1, 256, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
+    "batched_8cosmo_512k_n323_rtol1e-5_grad": dict(cosmo="sample", ncosmo=8, num_k=512, kmin=1e-4, kmax=10.0,
+                                                   dims=_N323, rtol=1e-5, atol=1e-5, aexp=[1.0]),
+    "fiducial_1cosmo_128k_8a_n323_rtol1e-5_grad": dict(cosmo="fiducial", ncosmo=1, num_k=128, kmin=1e-3, kmax=1.0,
+                                                       dims=_N323, rtol=1e-5, atol=1e-5,
+                                                       aexp=[float(a) for a in np.linspace(0.2, 1.0, 8)]),
+    "batched_64cosmo_512k_n323_rtol1e-5": dict(cosmo="sample", ncosmo=64, num_k=512, kmin=1e-4, kmax=10.0, dims=_N323,
+                                               rtol=1e-5, atol=1e-5, aexp=[1.0]),
+    "batched_8cosmo_512k_n323_rtol1e-5": dict(cosmo="sample", ncosmo=8, num_k=512, kmin=1e-4, kmax=10.0, dims=_N323,
+                                              rtol=1e-5, atol=1e-5, aexp=[1.0]),
+    "fiducial_1cosmo_256k_n323_rtol1e-5": dict(cosmo="fiducial", ncosmo=1, num_k=256, kmin=1e-4, kmax=10.0,
+                                               dims=_N323, rtol=1e-5, atol=1e-5, aexp=[1.0]),
+    "lcdm_1cosmo_64k_n80_rtol1e-3": dict(cosmo="lcdm", ncosmo=1, num_k=64, kmin=1e-4, kmax=1.0, dims=_N80, rtol=1e-3,
+                                         atol=1e-6, aexp=[1.0]),
+    "single_1cosmo_256k_n323_rtol1e-5": dict(cosmo="sample", ncosmo=1, num_k=256, kmin=1e-4, kmax=10.0, dims=_N323,
+                                             rtol=1e-5, atol=1e-5, aexp=[1.0]),
     # profiling case: enough modes to fill every SM's slots, short enough for a counter capture
-    "batched_2cosmo_512k_n323_rtol1e-5": (2, 512, 1e-4, 10.0, dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15), 1e-5, 1e-5),
+    "batched_2cosmo_512k_n323_rtol1e-5": dict(cosmo="sample", ncosmo=2, num_k=512, kmin=1e-4, kmax=10.0, dims=_N323,
+                                              rtol=1e-5, atol=1e-5, aexp=[1.0]),
 }
 DEFAULT_WORKLOAD = "batched_8cosmo_512k_n323_rtol1e-5_grad"
 
@@ -59,13 +74,18 @@ def _dist():
 def make_inputs(name, rank=0, world=1, seed=1234):
     from discoeb_gb300 import background, tables
     from discoeb_gb300.gradient import evolve_backgrounds, perturbed_params
-    from discoeb_gb300.workloads import sample_cosmologies
-
-    ncosmo, num_k, kmin, kmax, dims, rtol, atol = WORKLOADS[name]
-    grad = name.endswith("_grad")
     from discoeb_gb300.sharding import shard
+    from discoeb_gb300.workloads import fiducial_mnu_param, lcdm_massless_param, sample_cosmologies
 
-    params, rejected = sample_cosmologies(ncosmo * world, seed=seed)
+    wl = WORKLOADS[name]
+    ncosmo, num_k, kmin, kmax, dims, rtol, atol = (wl["ncosmo"], wl["num_k"], wl["kmin"], wl["kmax"], wl["dims"],
+                                                   wl["rtol"], wl["atol"])
+    grad = name.endswith("_grad")
+    if wl["cosmo"] == "sample":
+        params, rejected = sample_cosmologies(ncosmo * world, seed=seed)
+    else:
+        fixed = fiducial_mnu_param() if wl["cosmo"] == "fiducial" else lcdm_massless_param()
+        params, rejected = [dict(fixed) for _ in range(ncosmo * world)], 0
     mine = [params[i] for i in shard(ncosmo, world, rank)]
     pert, bgs = None, None
     if grad:
@@ -82,12 +102,13 @@ def make_inputs(name, rank=0, world=1, seed=1234):
     else:
         ps = [background.evolve_background(param=p) for p in mine]
     tabs = tables.pack_batch(ps, dims["nqmax"])
-    tau = np.stack([tables.tau_of_a(p, [1.0]) for p in ps])
+    tau = np.stack([tables.tau_of_a(p, wl["aexp"]) for p in ps])
     k = np.geomspace(kmin, kmax, num_k)
     kk = np.tile(k, ncosmo)
     com = np.repeat(np.arange(ncosmo, dtype=np.int32), num_k)
     return dict(ps=ps, tables=tabs, tau=tau, k=kk, cosmo=com, dims=dims, rtol=rtol, atol=atol, ncosmo=ncosmo,
-                num_k=num_k, rejected=rejected, grad=grad, params=mine, pert=pert, bgs=bgs, kgrid=k)
+                num_k=num_k, rejected=rejected, grad=grad, params=mine, pert=pert, bgs=bgs, kgrid=k, aexp=wl["aexp"],
+                cosmo_kind=wl["cosmo"])
 
 
 class ClockSampler:
@@ -160,12 +181,21 @@ def cpu_baseline(inp, seconds=20.0, threads=0):
     per_mode = t_used / done_modes
     solves = 13 if inp.get("grad") else 1   # nominal + 6 parameters x +-eps by central differences
     return {"value": 1.0 / (per_mode * num_k * solves), "unit": "cosmology solves/s", "cores": threads, "kind": "port",
-            "sample": f"{done_modes} modes of cosmology 0 (k strided over the 512-point grid), {t_used:.1f} s"
+            "sample": f"{done_modes} modes of cosmology 0 (k strided over the {num_k}-point grid), {t_used:.1f} s"
                       + (", x13 solves per cosmology for the 6 ODE gradients (+-eps) and the nominal P(k)" if solves > 1 else "")}
 
 
+def l2_flush_buffer():
+    """256 MB device buffer written before every timed step (L2 is 129 MB), so
+    no step starts with the previous step's tables or outputs in L2."""
+    import torch
+
+    return torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+
 def algorithmic_flops_per_step(dims, nq):
-    """FP64 flops of one attempted step of the structured Rodas5 solve."""
+    """FP64 flops of one attempted step of the structured Rodas5 solve: 8 RHS evaluations (one
+    forward-mode), stage sums, the O(n) factorisation and 8 structured solves."""
     from discoeb_gb300.perturbations import nvar
 
     n = nvar(dims["lmaxg"], dims["lmaxgp"], dims["lmaxr"], dims["lmaxnu"], dims["nqmax"])
@@ -213,21 +243,27 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    flush = l2_flush_buffer()
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
+        e_start.record(stream)
         for i in range(args.steps):
+            flush.fill_(i & 0xFF)
             ev0[i].record(stream)
             prob.launch(cfg, stream)
             ev1[i].record(stream)
             prob.power(4, stream)
+        e_end.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+    dev_s = e_start.elapsed_time(e_end) / 1e3
     if world > 1:
         torch.distributed.barrier()
     kern_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
     from discoeb_gb300.sharding import max_over_ranks
 
-    t_step = max_over_ranks(wall / args.steps, device="cuda")
+    t_step = max_over_ranks(dev_s / args.steps, device="cuda")
     total_cosmo = inp["ncosmo"] * world
     value = total_cosmo / t_step
 
@@ -258,7 +294,9 @@ def run_ours(args):
         "config": {"workload": args.workload, "ncosmo_per_gpu": inp["ncosmo"], "num_k": inp["num_k"],
                    "modes_per_step": int(inp["k"].shape[0]), "nvar": prob.n, "rtol": inp["rtol"],
                    "linear_solver": "structured", "exec_mode": ["auto", "lane", "warp"][prob.plan.dims.exec_mode]
-                   if args.exec_mode != "auto" else "auto", "l2": "working set > L2 (workspace %.2f GB)" % (prob.plan.workspace_bytes() / 1e9),
+                   if args.exec_mode != "auto" else "auto",
+                   "l2": "flushed before every timed step (256 MB write); per-mode state in shared memory",
+                   "aexp_out": inp["aexp"], "cosmology": inp["cosmo_kind"],
                    "redrawn_cosmologies": inp["rejected"]},
         "e2e": {"value": total_cosmo / t_e2e if world == 1 else None, "unit": "cosmology solves/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -284,11 +322,11 @@ def run_gradient(args, inp, world, rank, local):
     import torch
 
     import discoeb_gb300 as deb
-    from discoeb_gb300 import _native
+    from discoeb_gb300 import _native, perturbations as pt
     from discoeb_gb300.gradient import GradientProblem
 
     dims = inp["dims"]
-    gp = GradientProblem(inp["params"], inp["bgs"], inp["pert"], inp["kgrid"], [1.0], rtol=inp["rtol"],
+    gp = GradientProblem(inp["params"], inp["bgs"], inp["pert"], inp["kgrid"], inp["aexp"], rtol=inp["rtol"],
                          atol=inp["atol"], max_steps=args.max_steps, **dims)
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
@@ -299,19 +337,25 @@ def run_gradient(args, inp, world, rank, local):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    flush = l2_flush_buffer()
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
+        e_start.record(stream)
         for i in range(args.steps):
+            flush.fill_(i & 0xFF)
             gp.run(stream, evs[i])
+        e_end.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+    dev_s = e_start.elapsed_time(e_end) / 1e3
     if world > 1:
         torch.distributed.barrier()
     rec_ms = [e[0].elapsed_time(e[1]) for e in evs]
     rep_ms = [e[1].elapsed_time(e[2]) for e in evs]
     from discoeb_gb300.sharding import max_over_ranks
 
-    t_step = max_over_ranks(wall / args.steps, device="cuda")
+    t_step = max_over_ranks(dev_s / args.steps, device="cuda")
     total_cosmo = inp["ncosmo"] * world
     value = total_cosmo / t_step
 
@@ -320,7 +364,7 @@ def run_gradient(args, inp, world, rank, local):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        P, D, _ = deb.evolve_perturbations_grad(params=inp["params"], aexp_out=[1.0], kmin=inp["kgrid"][0],
+        P, D, _ = deb.evolve_perturbations_grad(params=inp["params"], aexp_out=inp["aexp"], kmin=inp["kgrid"][0],
                                                 kmax=inp["kgrid"][-1], num_k=inp["num_k"], rtol=inp["rtol"],
                                                 atol=inp["atol"], max_steps=args.max_steps, backgrounds=inp["bgs"],
                                                 **dims)
@@ -337,15 +381,18 @@ def run_gradient(args, inp, world, rank, local):
     kern_s = (statistics.median(rec_ms) + statistics.median(rep_ms)) * 1e-3
     achieved = flops / kern_s
     out = {
-        "metric": "P(k)+dP/dtheta solves/s on 1 GB300, batched FP64 (8 parameters; structured Rodas5, frozen-step tangents)",
+        "metric": "P(k)+dP/dtheta solves/s on 1 GB300, batched FP64 (8 parameters; structured Rodas5, tangents of the recorded step sequence)",
         "value": value, "unit": "cosmology solves/s (P(k) + 8-parameter gradient)", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded cosmology sample, host RECFAST tables for theta and theta +- 1e-4 theta)",
         "config": {"workload": args.workload, "ncosmo_per_gpu": inp["ncosmo"], "num_k": inp["num_k"],
-                   "modes_per_step": gp.nmode, "replay_items_per_step": gp.nmode * gp.nset, "nvar": 323,
-                   "rtol": inp["rtol"], "theta": list(gp.theta), "gradient": "central differences on the frozen step sequence",
-                   "l2": "per-mode state in shared memory; tables %.1f MB read per step" % ((gp.host_tab0.nbytes + gp.host_tabs.nbytes) / 1e6),
+                   "modes_per_step": gp.nmode, "replay_items_per_step": gp.nmode * gp.nset,
+                   "nvar": pt.nvar(dims["lmaxg"], dims["lmaxgp"], dims["lmaxr"], dims["lmaxnu"], dims["nqmax"]),
+                   "rtol": inp["rtol"], "theta": list(gp.theta),
+                   "gradient": "central differences over the replayed nominal step sequence (jacfwd semantics)",
+                   "l2": "flushed before every timed step (256 MB write); tables %.1f MB read per step" % ((gp.host_tab0.nbytes + gp.host_tabs.nbytes) / 1e6),
+                   "aexp_out": inp["aexp"], "cosmology": inp["cosmo_kind"],
                    "redrawn_cosmologies": inp["rejected"]},
         "e2e": {"value": total_cosmo / t_e2e if world == 1 else None, "unit": "cosmology solves/s (P(k) + 8-parameter gradient)",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -379,7 +426,7 @@ def run_reference(args):
         if i >= args.warmup:
             vals.append(cb["value"])
     v = statistics.median(vals)
-    metric = ("P(k)+dP/dtheta solves/s on 1 GB300, batched FP64 (8 parameters; structured Rodas5, frozen-step tangents)"
+    metric = ("P(k)+dP/dtheta solves/s on 1 GB300, batched FP64 (8 parameters; structured Rodas5, tangents of the recorded step sequence)"
               if inp["grad"] else "P(k) forward solves/s on 1 GB300, batched FP64 structured Rodas5 (gradient not included)")
     out = {"impl": "reference", "metric": metric,
            "value": v * 1.0, "unit": "cosmology solves/s" + (" (P(k) + 8-parameter gradient)" if inp["grad"] else ""),
