@@ -190,7 +190,10 @@ def l2_flush_buffer():
     no step starts with the previous step's tables or outputs in L2."""
     import torch
 
-    return torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    buf.fill_(0)   # first touch outside the timed region
+    torch.cuda.synchronize()
+    return buf
 
 
 def algorithmic_flops_per_step(dims, nq):
@@ -414,6 +417,55 @@ def run_gradient(args, inp, world, rank, local):
         torch.distributed.destroy_process_group()
 
 
+def run_accuracy(args):
+    """Max relative error of the GPU result at the workload's tolerance
+    against tight oracle solves on log-spaced k over the workload's range:
+    P(k) against rtol 1e-8; for gradient workloads also d ln P / d theta
+    against central differences of rtol 1e-7 oracle solves of the same
+    theta +- eps tables (error relative to each parameter's largest
+    |d ln P / d theta|).  Prints one JSON line."""
+    import torch
+
+    import oracle
+    import discoeb_gb300 as deb
+    from discoeb_gb300 import tables as tb
+
+    inp = make_inputs(args.workload, 0, 1)
+    dims = inp["dims"]
+    k = np.geomspace(inp["kgrid"][0], inp["kgrid"][-1], args.accuracy_modes)
+    out = {"workload": args.workload, "modes": int(k.size), "k": [float(x) for x in k],
+           "aexp_out": inp["aexp"], "rtol": inp["rtol"]}
+    p0 = inp["ps"][0]
+    tab0, tau0 = tb.pack_cosmology(p0, dims["nqmax"]), tb.tau_of_a(p0, inp["aexp"])
+    yt, st = oracle.solve(tab0, k, tau0, rtol=1e-8, atol=1e-8 * min(1.0, inp["atol"] / inp["rtol"]),
+                          max_steps=2000000, **dims)
+    if inp["grad"]:
+        P, D, _ = deb.evolve_perturbations_grad(params=inp["params"][0], aexp_out=inp["aexp"], kmin=float(k[0]),
+                                                kmax=float(k[-1]), num_k=k.size, rtol=inp["rtol"], atol=inp["atol"],
+                                                max_steps=args.max_steps, backgrounds=inp["bgs"][0], **dims)
+        errs = {}
+        for j, (name, eps, _, _) in enumerate(inp["pert"][0]):
+            bp, bm = inp["bgs"][0][1 + 2 * j], inp["bgs"][0][2 + 2 * j]
+            yp, sp = oracle.solve(tb.pack_cosmology(bp, dims["nqmax"]), k, tb.tau_of_a(bp, inp["aexp"]), rtol=1e-7,
+                                  atol=1e-7 * min(1.0, inp["atol"] / inp["rtol"]), max_steps=2000000, **dims)
+            ym, sm = oracle.solve(tb.pack_cosmology(bm, dims["nqmax"]), k, tb.tau_of_a(bm, inp["aexp"]), rtol=1e-7,
+                                  atol=1e-7 * min(1.0, inp["atol"] / inp["rtol"]), max_steps=2000000, **dims)
+            gt = (np.log(yp[..., 4] ** 2) - np.log(ym[..., 4] ** 2)) / (2 * eps)
+            from discoeb_gb300.gradient import THETA
+            col = THETA.index(name)
+            errs[name] = float(np.abs(D[:, :, col] - gt).max() / np.abs(gt).max())
+        out["grad_max_rel_err"] = max(errs.values())
+        out["grad_rel_err_by_param"] = errs
+    else:
+        y = deb.solve(tab0[None], k, tau0[None], rtol=inp["rtol"], atol=inp["atol"], max_steps=args.max_steps, **dims)
+        P = np.stack([deb.get_power(k=k, y=y[:, o, :], idx=4, param=p0) for o in range(y.shape[1])], axis=1)
+    Pt = np.stack([deb.get_power(k=k, y=yt[:, o, :], idx=4, param=p0) for o in range(yt.shape[1])], axis=1)
+    out["pk_max_rel_err"] = float((np.abs(P - Pt) / np.abs(Pt)).max())
+    out["oracle_status_ok"] = bool((st[:, 0] == 0).all())
+    torch.cuda.synchronize()
+    print(json.dumps(out))
+
+
 def run_reference(args):
     world, rank, local = _dist()
     if rank != 0:
@@ -452,9 +504,13 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--exec-mode", default="auto", choices=["auto", "lane", "warp"])
+    ap.add_argument("--accuracy", action="store_true", help="print the error against tight oracle solves instead")
+    ap.add_argument("--accuracy-modes", type=int, default=8)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.accuracy:
+        run_accuracy(args)
     else:
         run_ours(args)
 
