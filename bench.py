@@ -442,7 +442,7 @@ def run_accuracy(args):
     if inp["grad"]:
         P, D, _ = deb.evolve_perturbations_grad(params=inp["params"][0], aexp_out=inp["aexp"], kmin=float(k[0]),
                                                 kmax=float(k[-1]), num_k=k.size, rtol=inp["rtol"], atol=inp["atol"],
-                                                max_steps=args.max_steps, backgrounds=inp["bgs"][0], **dims)
+                                                max_steps=args.max_steps, backgrounds=[inp["bgs"][0]], **dims)
         errs = {}
         for j, (name, eps, _, _) in enumerate(inp["pert"][0]):
             bp, bm = inp["bgs"][0][1 + 2 * j], inp["bgs"][0][2 + 2 * j]
