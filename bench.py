@@ -41,12 +41,14 @@ sys.path.insert(0, ROOT)
 _N323 = dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15)
 _N80 = dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=8, nqmax=3)
 # cosmo: "sample" (seeded draws over the batched ranges), "fiducial" (LCDM + 0.06 eV nu + w0 -0.9, wa 0.1)
-# or "lcdm" (flat LCDM, massless nu); names ending in _grad add the 8-parameter gradient
+# or "lcdm" (flat LCDM, massless nu); names ending in _grad add the 8-parameter gradient; step_ts lands
+# steps on every output time (diffrax PIDController(step_ts=...)), so interior outputs and their
+# derivatives are step ends rather than in-step interpolants
 WORKLOADS = {
     "batched_8cosmo_512k_n323_rtol1e-5_grad": dict(cosmo="sample", ncosmo=8, num_k=512, kmin=1e-4, kmax=10.0,
                                                    dims=_N323, rtol=1e-5, atol=1e-5, aexp=[1.0]),
     "fiducial_1cosmo_128k_8a_n323_rtol1e-5_grad": dict(cosmo="fiducial", ncosmo=1, num_k=128, kmin=1e-3, kmax=1.0,
-                                                       dims=_N323, rtol=1e-5, atol=1e-5,
+                                                       dims=_N323, rtol=1e-5, atol=1e-5, step_ts=True,
                                                        aexp=[float(a) for a in np.linspace(0.2, 1.0, 8)]),
     "batched_64cosmo_512k_n323_rtol1e-5": dict(cosmo="sample", ncosmo=64, num_k=512, kmin=1e-4, kmax=10.0, dims=_N323,
                                                rtol=1e-5, atol=1e-5, aexp=[1.0]),
@@ -108,7 +110,7 @@ def make_inputs(name, rank=0, world=1, seed=1234):
     com = np.repeat(np.arange(ncosmo, dtype=np.int32), num_k)
     return dict(ps=ps, tables=tabs, tau=tau, k=kk, cosmo=com, dims=dims, rtol=rtol, atol=atol, ncosmo=ncosmo,
                 num_k=num_k, rejected=rejected, grad=grad, params=mine, pert=pert, bgs=bgs, kgrid=k, aexp=wl["aexp"],
-                cosmo_kind=wl["cosmo"])
+                cosmo_kind=wl["cosmo"], step_ts=bool(wl.get("step_ts", False)))
 
 
 class ClockSampler:
@@ -299,7 +301,7 @@ def run_ours(args):
                    "linear_solver": "structured", "exec_mode": ["auto", "lane", "warp"][prob.plan.dims.exec_mode]
                    if args.exec_mode != "auto" else "auto",
                    "l2": "flushed before every timed step (256 MB write); per-mode state in shared memory",
-                   "aexp_out": inp["aexp"], "cosmology": inp["cosmo_kind"],
+                   "aexp_out": inp["aexp"], "cosmology": inp["cosmo_kind"], "step_to_outputs": inp["step_ts"],
                    "redrawn_cosmologies": inp["rejected"]},
         "e2e": {"value": total_cosmo / t_e2e if world == 1 else None, "unit": "cosmology solves/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -330,7 +332,7 @@ def run_gradient(args, inp, world, rank, local):
 
     dims = inp["dims"]
     gp = GradientProblem(inp["params"], inp["bgs"], inp["pert"], inp["kgrid"], inp["aexp"], rtol=inp["rtol"],
-                         atol=inp["atol"], max_steps=args.max_steps, **dims)
+                         atol=inp["atol"], max_steps=args.max_steps, step_to_outputs=inp["step_ts"], **dims)
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
         gp.run(stream)
@@ -370,7 +372,7 @@ def run_gradient(args, inp, world, rank, local):
         P, D, _ = deb.evolve_perturbations_grad(params=inp["params"], aexp_out=inp["aexp"], kmin=inp["kgrid"][0],
                                                 kmax=inp["kgrid"][-1], num_k=inp["num_k"], rtol=inp["rtol"],
                                                 atol=inp["atol"], max_steps=args.max_steps, backgrounds=inp["bgs"],
-                                                **dims)
+                                                step_to_outputs=inp["step_ts"], **dims)
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     h2d = (gp.host_tab0.nbytes + gp.host_tabs.nbytes + gp.host_tau0.nbytes + gp.host_taus.nbytes + gp.host_k.nbytes
@@ -395,7 +397,7 @@ def run_gradient(args, inp, world, rank, local):
                    "rtol": inp["rtol"], "theta": list(gp.theta),
                    "gradient": "central differences over the replayed nominal step sequence (jacfwd semantics)",
                    "l2": "flushed before every timed step (256 MB write); tables %.1f MB read per step" % ((gp.host_tab0.nbytes + gp.host_tabs.nbytes) / 1e6),
-                   "aexp_out": inp["aexp"], "cosmology": inp["cosmo_kind"],
+                   "aexp_out": inp["aexp"], "cosmology": inp["cosmo_kind"], "step_to_outputs": inp["step_ts"],
                    "redrawn_cosmologies": inp["rejected"]},
         "e2e": {"value": total_cosmo / t_e2e if world == 1 else None, "unit": "cosmology solves/s (P(k) + 8-parameter gradient)",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -417,12 +419,16 @@ def run_gradient(args, inp, world, rank, local):
         torch.distributed.destroy_process_group()
 
 
+# width of each parameter's sampled range (the batched spec), the scale of the reference derivative's step
+PRIOR_WIDTH = {"Omegam": 0.1, "Omegab": 0.015, "h": 0.15, "mnu": 0.24, "w_DE_0": 0.4, "w_DE_a": 0.6}
+
+
 def run_accuracy(args):
     """Max relative error of the GPU result at the workload's tolerance
     against tight oracle solves on log-spaced k over the workload's range:
     P(k) against rtol 1e-8; for gradient workloads also d ln P / d theta
-    against central differences of rtol 1e-7 oracle solves of the same
-    theta +- eps tables (error relative to each parameter's largest
+    against central differences over 1e-3 of each parameter's range of
+    rtol 1e-9 oracle solves (error relative to each parameter's largest
     |d ln P / d theta|).  Prints one JSON line."""
     import torch
 
@@ -438,26 +444,42 @@ def run_accuracy(args):
     p0 = inp["ps"][0]
     tab0, tau0 = tb.pack_cosmology(p0, dims["nqmax"]), tb.tau_of_a(p0, inp["aexp"])
     yt, st = oracle.solve(tab0, k, tau0, rtol=1e-8, atol=1e-8 * min(1.0, inp["atol"] / inp["rtol"]),
-                          max_steps=2000000, **dims)
+                          max_steps=2000000, step_to_outputs=inp["step_ts"], **dims)
     if inp["grad"]:
+        from discoeb_gb300.gradient import THETA, _get, _with, evolve_backgrounds
+
         P, D, _ = deb.evolve_perturbations_grad(params=inp["params"][0], aexp_out=inp["aexp"], kmin=float(k[0]),
                                                 kmax=float(k[-1]), num_k=k.size, rtol=inp["rtol"], atol=inp["atol"],
-                                                max_steps=args.max_steps, backgrounds=[inp["bgs"][0]], **dims)
+                                                max_steps=args.max_steps, backgrounds=[inp["bgs"][0]],
+                                                step_to_outputs=inp["step_ts"], **dims)
+        # reference derivative: central differences over 1e-3 of each parameter's range
+        # (eps = 1e-4 theta is as small as 5e-6 for some draws, where differences of
+        # adaptive solves are dominated by step-control noise) of rtol 1e-9 solves
+        pert = inp["pert"][0]
+        p = inp["params"][0]
+        tp = []
+        for (name, _, _, _) in pert:
+            v, e = float(_get(p, name)), 1e-3 * PRIOR_WIDTH[name]
+            tp += [_with(p, name, v + e), _with(p, name, v - e)]
+        tb_ = evolve_backgrounds(tp)
         errs = {}
-        for j, (name, eps, _, _) in enumerate(inp["pert"][0]):
-            bp, bm = inp["bgs"][0][1 + 2 * j], inp["bgs"][0][2 + 2 * j]
-            yp, sp = oracle.solve(tb.pack_cosmology(bp, dims["nqmax"]), k, tb.tau_of_a(bp, inp["aexp"]), rtol=1e-7,
-                                  atol=1e-7 * min(1.0, inp["atol"] / inp["rtol"]), max_steps=2000000, **dims)
-            ym, sm = oracle.solve(tb.pack_cosmology(bm, dims["nqmax"]), k, tb.tau_of_a(bm, inp["aexp"]), rtol=1e-7,
-                                  atol=1e-7 * min(1.0, inp["atol"] / inp["rtol"]), max_steps=2000000, **dims)
-            gt = (np.log(yp[..., 4] ** 2) - np.log(ym[..., 4] ** 2)) / (2 * eps)
-            from discoeb_gb300.gradient import THETA
+        for j, (name, _, _, _) in enumerate(pert):
+            sols = []
+            for q in tb_[2 * j:2 * j + 2]:
+                yq, sq = oracle.solve(tb.pack_cosmology(q, dims["nqmax"]), k, tb.tau_of_a(q, inp["aexp"]), rtol=1e-9,
+                                      atol=1e-9, max_steps=4000000, step_to_outputs=inp["step_ts"], **dims)
+                if (sq[:, 0] != 0).any():
+                    raise RuntimeError(f"reference solve failed for {name}")
+                sols.append(yq)
+            gt = (np.log(sols[0][..., 4] ** 2) - np.log(sols[1][..., 4] ** 2)) / (2e-3 * PRIOR_WIDTH[name])
             col = THETA.index(name)
             errs[name] = float(np.abs(D[:, :, col] - gt).max() / np.abs(gt).max())
         out["grad_max_rel_err"] = max(errs.values())
         out["grad_rel_err_by_param"] = errs
+        out["step_to_outputs"] = inp["step_ts"]
     else:
-        y = deb.solve(tab0[None], k, tau0[None], rtol=inp["rtol"], atol=inp["atol"], max_steps=args.max_steps, **dims)
+        y = deb.solve(tab0[None], k, tau0[None], rtol=inp["rtol"], atol=inp["atol"], max_steps=args.max_steps,
+                      step_to_outputs=inp["step_ts"], **dims)
         P = np.stack([deb.get_power(k=k, y=y[:, o, :], idx=4, param=p0) for o in range(y.shape[1])], axis=1)
     Pt = np.stack([deb.get_power(k=k, y=yt[:, o, :], idx=4, param=p0) for o in range(yt.shape[1])], axis=1)
     out["pk_max_rel_err"] = float((np.abs(P - Pt) / np.abs(Pt)).max())

@@ -9,8 +9,8 @@ FP64 input tables on the host.
 from .perturbations import (evolve_perturbations, evolve_perturbations_batched, evolve_perturbations_multi,
                             get_power, nvar, solve, DeviceProblem)
 from .background import evolve_background, get_neutrino_momentum_bins
-from .gradient import evolve_perturbations_grad, fisher_matrix
+from .gradient import PowerSpectrum, THETA, evolve_perturbations_grad, fisher_matrix
 
 __all__ = ["evolve_perturbations", "evolve_perturbations_batched", "evolve_perturbations_multi", "get_power", "nvar",
            "solve", "DeviceProblem", "evolve_background", "get_neutrino_momentum_bins", "evolve_perturbations_grad",
-           "fisher_matrix"]
+           "fisher_matrix", "PowerSpectrum", "THETA"]

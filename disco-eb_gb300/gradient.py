@@ -1,21 +1,24 @@
-"""d log P(k, a) / d theta on the GPU: frozen-step tangents.
+"""d log P(k, a) / d theta on the GPU: tangents of the recorded step sequence.
 
 The reference obtains gradients with ``jax.jacfwd`` through
 ``evolve_background`` and ``evolve_perturbations`` (notebooks'
 ``compute_matter_power``; ``DirectAdjoint`` at ``perturbations.py:765``).
 diffrax's PID controller stops gradients through its step-size factor, so
-that derivative is the derivative of the solve on the nominal step sequence:
-the 7-step start-time bisection is piecewise constant in theta, every step
-time is fixed, and only the final step follows ``tau_out(theta)``.
+every step length is dt0 = tau_start / 4 times frozen factors: under jacfwd
+the step times scale with tau_start(theta) (whose derivative flows through
+the start-time bisection's final midpoint), and steps ending on an output
+time follow tau_out(theta).
 
 Here that quantity is computed by central differences of exactly that map:
 ``deb_forward_record`` runs the nominal solve and stores every mode's
-accepted step times, then one ``deb_replay`` launch integrates all
-(mode, theta_p +- eps_p) pairs on those steps with the perturbed tables.
-The difference quotient equals the tangent of the frozen-step map to
-O(eps^2) (eps = 1e-4 relative by default); the map has no branch, so there
-is no step-selection noise.  ``A_s`` and ``n_s`` enter only ``get_power``
-(``perturbations.py:1123``): their derivatives are analytic.
+tau_start and accepted step times, then one ``deb_replay`` launch integrates
+all (mode, theta_p +- eps_p) pairs on those steps, rescaled by each set's
+own tau_start, with the perturbed tables.  The difference quotient equals
+the tangent of that map to O(eps^2) (eps = 1e-4 relative by default); the
+map has no step-size decision, so there is no step-selection noise.  ``A_s``
+and ``n_s`` enter only ``get_power`` (``perturbations.py:1123``): their
+derivatives are analytic.  :class:`PowerSpectrum` wraps the pair as a
+``torch.autograd.Function``.
 """
 from __future__ import annotations
 
@@ -241,3 +244,55 @@ def fisher_matrix(kmodes, dlogP, volume_mpc3: float):
     d = torch.as_tensor(np.asarray(dlogP, dtype=np.float64), device="cuda")
     F = torch.einsum("k,kai,kaj->ij", w, d, d)
     return F.cpu().numpy()
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+class PowerSpectrum:
+    """``torch.autograd.Function`` from theta to P(k, a) for one cosmology.
+
+    ``PowerSpectrum.apply(theta, base_params, options)`` with ``theta`` a
+    float64 tensor [8] in the order of :data:`THETA` (h, not H0), overriding
+    those entries of ``base_params``; ``options`` is a dict of the keyword
+    arguments of :func:`evolve_perturbations_grad` (aexp_out, kmin, kmax,
+    num_k, hierarchy sizes, tolerances, ...).  Forward runs the recorded
+    solve and the replay of theta +- eps (host tables for the 13 parameter
+    sets, one GPU launch pair) and returns P [num_k, nout] on theta's device;
+    it keeps d ln P / d theta, so backward is grad_theta = sum over (k, a) of
+    grad_P * P * d ln P / d theta, with no further solve.
+    """
+
+    _fn = None
+
+    @classmethod
+    def apply(cls, theta, base_params, options):
+        if cls._fn is None:
+            torch = _torch()
+
+            class _Fn(torch.autograd.Function):
+                @staticmethod
+                def forward(ctx, th, base, opts):
+                    vals = th.detach().cpu().numpy().astype(np.float64)
+                    if vals.shape != (len(THETA),):
+                        raise ValueError(f"theta must have {len(THETA)} entries in the order {THETA}")
+                    params = dict(base)
+                    for name, v in zip(THETA, vals):
+                        params = _with(params, name, float(v))
+                    P, D, _ = evolve_perturbations_grad(params=params, theta=THETA, **opts)
+                    Pt = torch.as_tensor(P, dtype=torch.float64, device=th.device)
+                    Dt = torch.as_tensor(D, dtype=torch.float64, device=th.device)
+                    ctx.save_for_backward(Pt, Dt)
+                    return Pt
+
+                @staticmethod
+                def backward(ctx, gP):
+                    Pt, Dt = ctx.saved_tensors
+                    g = torch.einsum("ka,kat->t", gP.to(torch.float64) * Pt, Dt)
+                    return g, None, None
+
+            cls._fn = _Fn
+        return cls._fn.apply(theta, base_params, options)

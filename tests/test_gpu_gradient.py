@@ -124,3 +124,23 @@ def test_fisher_matrix_is_symmetric_and_positive(setup):
     assert F.shape == (8, 8) and np.isfinite(F).all()
     np.testing.assert_allclose(F, F.T, rtol=1e-12)
     assert np.linalg.eigvalsh(F).min() >= -1e-8 * np.abs(F).max()
+
+
+def test_autograd_function_backward_is_P_times_dlogP(setup):
+    """PowerSpectrum.apply: forward equals evolve_perturbations_grad's P; the
+    gradient of a weighted sum of P is sum w P d ln P / d theta."""
+    import torch
+
+    base, pert, bgs = setup
+    from discoeb_gb300.gradient import THETA, _get
+
+    opts = dict(aexp_out=[0.5, 1.0], kmin=1e-3, kmax=0.5, num_k=5, rtol=1e-5, atol=1e-8, max_steps=20000,
+                backgrounds=[bgs], **DIMS)
+    theta = torch.tensor([float(_get(base, n)) for n in THETA], dtype=torch.float64, device="cuda", requires_grad=True)
+    P = deb.PowerSpectrum.apply(theta, base, opts)
+    P0, D0, _ = deb.evolve_perturbations_grad(params=base, **opts)
+    np.testing.assert_allclose(P.detach().cpu().numpy(), P0, rtol=1e-12)
+    w = torch.linspace(1.0, 2.0, P.numel(), dtype=torch.float64, device="cuda").reshape(P.shape)
+    (w * P).sum().backward()
+    expect = np.einsum("ka,ka,kat->t", w.cpu().numpy(), P0, D0)
+    np.testing.assert_allclose(theta.grad.cpu().numpy(), expect, rtol=1e-10)
