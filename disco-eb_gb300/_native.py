@@ -33,7 +33,8 @@ class DebSolverCfg(ctypes.Structure):
 _lib = None
 EXPORTS = ("deb_nvar", "deb_plan_create", "deb_plan_workspace_bytes", "deb_plan_set_order", "deb_forward",
            "deb_forward_static",
-           "deb_forward_record", "deb_replay", "deb_get_power",
+           "deb_forward_record", "deb_replay", "deb_get_power", "deb_power_multipoles", "deb_density_velocity",
+           "deb_power_kaiser", "deb_savgol_log", "deb_fftlog_phase",
            "deb_plan_destroy", "deb_measure_fp64_peak", "deb_error_string", "deb_version")
 
 
@@ -62,6 +63,12 @@ def load(path: str | None = None):
                              ctypes.POINTER(DebSolverCfg), vp, ctypes.c_int, vp, vp, vp, vp]
     L.deb_get_power.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
                                 ctypes.c_int, vp, vp]
+    ci, cd = ctypes.c_int, ctypes.c_double
+    L.deb_power_multipoles.argtypes = [vp, ci, ci, vp, vp, ci, ci, vp, ci, cd, vp, vp, vp, vp]
+    L.deb_density_velocity.argtypes = [vp, ci, ci, vp, vp, ci, vp, ci, vp, vp, vp]
+    L.deb_power_kaiser.argtypes = [vp, vp, ci, vp, ci, cd, vp, vp]
+    L.deb_savgol_log.argtypes = [vp, ci, ci, vp, ci, vp, vp]
+    L.deb_fftlog_phase.argtypes = [ci, cd, ci, vp, vp]
     L.deb_plan_destroy.argtypes = [vp]
     L.deb_plan_destroy.restype = None
     L.deb_measure_fp64_peak.argtypes = [ctypes.POINTER(ctypes.c_double), vp]

@@ -6,7 +6,7 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-SRC = [os.path.join(HERE, "csrc", "deb_solver.cu")]
+SRC = [os.path.join(HERE, "csrc", "deb_solver.cu"), os.path.join(HERE, "csrc", "deb_observables.cu")]
 DEPS = SRC + [os.path.join(HERE, "csrc", "deb_core.cuh"), os.path.join(ROOT, "include", "discoeb_gb300.h")]
 OUT = os.path.join(HERE, "_build", "libdiscoeb_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"

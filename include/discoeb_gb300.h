@@ -179,6 +179,36 @@ int deb_get_power(const double* d_tables, int ncosmo, int blob_len, const double
 void deb_plan_destroy(deb_plan* plan);
 
 /*
+ * Observables on top of the perturbations (no plan needed; stream-ordered).
+ *
+ * deb_power_multipoles -- power_multipoles (perturbations.py:1202-1224):
+ *   with A = sqrt(2 pi^2 A_s (k/k_p)^(n_s-1) k^-3), delta = A y[.,4],
+ *   theta = A y[.,5] (theta / aH, so -f delta in linear theory):
+ *   P0 = b^2 delta^2 - 2b/3 delta theta + theta^2/5, P2 = -4b/3 delta theta
+ *   + 4/7 theta^2, P4 = 8/35 theta^2.  d_y [nmode, nout, stride]; outputs [nmode, nout].
+ * deb_density_velocity -- the delta and theta amplitudes above for one output
+ *   (perturbations.py:1188-1190); d_y [nmode, stride]; d_delta, d_theta [nmode].
+ * deb_power_kaiser -- power_Kaiser's P(k, mu) = (b delta - mu^2 theta)^2
+ *   (perturbations.py:1198); d_Pkmu [nmode, nmu].
+ * deb_savgol_log -- get_power_smoothed's filter (perturbations.py:1148-1159,
+ *   util.py:407-444): exp of the 'same' convolution of ln P (nrow rows of n
+ *   points) with d_coeffs[window] (window odd), the first window/2 and last
+ *   window/2 + 1 points of each row copied from the input.
+ * deb_fftlog_phase -- get_xi_from_P's phase factors (perturbations.py:1088-1094):
+ *   exp(2i (arg Gamma((1.5+ell)/2 + i t_p) - ln(pi) t_p)), t_p = pi p / L,
+ *   L = ln(kmax/kmin), p = 0..nfreq-1, as interleaved (re, im) pairs.
+ */
+int deb_power_multipoles(const double* d_tables, int ncosmo, int blob_len, const double* d_k, const int* d_cosmo_of_mode,
+                         int nmode, int nout, const double* d_y, int stride, double bias, double* d_P0, double* d_P2,
+                         double* d_P4, void* stream);
+int deb_density_velocity(const double* d_tables, int ncosmo, int blob_len, const double* d_k, const int* d_cosmo_of_mode,
+                         int nmode, const double* d_y, int stride, double* d_delta, double* d_theta, void* stream);
+int deb_power_kaiser(const double* d_delta, const double* d_theta, int nmode, const double* d_mu, int nmu, double bias,
+                     double* d_Pkmu, void* stream);
+int deb_savgol_log(const double* d_P, int nrow, int n, const double* d_coeffs, int window, double* d_out, void* stream);
+int deb_fftlog_phase(int nfreq, double log_kmax_over_kmin, int ell, double* d_phase, void* stream);
+
+/*
  * Allocation-free variant of deb_forward.  No counterpart in the reference.
  *
  * Some callers cannot allocate device memory at all -- for example code that
