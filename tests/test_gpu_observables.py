@@ -19,7 +19,7 @@ DIMS = dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=8, nqmax=3)
 def sol():
     p = bg.evolve_background(param=lcdm_massless_param())
     y, k, p = deb.evolve_perturbations(param=p, aexp_out=[0.5, 1.0], kmin=1e-4, kmax=1.0, num_k=128, rtol=1e-4,
-                                       atol=1e-7, **DIMS)
+                                       atol=1e-7, max_steps=20000, **DIMS)
     return p, y, k
 
 
