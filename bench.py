@@ -234,12 +234,13 @@ def run_ours(args):
     cfg = pt._cfg(inp["rtol"], inp["atol"], 0.25, 0.80, 0.0, 20.0, 0.3, args.max_steps)
     stream = torch.cuda.current_stream()
 
-    def one_step():
-        prob.launch(cfg, stream)
-        return prob.power(4, stream)
-
+    tune_ms = prob.tune(cfg) if args.tune else {}
+    launch = prob.plan.launch_info()
     for _ in range(args.warmup):
-        one_step()
+        prob.launch(cfg, stream)
+        prob.power(4, stream)
+    # the whole solve (queue reset, persistent launch, get_power) as one CUDA graph
+    prob.capture(cfg, 4)
     torch.cuda.synchronize()
     st = prob.status.cpu().numpy()
     steps = prob.steps.cpu().numpy()
@@ -256,9 +257,8 @@ def run_ours(args):
         for i in range(args.steps):
             flush.fill_(i & 0xFF)
             ev0[i].record(stream)
-            prob.launch(cfg, stream)
+            prob.replay()
             ev1[i].record(stream)
-            prob.power(4, stream)
         e_end.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
@@ -300,6 +300,8 @@ def run_ours(args):
                    "modes_per_step": int(inp["k"].shape[0]), "nvar": prob.n, "rtol": inp["rtol"],
                    "linear_solver": "structured", "exec_mode": ["auto", "lane", "warp"][prob.plan.dims.exec_mode]
                    if args.exec_mode != "auto" else "auto",
+                   "cuda_graph": "queue reset + persistent launch + get_power captured once, replayed per step",
+                   "launch_shape": launch, "autotune_ms": {f"{a}/{b}": round(v, 2) for (a, b), v in tune_ms.items()},
                    "l2": "flushed before every timed step (256 MB write); per-mode state in shared memory",
                    "aexp_out": inp["aexp"], "cosmology": inp["cosmo_kind"], "step_to_outputs": inp["step_ts"],
                    "redrawn_cosmologies": inp["rejected"]},
@@ -334,45 +336,67 @@ def run_gradient(args, inp, world, rank, local):
     gp = GradientProblem(inp["params"], inp["bgs"], inp["pert"], inp["kgrid"], inp["aexp"], rtol=inp["rtol"],
                          atol=inp["atol"], max_steps=args.max_steps, step_to_outputs=inp["step_ts"], **dims)
     stream = torch.cuda.current_stream()
-    for _ in range(args.warmup):
-        gp.run(stream)
+    tune_ms = gp.tune() if args.tune else {}
+    launch = gp.plan.launch_info()
+    # eager warm-up steps, timed per launch for the record / replay split
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(max(1, args.warmup))]
+    for i in range(len(evs)):
+        gp.run(stream, evs[i])
     torch.cuda.synchronize()
     gp.check()
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    rec_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    rep_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    # the whole step (record, replay, get_power, difference quotients) as one CUDA graph
+    gp.capture()
+    gp.replay(stream)
+    torch.cuda.synchronize()
+    gp.check()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     flush = l2_flush_buffer()
     e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         e_start.record(stream)
         for i in range(args.steps):
             flush.fill_(i & 0xFF)
-            gp.run(stream, evs[i])
+            ev0[i].record(stream)
+            gp.replay(stream)
+            ev1[i].record(stream)
         e_end.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     dev_s = e_start.elapsed_time(e_end) / 1e3
+    graph_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+    gp.check()
     if world > 1:
         torch.distributed.barrier()
-    rec_ms = [e[0].elapsed_time(e[1]) for e in evs]
-    rep_ms = [e[1].elapsed_time(e[2]) for e in evs]
     from discoeb_gb300.sharding import max_over_ranks
 
     t_step = max_over_ranks(dev_s / args.steps, device="cuda")
     total_cosmo = inp["ncosmo"] * world
     value = total_cosmo / t_step
 
-    # end to end through the public call from host buffers (tables for theta and theta +- eps)
+    # end to end through the public call from host buffers (tables for theta and theta +- eps): the first
+    # two calls of a shape build the problem and capture its graph (untimed), later calls pack and copy
+    # their inputs through pinned memory, replay the graph and copy P and the gradient back
     e2e_steps = max(1, min(args.steps, 2))
+
+    def e2e_call():
+        return deb.evolve_perturbations_grad(params=inp["params"], aexp_out=inp["aexp"], kmin=inp["kgrid"][0],
+                                             kmax=inp["kgrid"][-1], num_k=inp["num_k"], rtol=inp["rtol"],
+                                             atol=inp["atol"], max_steps=args.max_steps, backgrounds=inp["bgs"],
+                                             step_to_outputs=inp["step_ts"], **dims)
+
+    e2e_call()
+    e2e_call()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        P, D, _ = deb.evolve_perturbations_grad(params=inp["params"], aexp_out=inp["aexp"], kmin=inp["kgrid"][0],
-                                                kmax=inp["kgrid"][-1], num_k=inp["num_k"], rtol=inp["rtol"],
-                                                atol=inp["atol"], max_steps=args.max_steps, backgrounds=inp["bgs"],
-                                                step_to_outputs=inp["step_ts"], **dims)
+        P, D, _ = e2e_call()
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     h2d = (gp.host_tab0.nbytes + gp.host_tabs.nbytes + gp.host_tau0.nbytes + gp.host_taus.nbytes + gp.host_k.nbytes
@@ -383,7 +407,7 @@ def run_gradient(args, inp, world, rank, local):
     att = int(gp.d_steps.sum().item())
     rep = int(gp.d_nrec.sum().item()) * gp.nset
     flops = algorithmic_flops_per_step(dims, dims["nqmax"]) * (att + rep)
-    kern_s = (statistics.median(rec_ms) + statistics.median(rep_ms)) * 1e-3
+    kern_s = statistics.median(graph_ms) * 1e-3     # the graph's two solver launches + sub-ms tail work
     achieved = flops / kern_s
     out = {
         "metric": "P(k)+dP/dtheta solves/s on 1 GB300, batched FP64 (8 parameters; structured Rodas5, tangents of the recorded step sequence)",
@@ -396,6 +420,8 @@ def run_gradient(args, inp, world, rank, local):
                    "nvar": pt.nvar(dims["lmaxg"], dims["lmaxgp"], dims["lmaxr"], dims["lmaxnu"], dims["nqmax"]),
                    "rtol": inp["rtol"], "theta": list(gp.theta),
                    "gradient": "central differences over the replayed nominal step sequence (jacfwd semantics)",
+                   "cuda_graph": "record + replay + get_power + quotients captured once, replayed per step",
+                   "launch_shape": launch, "autotune_ms": {f"{a}/{b}": round(v, 2) for (a, b), v in tune_ms.items()},
                    "l2": "flushed before every timed step (256 MB write); tables %.1f MB read per step" % ((gp.host_tab0.nbytes + gp.host_tabs.nbytes) / 1e6),
                    "aexp_out": inp["aexp"], "cosmology": inp["cosmo_kind"], "step_to_outputs": inp["step_ts"],
                    "redrawn_cosmologies": inp["rejected"]},
@@ -405,10 +431,11 @@ def run_gradient(args, inp, world, rank, local):
                      "frac": achieved / peak, "traffic": None,
                      "note": "FP64-pipe bound (state in shared memory); peak = FP64 FMA microkernel measured in this run; "
                              "achieved = algorithmic FLOPs of the structured Rodas5 step x (attempted + replayed steps)"},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": 4 * args.steps,
         "clocks": clk.summary(),
         "forward_value": total_cosmo / (statistics.median(rec_ms) * 1e-3),
-        "record_ms_median": statistics.median(rec_ms), "replay_ms_median": statistics.median(rep_ms),
+        "graph_ms_median": statistics.median(graph_ms),
+        "record_ms_eager_median": statistics.median(rec_ms), "replay_ms_eager_median": statistics.median(rep_ms),
         "attempted_steps_per_launch": att, "replayed_steps_per_launch": rep,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -488,6 +515,45 @@ def run_accuracy(args):
     print(json.dumps(out))
 
 
+def run_plain(args):
+    """The plain single-cosmology FP64 GPU form of the gradient workload, the
+    denominator the batched form is compared with: the reference's own
+    method on the GPU -- dense W = I/(gamma h) - J formed every step and
+    factored by FP64 LU with partial pivoting (O(n^3), as lu_factor in
+    ode_integrators_stiff.py:772-780) -- one cosmology (the workload's
+    first) per launch pair, record + replay of its 12 theta +- eps sets.
+    One untimed 2-mode launch first, then one timed pair.  Prints one JSON
+    line (not a bench line)."""
+    import torch
+
+    from discoeb_gb300.gradient import GradientProblem
+
+    torch.cuda.set_device(0)
+    inp = make_inputs(args.workload, 0, 1)
+    if not inp["grad"]:
+        raise SystemExit("--plain needs a gradient workload")
+    dims = inp["dims"]
+    kw = dict(rtol=inp["rtol"], atol=inp["atol"], max_steps=args.max_steps, step_to_outputs=inp["step_ts"],
+              linear_solver="dense", **dims)
+    warm = GradientProblem(inp["params"][:1], inp["bgs"][:1], inp["pert"][:1], inp["kgrid"][:2], inp["aexp"], **kw)
+    warm.run()
+    torch.cuda.synchronize()
+    gp = GradientProblem(inp["params"][:1], inp["bgs"][:1], inp["pert"][:1], inp["kgrid"], inp["aexp"], **kw)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    with ClockSampler(0) as clk:
+        gp.run(torch.cuda.current_stream(), ev)
+        torch.cuda.synchronize()
+    gp.check()
+    rec_ms, rep_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    print(json.dumps({
+        "form": "plain single-cosmology FP64 GPU form (dense LU per step, reference method)",
+        "workload": args.workload, "num_k": inp["num_k"], "replay_items": gp.nmode * gp.nset,
+        "record_ms": rec_ms, "replay_ms": rep_ms,
+        "value": 1e3 / (rec_ms + rep_ms), "forward_value": 1e3 / rec_ms,
+        "unit": "cosmology solves/s (P(k) + 8-parameter gradient); forward_value: P(k) only",
+        "attempted_steps": int(gp.d_steps.sum().item()), "clocks": clk.summary()}))
+
+
 def run_reference(args):
     world, rank, local = _dist()
     if rank != 0:
@@ -526,13 +592,18 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--exec-mode", default="auto", choices=["auto", "lane", "warp"])
+    ap.add_argument("--no-tune", dest="tune", action="store_false", help="skip the launch-shape autotuner")
     ap.add_argument("--accuracy", action="store_true", help="print the error against tight oracle solves instead")
+    ap.add_argument("--plain", action="store_true",
+                    help="time the plain single-cosmology FP64 dense-LU GPU form of the workload instead")
     ap.add_argument("--accuracy-modes", type=int, default=8)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.accuracy:
         run_accuracy(args)
+    elif args.plain:
+        run_plain(args)
     else:
         run_ours(args)
 

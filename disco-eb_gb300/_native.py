@@ -23,6 +23,13 @@ class DebDims(ctypes.Structure):
                 ("linear_solver", ctypes.c_int), ("exec_mode", ctypes.c_int)]
 
 
+class DebLaunchCfg(ctypes.Structure):
+    _fields_ = [("stage_vectors", ctypes.c_int), ("modes_per_sm", ctypes.c_int)]
+
+
+STAGE_VECTORS = {"auto": 0, "shared": 1, "global": 2}
+
+
 class DebSolverCfg(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double), ("pcoeff", ctypes.c_double),
                 ("icoeff", ctypes.c_double), ("dcoeff", ctypes.c_double), ("factormax", ctypes.c_double),
@@ -31,7 +38,7 @@ class DebSolverCfg(ctypes.Structure):
 
 
 _lib = None
-EXPORTS = ("deb_nvar", "deb_plan_create", "deb_plan_workspace_bytes", "deb_plan_set_order", "deb_forward",
+EXPORTS = ("deb_nvar", "deb_plan_create", "deb_plan_create_ex", "deb_plan_launch_info", "deb_plan_workspace_bytes", "deb_plan_set_order", "deb_forward",
            "deb_forward_static",
            "deb_forward_record", "deb_replay", "deb_get_power", "deb_power_multipoles", "deb_density_velocity",
            "deb_power_kaiser", "deb_savgol_log", "deb_fftlog_phase",
@@ -51,6 +58,9 @@ def load(path: str | None = None):
     vp = ctypes.c_void_p
     L.deb_nvar.argtypes = [ctypes.POINTER(DebDims)]
     L.deb_plan_create.argtypes = [ctypes.POINTER(DebDims), ctypes.c_int, ctypes.POINTER(vp)]
+    L.deb_plan_create_ex.argtypes = [ctypes.POINTER(DebDims), ctypes.c_int, ctypes.POINTER(DebLaunchCfg),
+                                     ctypes.POINTER(vp)]
+    L.deb_plan_launch_info.argtypes = [vp, ctypes.POINTER(DebLaunchCfg), ctypes.POINTER(ctypes.c_int)]
     L.deb_plan_workspace_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
     L.deb_plan_set_order.argtypes = [vp, vp, ctypes.c_int]
     L.deb_forward.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp,
@@ -87,11 +97,25 @@ def check(rc: int, what: str):
 class Plan:
     """Owns one deb_plan (device workspace sized for max_modes)."""
 
-    def __init__(self, dims: DebDims, max_modes: int):
+    def __init__(self, dims: DebDims, max_modes: int, launch: tuple[str, int] | None = None):
+        """``launch`` = (stage vectors "auto" | "shared" | "global", modes per SM cap or 0)."""
         self.dims = dims
         self.max_modes = max_modes
         self.ptr = ctypes.c_void_p()
-        check(load().deb_plan_create(ctypes.byref(dims), int(max_modes), ctypes.byref(self.ptr)), "deb_plan_create")
+        if launch is None:
+            check(load().deb_plan_create(ctypes.byref(dims), int(max_modes), ctypes.byref(self.ptr)), "deb_plan_create")
+        else:
+            lc = DebLaunchCfg(STAGE_VECTORS[launch[0]], int(launch[1]))
+            check(load().deb_plan_create_ex(ctypes.byref(dims), int(max_modes), ctypes.byref(lc), ctypes.byref(self.ptr)),
+                  "deb_plan_create_ex")
+
+    def launch_info(self) -> dict:
+        """Resolved launch shape: stage vector placement, modes per SM, modes in flight."""
+        lc, nf = DebLaunchCfg(), ctypes.c_int()
+        check(load().deb_plan_launch_info(self.ptr, ctypes.byref(lc), ctypes.byref(nf)), "deb_plan_launch_info")
+        names = {v: k for k, v in STAGE_VECTORS.items()}
+        return {"stage_vectors": names[lc.stage_vectors], "modes_per_sm": int(lc.modes_per_sm),
+                "modes_in_flight": int(nf.value)}
 
     def workspace_bytes(self) -> int:
         b = ctypes.c_size_t()

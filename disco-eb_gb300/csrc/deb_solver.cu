@@ -26,6 +26,9 @@
 namespace {
 
 constexpr int kBlock = 128;
+// one-warp blocks resident per SM: the warp kernel is compiled with up to 255
+// registers per thread (launch bound 32), 8 such warps fill the register file
+constexpr int kMaxWarpBlocksPerSM = 8;
 
 __constant__ deb::Tab c_tab;
 __constant__ deb::Rodas c_rodas;
@@ -227,6 +230,8 @@ __global__ void fp64_peak_kernel(double* out, int iters, double a, double b) {
 }
 
 bool g_consts_ready[64] = {false};
+// largest dynamic shared memory size set on forward_warp_kernel, per device
+long g_warp_smem_attr[64] = {0};
 
 int upload_constants() {
   int dev = 0;
@@ -252,7 +257,7 @@ struct deb_plan {
   // lane mode
   int lane_blocks, lane_slots;
   // warp mode
-  int warp_block_warps, warp_blocks, warp_smem, warp_k_global;
+  int warp_block_warps, warp_blocks, warp_smem, warp_k_global, warp_per_sm;
   long warp_smem_bytes;
   double* kws;      // warp mode: stage vectors in global memory
   double* ws;       // lane slots (or warp slots when shared memory is too small)
@@ -287,7 +292,14 @@ int deb_nvar(const deb_dims* d) {
 }
 
 int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
+  return deb_plan_create_ex(dims, max_modes, nullptr, out);
+}
+
+int deb_plan_create_ex(const deb_dims* dims, int max_modes, const deb_launch_cfg* lc, deb_plan** out) {
   if (!dims || !out || max_modes <= 0) return DEB_ERR_INVALID;
+  const int stage_where = lc ? lc->stage_vectors : DEB_STAGE_AUTO;
+  const int mps_cap = lc ? lc->modes_per_sm : 0;
+  if (stage_where < DEB_STAGE_AUTO || stage_where > DEB_STAGE_GLOBAL || mps_cap < 0) return DEB_ERR_INVALID;
   *out = nullptr;
   if (dims->lmaxg < 3 || dims->lmaxgp < 3 || dims->lmaxr < 3 || dims->lmaxnu < 3 || dims->nqmax < 1 || dims->nout < 1)
     return DEB_ERR_INVALID;
@@ -336,19 +348,32 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
     const long full_bytes = p->slot_len * 8, hot_bytes = deb::hot_len(p->D) * 8;
     const long sm_bytes = 228L * 1024;
     long smem_bytes;
-    if (sm_bytes / (full_bytes + 1024) >= 2) { smem_bytes = full_bytes; p->warp_k_global = 0; }
-    else { smem_bytes = hot_bytes; p->warp_k_global = 1; }
+    const bool full_fits = sm_bytes / (full_bytes + 1024) >= 2 && full_bytes <= smem_optin;
+    bool k_global;
+    if (stage_where == DEB_STAGE_SHARED) {
+      if (full_bytes > smem_optin) { delete p; return DEB_ERR_INVALID; }
+      k_global = false;
+    } else if (stage_where == DEB_STAGE_GLOBAL) {
+      k_global = true;
+    } else {
+      k_global = !full_fits;
+    }
+    smem_bytes = k_global ? hot_bytes : full_bytes;
+    p->warp_k_global = k_global ? 1 : 0;
     p->warp_smem = smem_bytes <= smem_optin;
     if (!p->warp_smem) p->warp_k_global = 0;
     p->warp_block_warps = 1;
-    // blocks (= modes in flight) per SM limited by shared memory and by
-    // registers (at most 12 one-warp blocks)
-    int per_sm = 12;
+    // blocks (= modes in flight) per SM limited by shared memory, by
+    // registers (at most 8 one-warp blocks of 255 registers per thread) and
+    // by the caller's cap
+    int per_sm = kMaxWarpBlocksPerSM;
     if (p->warp_smem) {
       const int by_smem = (int)(sm_bytes / (smem_bytes + 1024));
       if (by_smem < per_sm) per_sm = by_smem;
-      if (per_sm < 1) per_sm = 1;
     }
+    if (mps_cap > 0 && mps_cap < per_sm) per_sm = mps_cap;
+    if (per_sm < 1) per_sm = 1;
+    p->warp_per_sm = per_sm;
     long cap_warps = (long)nsm * per_sm;
     if (cap_warps > mem_cap) cap_warps = mem_cap;
     long want = max_modes;
@@ -356,11 +381,14 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
     p->warp_blocks = (int)nw;
     nslots = nw;
     p->warp_smem_bytes = smem_bytes;
-    if (p->warp_smem) {
+    // the attribute belongs to the kernel, not to the plan: only ever raise
+    // it, so that plans made earlier with a larger slot stay launchable
+    if (p->warp_smem && (dev < 0 || dev >= 64 || g_warp_smem_attr[dev] < smem_bytes)) {
       if (cudaFuncSetAttribute(forward_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes) != cudaSuccess) {
         delete p;
         return DEB_ERR_CUDA;
       }
+      if (dev >= 0 && dev < 64) g_warp_smem_attr[dev] = smem_bytes;
     }
   }
   const bool need_ws = mode == DEB_EXEC_LANE || !p->warp_smem;
@@ -391,6 +419,20 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** out) {
 int deb_plan_workspace_bytes(const deb_plan* p, size_t* bytes) {
   if (!p || !bytes) return DEB_ERR_INVALID;
   *bytes = p->ws_bytes;
+  return DEB_OK;
+}
+
+int deb_plan_launch_info(const deb_plan* p, deb_launch_cfg* cfg, int* modes_in_flight) {
+  if (!p || !cfg || !modes_in_flight) return DEB_ERR_INVALID;
+  if (p->exec_mode == DEB_EXEC_LANE) {
+    cfg->stage_vectors = DEB_STAGE_GLOBAL;
+    cfg->modes_per_sm = 0;
+    *modes_in_flight = p->lane_slots;
+  } else {
+    cfg->stage_vectors = (p->warp_smem && !p->warp_k_global) ? DEB_STAGE_SHARED : DEB_STAGE_GLOBAL;
+    cfg->modes_per_sm = p->warp_per_sm;
+    *modes_in_flight = p->warp_blocks;
+  }
   return DEB_OK;
 }
 

@@ -75,6 +75,26 @@ def perturbed_params(cosmo, theta=THETA, rel_step=1e-4):
     return out
 
 
+def _host_inputs(plist, backgrounds, pert, kmodes, aexp_out, nqmax, theta):
+    """Packed host arrays of one gradient problem (tables, output times, k,
+    cosmology index, eps per parameter, 1/A_s and ln(k/k_p) per mode)."""
+    nc, num_k = len(plist), kmodes.shape[0]
+    nominal = [b[0] for b in backgrounds]
+    sets = [b[1:] for b in backgrounds]
+    com = np.repeat(np.arange(nc, dtype=np.int32), num_k)
+    kp = np.array([p.get("k_p", 0.05) for p in plist], dtype=np.float64)[com]
+    As = np.array([p["A_s"] for p in plist], dtype=np.float64)[com]
+    k = np.tile(kmodes, nc)
+    return dict(
+        tab0=_tables.pack_batch(nominal, nqmax),
+        tau0=np.stack([_tables.tau_of_a(b, aexp_out) for b in nominal]),
+        tabs=_tables.pack_batch([q for st in sets for q in st], nqmax),
+        taus=np.stack([_tables.tau_of_a(q, aexp_out) for st in sets for q in st]),
+        k=k, com=com,
+        eps=np.ascontiguousarray(np.array([[e for (_, e, _, _) in pp] for pp in pert], dtype=np.float64)[com].T),
+        inv_As=(1.0 / As)[:, None], lnk=np.log(k / kp)[:, None])
+
+
 class GradientProblem:
     """Device-resident inputs, buffers and plan of one gradient launch pair.
 
@@ -82,12 +102,16 @@ class GradientProblem:
     [nominal, theta_1 + eps_1, theta_1 - eps_1, ...] (see
     :func:`perturbed_params`).  :meth:`run` enqueues the recorded nominal
     solve, the replay of every perturbed set, ``get_power`` and the
-    difference quotients on one stream, without synchronising.
+    difference quotients on one stream, without synchronising;
+    :meth:`capture` records that sequence once as a CUDA graph and
+    :meth:`replay` re-runs it; :meth:`load` copies the inputs of another
+    problem of the same shape into the same device buffers (through pinned
+    host memory), so one captured graph serves many calls.
     """
 
     def __init__(self, plist, backgrounds, pert, kmodes, aexp_out, *, lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, rtol, atol,
                  pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, max_steps=2048, idx=4,
-                 theta=THETA, step_to_outputs=False):
+                 theta=THETA, step_to_outputs=False, launch=None, linear_solver="structured"):
         import torch
 
         self.theta = tuple(theta)
@@ -95,25 +119,27 @@ class GradientProblem:
         self.kmodes = np.asarray(kmodes, dtype=np.float64)
         self.num_k = self.kmodes.shape[0]
         aexp_out = np.atleast_1d(np.asarray(aexp_out, dtype=np.float64))
+        self.aexp_out = aexp_out
+        self.nqmax = nqmax
         self.nout = aexp_out.shape[0]
         self.npar = len(pert[0])
         self.nset = 2 * self.npar
         self.idx = idx
-        nominal = [b[0] for b in backgrounds]
-        sets = [b[1:] for b in backgrounds]
-        self.host_tab0 = _tables.pack_batch(nominal, nqmax)
-        self.host_tau0 = np.stack([_tables.tau_of_a(b, aexp_out) for b in nominal])
-        self.host_tabs = _tables.pack_batch([q for st in sets for q in st], nqmax)
-        self.host_taus = np.stack([_tables.tau_of_a(q, aexp_out) for st in sets for q in st])
-        self.host_k = np.tile(self.kmodes, self.nc)
-        self.host_com = np.repeat(np.arange(self.nc, dtype=np.int32), self.num_k)
+        h = _host_inputs(plist, backgrounds, pert, self.kmodes, aexp_out, nqmax, self.theta)
+        self.host_tab0, self.host_tau0, self.host_tabs, self.host_taus = h["tab0"], h["tau0"], h["tabs"], h["taus"]
+        self.host_k, self.host_com = h["k"], h["com"]
         self.nmode = self.host_k.shape[0]
         dev = torch.device("cuda", torch.cuda.current_device())
         self.device = dev
-        T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a)).to(dev, dt)
-        self.d_tab0, self.d_tabs = T(self.host_tab0), T(self.host_tabs)
-        self.d_k, self.d_com = T(self.host_k), T(self.host_com, torch.int32)
-        self.d_tau0, self.d_taus = T(self.host_tau0), T(self.host_taus)
+        # pinned staging copies of every per-call input, and their device twins
+        self._names = ("tab0", "tau0", "tabs", "taus", "k", "com", "eps", "inv_As", "lnk")
+        self._pinned = {n: torch.from_numpy(np.ascontiguousarray(h[n])).pin_memory() for n in self._names}
+        self._dev = {n: self._pinned[n].to(dev) for n in self._names}
+        self.d_tab0, self.d_tabs = self._dev["tab0"], self._dev["tabs"]
+        self.d_k, self.d_com = self._dev["k"], self._dev["com"]
+        self.d_tau0, self.d_taus = self._dev["tau0"], self._dev["taus"]
+        self.eps_m = self._dev["eps"][:, :, None]     # [npar, nmode, 1]
+        self.d_inv_As, self.d_lnk = self._dev["inv_As"], self._dev["lnk"]
         self.rec_len = int(max_steps) + 1
         nm, ns, no = self.nmode, self.nset, self.nout
         self.d_rec = torch.empty((nm, self.rec_len), dtype=torch.float64, device=dev)
@@ -125,18 +151,61 @@ class GradientProblem:
         self.d_sts = torch.empty((ns * nm,), dtype=torch.int32, device=dev)
         self.d_P = torch.empty((nm, no), dtype=torch.float64, device=dev)
         self.d_dl = torch.empty((nm, no, len(self.theta)), dtype=torch.float64, device=dev)
-        eps = torch.as_tensor([[e for (_, e, _, _) in pp] for pp in pert], dtype=torch.float64, device=dev)
-        self.eps_m = eps[self.d_com.long()].t().contiguous()[:, :, None]     # [npar, nmode, 1]
         self.ode_names = [n for (n, _, _, _) in pert[0]]
-        kp = torch.as_tensor([p.get("k_p", 0.05) for p in plist], dtype=torch.float64, device=dev)[self.d_com.long()]
-        As = torch.as_tensor([p["A_s"] for p in plist], dtype=torch.float64, device=dev)[self.d_com.long()]
-        self.d_inv_As = (1.0 / As)[:, None]
-        self.d_lnk = torch.log(self.d_k / kp)[:, None]
-        dims = _pt._dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, no, False, "structured", "warp")
-        self.plan = _pt.get_plan(dims, ns * nm)
+        self.dims = _pt._dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, no, False, linear_solver, "warp")
+        self.plan = _pt.get_plan(self.dims, ns * nm, launch)
         self.cfg = _pt._cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps,
                             step_to_outputs=step_to_outputs)
-        self.order = T(_pt.schedule_order(self.host_k), torch.int32)
+        self.order = torch.as_tensor(_pt.schedule_order(self.host_k)).to(dev, torch.int32)
+        self.graph = None
+        self._copied = None
+        self.key = None
+
+    def load(self, plist, backgrounds, pert, stream=None):
+        """Copy the inputs of another set of cosmologies of the same shape
+        (same count, k-grid, output times count, table lengths) into this
+        problem's device buffers: host packing, then one pinned host-to-device
+        copy per input array on ``stream``.  Returns the bytes copied."""
+        import torch
+
+        h = _host_inputs(plist, backgrounds, pert, self.kmodes, self.aexp_out, self.nqmax, self.theta)
+        s = stream if stream is not None else torch.cuda.current_stream()
+        if self._copied is not None:
+            self._copied.synchronize()   # the previous load's copies have left the pinned buffers
+        nbytes = 0
+        with torch.cuda.stream(s):
+            for n in self._names:
+                a = np.ascontiguousarray(h[n])
+                if a.shape != tuple(self._pinned[n].shape):
+                    raise ValueError(f"load: input {n} has shape {a.shape}, the problem was built for "
+                                     f"{tuple(self._pinned[n].shape)}")
+                self._pinned[n].numpy()[...] = a
+                self._dev[n].copy_(self._pinned[n], non_blocking=True)
+                nbytes += a.nbytes
+            self._copied = torch.cuda.Event()
+            self._copied.record(s)
+        self.host_tab0, self.host_tau0, self.host_tabs, self.host_taus = h["tab0"], h["tau0"], h["tabs"], h["taus"]
+        return nbytes
+
+    def _record(self, plan, s):
+        L = _native.load()
+        c = lambda t: ctypes.c_void_p(t.data_ptr())
+        _native.check(_pt.launch_ordered(plan, self.order, self.nmode, lambda: L.deb_forward_record(
+            plan.ptr, c(self.d_tab0), self.nc, self.host_tab0.shape[1], c(self.d_k), c(self.d_com), self.nmode,
+            c(self.d_tau0), ctypes.byref(self.cfg), c(self.d_y0), c(self.d_st0), c(self.d_steps), c(self.d_rec),
+            self.rec_len, c(self.d_nrec), ctypes.c_void_p(s.cuda_stream))), "deb_forward_record")
+
+    def tune(self, candidates=None):
+        """Choose the launch shape by timing the nominal recorded solve with
+        each candidate (:mod:`autotune`); the replay uses the same kernel.
+        Returns {shape: ms}."""
+        from . import autotune
+
+        best, times = autotune.tune(self.dims, self.nset * self.nmode, self._record,
+                                    candidates or autotune.CANDIDATES)
+        self.plan = _pt.get_plan(self.dims, self.nset * self.nmode, best)
+        self.graph = None
+        return times
 
     def run(self, stream=None, events=None):
         import torch
@@ -147,10 +216,7 @@ class GradientProblem:
         sp = ctypes.c_void_p(s.cuda_stream)
         if events:
             events[0].record(s)
-        _native.check(_pt.launch_ordered(self.plan, self.order, self.nmode, lambda: L.deb_forward_record(
-            self.plan.ptr, c(self.d_tab0), self.nc, self.host_tab0.shape[1], c(self.d_k), c(self.d_com), self.nmode,
-            c(self.d_tau0), ctypes.byref(self.cfg), c(self.d_y0), c(self.d_st0), c(self.d_steps), c(self.d_rec),
-            self.rec_len, c(self.d_nrec), sp)), "deb_forward_record")
+        self._record(self.plan, s)
         if events:
             events[1].record(s)
         _native.check(L.deb_replay(self.plan.ptr, c(self.d_tabs), self.nc, self.nset, self.host_tabs.shape[1],
@@ -175,11 +241,74 @@ class GradientProblem:
                       "deb_get_power")
         return self.d_P, self.d_dl
 
+    def capture(self):
+        """Capture :meth:`run` (record launch, replay launch, get_power and
+        the difference quotients) as one CUDA graph.  Runs it once eagerly
+        first; synchronises."""
+        import torch
+
+        self.run()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run(torch.cuda.current_stream())
+        self.graph = g
+        return g
+
+    def replay(self, stream=None):
+        """Re-run the captured graph on ``stream`` (default: current)."""
+        import torch
+
+        if self.graph is None:
+            self.capture()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        with torch.cuda.stream(s):
+            self.graph.replay()
+        return self.d_P, self.d_dl
+
     def check(self):
         st0 = self.d_st0.cpu().numpy()
         sts = self.d_sts.cpu().numpy()
         if (st0 != 0).any() or (sts != 0).any():
             raise RuntimeError(f"{int((st0 != 0).sum())} nominal / {int((sts != 0).sum())} replayed mode(s) failed")
+
+
+_problems: dict = {}
+_MAX_CACHED = 2
+
+
+def _run_cached(plist, backgrounds, pert, kmodes, aexp_out, opts):
+    """Run one gradient problem, reusing device buffers and the captured CUDA
+    graph of an earlier call of the same shape: the first call of a shape
+    runs eagerly, the second captures the graph (its eager run gives the
+    results), later calls copy their inputs in and replay the graph."""
+    import torch
+
+    aexp = np.atleast_1d(np.asarray(aexp_out, dtype=np.float64))
+    key = (torch.cuda.current_device(), len(plist), np.asarray(kmodes, dtype=np.float64).tobytes(), aexp.shape[0],
+           tuple(sorted(opts.items())), tuple(n for (n, _, _, _) in pert[0]))
+    gp = _problems.get(key)
+    if gp is not None:
+        try:
+            gp.load(plist, backgrounds, pert)
+        except ValueError:      # table lengths differ: not the same shape after all
+            gp = None
+            _problems.pop(key, None)
+    if gp is None:
+        gp = GradientProblem(plist, backgrounds, pert, kmodes, aexp_out, **opts)
+        gp.calls = 0
+        while len(_problems) >= _MAX_CACHED:
+            _problems.pop(next(iter(_problems)))
+        _problems[key] = gp
+    gp.calls += 1
+    if gp.calls == 1:
+        Pd, Dd = gp.run()
+    elif gp.graph is None:
+        gp.capture()
+        Pd, Dd = gp.d_P, gp.d_dl
+    else:
+        Pd, Dd = gp.replay()
+    return Pd, Dd, gp
 
 
 def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num_k: int, lmaxg: int = 11,
@@ -214,11 +343,10 @@ def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num
                 flat += [a, b]
         ev = evolve_backgrounds(flat, processes)
         backgrounds = [ev[i * (nset + 1):(i + 1) * (nset + 1)] for i in range(nc)]
-    gp = GradientProblem(plist, backgrounds, pert, kmodes, aexp_out, lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr,
-                         lmaxnu=lmaxnu, nqmax=nqmax, rtol=rtol, atol=atol, pcoeff=pcoeff, icoeff=icoeff, dcoeff=dcoeff,
-                         factormax=factormax, factormin=factormin, max_steps=max_steps, idx=idx, theta=theta,
-                         step_to_outputs=step_to_outputs)
-    Pd, Dd = gp.run()
+    opts = dict(lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr, lmaxnu=lmaxnu, nqmax=nqmax, rtol=rtol, atol=atol,
+                pcoeff=pcoeff, icoeff=icoeff, dcoeff=dcoeff, factormax=factormax, factormin=factormin,
+                max_steps=max_steps, idx=idx, theta=tuple(theta), step_to_outputs=step_to_outputs)
+    Pd, Dd, gp = _run_cached(plist, backgrounds, pert, kmodes, aexp_out, opts)
     if throw:
         gp.check()
     nout = gp.nout

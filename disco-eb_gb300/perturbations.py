@@ -22,6 +22,7 @@ import ctypes
 import numpy as np
 
 from . import _native
+from . import autotune as _autotune
 from . import tables as _tables
 
 _plans: dict = {}
@@ -85,17 +86,23 @@ def launch_ordered(plan, order, nmode: int, fn):
             L.deb_plan_set_order(plan.ptr, None, 0)
 
 
-def get_plan(dims: _native.DebDims, nmode: int) -> _native.Plan:
-    """Cached plan for these hierarchy sizes with room for >= nmode modes."""
+def get_plan(dims: _native.DebDims, nmode: int, launch=None) -> _native.Plan:
+    """Cached plan for these hierarchy sizes with room for >= nmode modes.
+
+    ``launch`` = (stage vectors, modes-per-SM cap) overrides the launch shape;
+    by default the shape :mod:`autotune` chose for these sizes is used, else
+    the library's default."""
     torch = _torch()
+    if launch is None:
+        launch = _autotune.chosen(dims)
     key = (torch.cuda.current_device(), dims.lmaxg, dims.lmaxgp, dims.lmaxr, dims.lmaxnu, dims.nqmax, dims.nout,
-           dims.return_full, dims.linear_solver, dims.exec_mode)
+           dims.return_full, dims.linear_solver, dims.exec_mode, launch)
     p = _plans.get(key)
     # an automatic plan is re-made when the batch size moves it across the
     # lane/warp threshold (the execution mode is fixed at plan creation)
     if p is None or p.max_modes < nmode or (dims.exec_mode == 0 and p.max_modes > 4 * max(nmode, 1)):
         _plans.pop(key, None)
-        p = _native.Plan(dims, max(nmode, 1))
+        p = _native.Plan(dims, max(nmode, 1), launch)
         _plans[key] = p
     return p
 
@@ -155,6 +162,49 @@ class DeviceProblem:
             self.nmode, ctypes.c_void_p(self.tau_out.data_ptr()), ctypes.byref(cfg), ctypes.c_void_p(self.y.data_ptr()),
             ctypes.c_void_p(self.status.data_ptr()), ctypes.c_void_p(self.steps.data_ptr()), ctypes.c_void_p(s.cuda_stream)))
         _native.check(rc, "deb_forward")
+
+    def tune(self, cfg: _native.DebSolverCfg, candidates=_autotune.CANDIDATES):
+        """Time this problem's launch for each candidate launch shape
+        (:mod:`autotune`), keep the fastest plan; returns {shape: ms}."""
+        if self.dims.exec_mode == _native.EXEC_MODES["lane"] or self.nmode == 0:
+            return {}
+        L = _native.load()
+
+        def launch(plan, s):
+            _native.check(launch_ordered(plan, self.order, self.nmode, lambda: L.deb_forward(
+                plan.ptr, ctypes.c_void_p(self.tables.data_ptr()), self.ncosmo, self.blob_len,
+                ctypes.c_void_p(self.k.data_ptr()),
+                ctypes.c_void_p(self.cosmo.data_ptr() if self.cosmo is not None else 0), self.nmode,
+                ctypes.c_void_p(self.tau_out.data_ptr()), ctypes.byref(cfg), ctypes.c_void_p(self.y.data_ptr()),
+                ctypes.c_void_p(self.status.data_ptr()), ctypes.c_void_p(self.steps.data_ptr()),
+                ctypes.c_void_p(s.cuda_stream))), "deb_forward")
+
+        best, times = _autotune.tune(self.dims, self.nmode, launch, candidates)
+        self.plan = get_plan(self.dims, self.nmode, best)
+        return times
+
+    def capture(self, cfg: _native.DebSolverCfg, idx: int = 4):
+        """Capture the whole solve (queue reset, the persistent launch and
+        get_power) as one CUDA graph; :meth:`replay` re-runs it on the
+        current stream with whatever the input buffers hold and returns the
+        graph's P(k) buffer [nmode, nout].  Runs the solve once eagerly
+        first (its y, status and steps are left in place) and returns that
+        run's P(k); the capture itself executes nothing."""
+        torch = _torch()
+        self.launch(cfg)                  # untimed launch outside the capture
+        P = self.power(idx)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            s = torch.cuda.current_stream()
+            self.launch(cfg, s)
+            self.graph_P = self.power(idx, s)
+        self.graph = g
+        return P
+
+    def replay(self):
+        self.graph.replay()
+        return self.graph_P
 
     def power(self, idx: int, stream=None):
         """P(k) of field ``idx`` for every mode and output, on the device."""

@@ -114,6 +114,28 @@ int deb_plan_create(const deb_dims* dims, int max_modes, deb_plan** plan);
 int deb_plan_workspace_bytes(const deb_plan* plan, size_t* bytes);
 
 /*
+ * Launch shape of the warp-per-mode kernel, no reference counterpart (the
+ * reference's vmap has no launch shape).  A mode's state is 16 vectors of
+ * nvar doubles plus a small block; the first 8 vectors and the block always
+ * live in shared memory, the 8 Rodas5 stage vectors either there too
+ * (DEB_STAGE_SHARED: 44 KB per mode at nvar 323, 5 modes per SM) or in an
+ * L2-resident global array (DEB_STAGE_GLOBAL: 24 KB of shared memory per
+ * mode, up to 8 modes per SM, each stage access an L2 round trip).
+ * modes_per_sm caps the modes in flight per SM (0: as many as fit).  Which
+ * shape is faster depends on the hierarchy sizes; discoeb_gb300.autotune
+ * times the candidates and picks one.  deb_plan_create uses
+ * {DEB_STAGE_AUTO, 0}: shared when two modes fit per SM, else global.
+ */
+enum deb_stage_vectors { DEB_STAGE_AUTO = 0, DEB_STAGE_SHARED = 1, DEB_STAGE_GLOBAL = 2 };
+typedef struct deb_launch_cfg {
+  int stage_vectors;   /* enum deb_stage_vectors */
+  int modes_per_sm;    /* cap on modes in flight per SM, 0 = no cap */
+} deb_launch_cfg;
+int deb_plan_create_ex(const deb_dims* dims, int max_modes, const deb_launch_cfg* launch, deb_plan** plan);
+/* The shape a plan resolved to, and its modes in flight (resident warps). */
+int deb_plan_launch_info(const deb_plan* plan, deb_launch_cfg* launch, int* modes_in_flight);
+
+/*
  * Scheduling hint, no reference counterpart.  The kernel hands modes to its
  * warps through a device-side queue; a launch ends when its last mode ends,
  * and step counts differ by 60x across k, so handing out the most expensive
