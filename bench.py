@@ -187,6 +187,11 @@ def cpu_baseline(inp, seconds=20.0, threads=0):
                       + (", x13 solves per cosmology for the 6 ODE gradients (+-eps) and the nominal P(k)" if solves > 1 else "")}
 
 
+def _launch_arg(text):
+    where, _, per_sm = text.partition("/")
+    return (where, int(per_sm or 0))
+
+
 def l2_flush_buffer():
     """256 MB device buffer written before every timed step (L2 is 129 MB), so
     no step starts with the previous step's tables or outputs in L2."""
@@ -234,7 +239,9 @@ def run_ours(args):
     cfg = pt._cfg(inp["rtol"], inp["atol"], 0.25, 0.80, 0.0, 20.0, 0.3, args.max_steps)
     stream = torch.cuda.current_stream()
 
-    tune_ms = prob.tune(cfg) if args.tune else {}
+    if args.launch:
+        prob.plan = pt.get_plan(prob.dims, prob.nmode, _launch_arg(args.launch))
+    tune_ms = prob.tune(cfg) if args.tune and not args.launch else {}
     launch = prob.plan.launch_info()
     for _ in range(args.warmup):
         prob.launch(cfg, stream)
@@ -336,7 +343,9 @@ def run_gradient(args, inp, world, rank, local):
     gp = GradientProblem(inp["params"], inp["bgs"], inp["pert"], inp["kgrid"], inp["aexp"], rtol=inp["rtol"],
                          atol=inp["atol"], max_steps=args.max_steps, step_to_outputs=inp["step_ts"], **dims)
     stream = torch.cuda.current_stream()
-    tune_ms = gp.tune() if args.tune else {}
+    if args.launch:
+        gp.plan = pt.get_plan(gp.dims, gp.nset * gp.nmode, _launch_arg(args.launch))
+    tune_ms = gp.tune() if args.tune and not args.launch else {}
     launch = gp.plan.launch_info()
     # eager warm-up steps, timed per launch for the record / replay split
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(max(1, args.warmup))]
@@ -399,8 +408,33 @@ def run_gradient(args, inp, world, rank, local):
         P, D, _ = e2e_call()
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / e2e_steps
-    h2d = (gp.host_tab0.nbytes + gp.host_tabs.nbytes + gp.host_tau0.nbytes + gp.host_taus.nbytes + gp.host_k.nbytes
-           + gp.host_com.nbytes)
+
+    # the same from the parameters alone: the tables of all 13 sets per cosmology produced on the GPU
+    def e2e_params_call():
+        return deb.evolve_perturbations_grad(params=inp["params"], aexp_out=inp["aexp"], kmin=inp["kgrid"][0],
+                                             kmax=inp["kgrid"][-1], num_k=inp["num_k"], rtol=inp["rtol"],
+                                             atol=inp["atol"], max_steps=args.max_steps, tables="gpu",
+                                             step_to_outputs=inp["step_ts"], **dims)
+
+    e2e_params_call()
+    e2e_params_call()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_params_call()
+    torch.cuda.synchronize()
+    t_e2e_params = (time.perf_counter() - t0) / e2e_steps
+    from discoeb_gb300 import gradient as _grad, tables_gpu
+
+    gpp = [g for g in _grad._problems.values() if g.gpu_tables][0]
+    # table production alone, all 13 sets per cosmology (two producer launches)
+    te0, te1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    te0.record(stream)
+    gpp.load(inp["params"], "gpu", inp["pert"])
+    te1.record(stream)
+    torch.cuda.synchronize()
+    tables_ms = te0.elapsed_time(te1)
+    h2d = gp.input_bytes()
     d2h = int(P.nbytes + D.nbytes) + 4 * (gp.nmode * (1 + gp.nset))
 
     peak = _native.measure_fp64_peak(stream.cuda_stream)
@@ -422,11 +456,18 @@ def run_gradient(args, inp, world, rank, local):
                    "gradient": "central differences over the replayed nominal step sequence (jacfwd semantics)",
                    "cuda_graph": "record + replay + get_power + quotients captured once, replayed per step",
                    "launch_shape": launch, "autotune_ms": {f"{a}/{b}": round(v, 2) for (a, b), v in tune_ms.items()},
-                   "l2": "flushed before every timed step (256 MB write); tables %.1f MB read per step" % ((gp.host_tab0.nbytes + gp.host_tabs.nbytes) / 1e6),
+                   "l2": "flushed before every timed step (256 MB write); tables %.1f MB read per step" % ((gp.d_tab0.numel() + gp.d_tabs.numel()) * 8 / 1e6),
                    "aexp_out": inp["aexp"], "cosmology": inp["cosmo_kind"], "step_to_outputs": inp["step_ts"],
                    "redrawn_cosmologies": inp["rejected"]},
         "e2e": {"value": total_cosmo / t_e2e if world == 1 else None, "unit": "cosmology solves/s (P(k) + 8-parameter gradient)",
-                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "inputs": "host tables of the 13 parameter sets per cosmology (evolve_background output), packed per call"},
+        "e2e_from_params": {"value": total_cosmo / t_e2e_params if world == 1 else None,
+                            "unit": "cosmology solves/s (P(k) + 8-parameter gradient)",
+                            "h2d_bytes_per_step": int(gpp.input_bytes()), "d2h_bytes_per_step": int(d2h),
+                            "inputs": "parameter dicts only; background + RECFAST tables of all 13 sets per cosmology "
+                                      "produced on the GPU inside the timed call",
+                            "gpu_table_production_ms": tables_ms},
         "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
                      "note": "FP64-pipe bound (state in shared memory); peak = FP64 FMA microkernel measured in this run; "
@@ -515,45 +556,6 @@ def run_accuracy(args):
     print(json.dumps(out))
 
 
-def run_plain(args):
-    """The plain single-cosmology FP64 GPU form of the gradient workload, the
-    denominator the batched form is compared with: the reference's own
-    method on the GPU -- dense W = I/(gamma h) - J formed every step and
-    factored by FP64 LU with partial pivoting (O(n^3), as lu_factor in
-    ode_integrators_stiff.py:772-780) -- one cosmology (the workload's
-    first) per launch pair, record + replay of its 12 theta +- eps sets.
-    One untimed 2-mode launch first, then one timed pair.  Prints one JSON
-    line (not a bench line)."""
-    import torch
-
-    from discoeb_gb300.gradient import GradientProblem
-
-    torch.cuda.set_device(0)
-    inp = make_inputs(args.workload, 0, 1)
-    if not inp["grad"]:
-        raise SystemExit("--plain needs a gradient workload")
-    dims = inp["dims"]
-    kw = dict(rtol=inp["rtol"], atol=inp["atol"], max_steps=args.max_steps, step_to_outputs=inp["step_ts"],
-              linear_solver="dense", **dims)
-    warm = GradientProblem(inp["params"][:1], inp["bgs"][:1], inp["pert"][:1], inp["kgrid"][:2], inp["aexp"], **kw)
-    warm.run()
-    torch.cuda.synchronize()
-    gp = GradientProblem(inp["params"][:1], inp["bgs"][:1], inp["pert"][:1], inp["kgrid"], inp["aexp"], **kw)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    with ClockSampler(0) as clk:
-        gp.run(torch.cuda.current_stream(), ev)
-        torch.cuda.synchronize()
-    gp.check()
-    rec_ms, rep_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
-    print(json.dumps({
-        "form": "plain single-cosmology FP64 GPU form (dense LU per step, reference method)",
-        "workload": args.workload, "num_k": inp["num_k"], "replay_items": gp.nmode * gp.nset,
-        "record_ms": rec_ms, "replay_ms": rep_ms,
-        "value": 1e3 / (rec_ms + rep_ms), "forward_value": 1e3 / rec_ms,
-        "unit": "cosmology solves/s (P(k) + 8-parameter gradient); forward_value: P(k) only",
-        "attempted_steps": int(gp.d_steps.sum().item()), "clocks": clk.summary()}))
-
-
 def run_reference(args):
     world, rank, local = _dist()
     if rank != 0:
@@ -593,17 +595,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--exec-mode", default="auto", choices=["auto", "lane", "warp"])
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="skip the launch-shape autotuner")
+    ap.add_argument("--launch", default=None,
+                    help="fixed launch shape STAGE/MODES_PER_SM (e.g. global/8, shared/5) instead of the autotuner")
     ap.add_argument("--accuracy", action="store_true", help="print the error against tight oracle solves instead")
-    ap.add_argument("--plain", action="store_true",
-                    help="time the plain single-cosmology FP64 dense-LU GPU form of the workload instead")
     ap.add_argument("--accuracy-modes", type=int, default=8)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.accuracy:
         run_accuracy(args)
-    elif args.plain:
-        run_plain(args)
     else:
         run_ours(args)
 

@@ -38,8 +38,9 @@ class DebSolverCfg(ctypes.Structure):
 
 
 _lib = None
-EXPORTS = ("deb_nvar", "deb_plan_create", "deb_plan_create_ex", "deb_plan_launch_info", "deb_plan_workspace_bytes", "deb_plan_set_order", "deb_forward",
-           "deb_forward_static",
+EXPORTS = ("deb_nvar", "deb_plan_create", "deb_plan_create_ex", "deb_plan_launch_info", "deb_plan_workspace_bytes",
+           "deb_plan_set_order", "deb_forward", "deb_forward_static", "deb_tables_blob_len", "deb_evolve_background",
+           "deb_tau_of_a", "deb_plan_create_grouped", "deb_forward_grouped",
            "deb_forward_record", "deb_replay", "deb_get_power", "deb_power_multipoles", "deb_density_velocity",
            "deb_power_kaiser", "deb_savgol_log", "deb_fftlog_phase",
            "deb_plan_destroy", "deb_measure_fp64_peak", "deb_error_string", "deb_version")
@@ -79,6 +80,11 @@ def load(path: str | None = None):
     L.deb_power_kaiser.argtypes = [vp, vp, ci, vp, ci, cd, vp, vp]
     L.deb_savgol_log.argtypes = [vp, ci, ci, vp, ci, vp, vp]
     L.deb_fftlog_phase.argtypes = [ci, cd, ci, vp, vp]
+    L.deb_plan_create_grouped.argtypes = [ctypes.POINTER(DebDims), ci, ci, ctypes.POINTER(vp)]
+    L.deb_forward_grouped.argtypes = [vp, vp, ci, ci, vp, vp, ci, vp, ctypes.POINTER(DebSolverCfg), vp, vp, vp, vp]
+    L.deb_tables_blob_len.argtypes = [ci, ci, ci]
+    L.deb_evolve_background.argtypes = [vp, vp, ci, vp, vp, vp, ci, vp, vp]
+    L.deb_tau_of_a.argtypes = [vp, ci, ci, vp, ci, vp, vp]
     L.deb_plan_destroy.argtypes = [vp]
     L.deb_plan_destroy.restype = None
     L.deb_measure_fp64_peak.argtypes = [ctypes.POINTER(ctypes.c_double), vp]
@@ -97,12 +103,17 @@ def check(rc: int, what: str):
 class Plan:
     """Owns one deb_plan (device workspace sized for max_modes)."""
 
-    def __init__(self, dims: DebDims, max_modes: int, launch: tuple[str, int] | None = None):
-        """``launch`` = (stage vectors "auto" | "shared" | "global", modes per SM cap or 0)."""
+    def __init__(self, dims: DebDims, max_modes: int, launch: tuple[str, int] | None = None, batch_size: int = 0):
+        """``launch`` = (stage vectors "auto" | "shared" | "global", modes per SM cap or 0);
+        ``batch_size`` > 0 makes a grouped plan (deb_plan_create_grouped)."""
         self.dims = dims
         self.max_modes = max_modes
+        self.batch_size = batch_size
         self.ptr = ctypes.c_void_p()
-        if launch is None:
+        if batch_size > 0:
+            check(load().deb_plan_create_grouped(ctypes.byref(dims), int(max_modes), int(batch_size),
+                                                 ctypes.byref(self.ptr)), "deb_plan_create_grouped")
+        elif launch is None:
             check(load().deb_plan_create(ctypes.byref(dims), int(max_modes), ctypes.byref(self.ptr)), "deb_plan_create")
         else:
             lc = DebLaunchCfg(STAGE_VECTORS[launch[0]], int(launch[1]))

@@ -6,7 +6,8 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-SRC = [os.path.join(HERE, "csrc", "deb_solver.cu"), os.path.join(HERE, "csrc", "deb_observables.cu")]
+SRC = [os.path.join(HERE, "csrc", "deb_solver.cu"), os.path.join(HERE, "csrc", "deb_observables.cu"),
+       os.path.join(HERE, "csrc", "deb_tables.cu")]
 DEPS = SRC + [os.path.join(HERE, "csrc", "deb_core.cuh"), os.path.join(ROOT, "include", "discoeb_gb300.h")]
 OUT = os.path.join(HERE, "_build", "libdiscoeb_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"

@@ -1410,18 +1410,27 @@ HD double replay_time(const Run& r, const double* tau_out, int j) {
   return v < 0.0 ? LDG(tau_out + (int)(-v) - 1) : v * r.scale;
 }
 
-// start a mode: start time, ICs, first step size (perturbations.py:742-756)
+// start time of one mode: 0.99 min(min tau_out, determine_starting_time)
+// (perturbations.py:742-743)
+HD double mode_start(const Cosmo& c, const ModeConst& m, const Ctl& ctl, const double* tau_out) {
+  double tmin = LDG(tau_out);
+  for (int o = 1; o < ctl.nout; ++o) { const double t = LDG(tau_out + o); tmin = t < tmin ? t : tmin; }
+  const double ts = start_time(c, m);
+  return 0.99 * (tmin < ts ? tmin : ts);
+}
+
+// start a mode: start time, ICs, first step size (perturbations.py:742-756);
+// t0_forced > 0 starts it at that time instead (a group's common start)
 template <int G>
 HD void mode_begin(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Ctl& ctl, const WS<G>& w,
-                   const double* tau_out, Run& r) {
-  double tmax = LDG(tau_out), tmin = tmax;
-  for (int o = 1; o < ctl.nout; ++o) { const double t = LDG(tau_out + o); tmax = t > tmax ? t : tmax; tmin = t < tmin ? t : tmin; }
+                   const double* tau_out, Run& r, double t0_forced = -1.0) {
+  double tmax = LDG(tau_out);
+  for (int o = 1; o < ctl.nout; ++o) { const double t = LDG(tau_out + o); tmax = t > tmax ? t : tmax; }
   // start time of this table set.  In a replay the recorded step times are
   // scaled by tau_start / nominal tau_start: with the step-size factors
   // frozen every step length is proportional to dt0 = tau_start / 4, which
   // is how jax.jacfwd sees the diffrax step sequence.
-  const double ts = start_time(c, m);
-  const double t0 = 0.99 * (tmin < ts ? tmin : ts);
+  const double t0 = t0_forced > 0.0 ? t0_forced : mode_start(c, m, ctl, tau_out);
   initial_conditions<G>(gp, c, m, D, t0, w, V_Y);
   r.t0 = t0; r.T1 = tmax;
   r.t1_out = -1;
@@ -1473,13 +1482,13 @@ HD void stage_prep(const Grp<G>& gp, const Rodas& R, const WS<G>& w, int n, int 
   }
 }
 
-// One attempted Rodas5 step (ode_integrators_stiff.py:718-834) plus the PID
-// decision.  Returns true while the mode still needs steps.
+// One attempted Rodas5 step (ode_integrators_stiff.py:718-834): the eight
+// stages from (r.t0, y0) over r.t1 - r.t0, y1 = u + k8 into the stage state
+// vector.  Returns the sum of squares of the six scaled error entries of the
+// PID norm (perturbations.py:701-705, 759-760); bad = y1 not finite.
 template <int G>
-HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, const Rodas& R,
-                  const Ctl& ctl, const WS<G>& w, const double* tau_out, double* yout, long ostride, Run& r) {
-  if (!(r.t0 < r.T1)) return false;
-  if (r.steps >= ctl.max_steps) { r.status = ST_MAX_STEPS; return false; }
+HD double step_attempt(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T,
+                       const Rodas& R, const Ctl& ctl, const WS<G>& w, const Run& r, bool& bad_out) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
   const double t0 = r.t0, dt = r.t1 - r.t0;
   const int vy = r.vy, vu = r.vu;
@@ -1544,7 +1553,20 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
     const double sc = w.v(vk8, j) * rcp(ctl.atol + (y0 > y1 ? y0 : y1) * ctl.rtol) * ew[q];
     ss += sc * sc;
   }
-  const double err = ctl.replay ? 0.0 : sqrt(ss / 6.0);
+  bad_out = bad;
+  return ss;
+}
+
+// The PID decision on an attempted step with error norm err (computed over
+// this mode, or over a group of modes sharing one step sequence), SaveAt
+// outputs inside an accepted step, and the next step.  Returns true while
+// the mode still needs steps.
+template <int G>
+HD bool step_decide(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Ctl& ctl,
+                    const WS<G>& w, const double* tau_out, double* yout, long ostride, Run& r, double err, bool bad) {
+  const int n = D.n;
+  const double dt = r.t1 - r.t0;
+  const int vy = r.vy, vu = r.vu, vy1 = vu;
   ++r.steps;
   if (!isfinite_(err) || (ctl.replay && bad)) { r.status = ST_NONFINITE; return false; }
   const bool keep = ctl.replay ? true : err < 1.0;
@@ -1609,6 +1631,75 @@ HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Di
   if (!(tn > r.t0) && r.t0 < r.T1) { r.status = ST_DT_UNDERFLOW; return false; }
   r.t1 = tn;
   return r.t0 < r.T1;
+}
+
+// One attempted step of one mode plus its PID decision.  Returns true while
+// the mode still needs steps.
+template <int G>
+HD bool mode_step(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T, const Rodas& R,
+                  const Ctl& ctl, const WS<G>& w, const double* tau_out, double* yout, long ostride, Run& r) {
+  if (!(r.t0 < r.T1)) return false;
+  if (r.steps >= ctl.max_steps) { r.status = ST_MAX_STEPS; return false; }
+  bool bad;
+  const double ss = step_attempt<G>(gp, c, m, D, T, R, ctl, w, r, bad);
+  const double err = ctl.replay ? 0.0 : sqrt(ss / 6.0);
+  return step_decide<G>(gp, c, m, D, ctl, w, tau_out, yout, ostride, r, err, bad);
+}
+
+// One mode of a group as group_solve sees it.
+template <int G>
+struct ModeCtx {
+  Cosmo c;
+  ModeConst m;
+  WS<G> w;
+  const double* tau_out;
+  double* yout;
+};
+
+// B <= 32 modes sharing one step sequence: the reference's batched variant
+// (evolve_modes_batched, perturbations.py:835-922, with Rodas5Batched,
+// ode_integrators_stiff.py:846-1010).  The modes start together at the
+// smallest of their start times (determine_start_times_per_batch,
+// perturbations.py:786-803), take the same steps, and the PID controller
+// sees one error norm: the RMS over the six filtered entries of every mode
+// (rms_norm_filtered_batched, perturbations.py:690-694).  ctx(b) returns
+// mode b's ModeCtx; its outputs follow the same SaveAt rule as one mode's.
+// r ends with the group's status and step counts.
+template <int G, class CtxFn>
+HD void group_solve(const Grp<G>& gp, const Dims& D, const Tab& T, const Rodas& R, const Ctl& ctl, int B, CtxFn ctx,
+                    long ostride, Run& r) {
+  double t0 = 1e300;
+  for (int b = 0; b < B; ++b) {
+    const ModeCtx<G> x = ctx(b);
+    const double ts = mode_start(x.c, x.m, ctl, x.tau_out);
+    t0 = ts < t0 ? ts : t0;
+  }
+  for (int b = 0; b < B; ++b) {
+    const ModeCtx<G> x = ctx(b);
+    mode_begin<G>(gp, x.c, x.m, D, ctl, x.w, x.tau_out, r, t0);
+  }
+  for (;;) {
+    if (!(r.t0 < r.T1)) break;
+    if (r.steps >= ctl.max_steps) { r.status = ST_MAX_STEPS; break; }
+    double ss = 0.0;
+    unsigned badm = 0u;
+    for (int b = 0; b < B; ++b) {
+      const ModeCtx<G> x = ctx(b);
+      bool bad;
+      ss += step_attempt<G>(gp, x.c, x.m, D, T, R, ctl, x.w, r, bad);
+      if (bad) badm |= 1u << b;
+    }
+    const double err = sqrt(ss / (6.0 * B));
+    const Run r0 = r;
+    bool more = false;
+    for (int b = 0; b < B; ++b) {
+      const ModeCtx<G> x = ctx(b);
+      Run rb = r0;
+      more = step_decide<G>(gp, x.c, x.m, D, ctl, x.w, x.tau_out, x.yout, ostride, rb, err, ((badm >> b) & 1u) != 0u);
+      if (b == B - 1) r = rb;
+    }
+    if (!more) break;
+  }
 }
 
 HD void fill_tables(Tab& T) {

@@ -180,6 +180,63 @@ __global__ void __launch_bounds__(32) forward_warp_kernel(KParams P) {
   }
 }
 
+// Groups of B consecutive modes sharing one step sequence (the reference's
+// batched variant): one warp per group, taken from the queue; the group's B
+// slots live in global memory and the warp steps its modes one after the
+// other inside each shared step (deb::group_solve).  A group whose modes are
+// not all valid or not all of one cosmology is marked BAD_INPUT.
+__global__ void __launch_bounds__(32) forward_group_kernel(KParams P, int B) {
+  const int lane = threadIdx.x & 31;
+  const long gwarp = blockIdx.x;
+  const deb::Grp<32> gp{lane};
+  const int osz = P.ctl.return_full ? P.D.n : DEB_NOUT_FIELDS;
+  const int ngroup = P.nmode / B;
+  for (;;) {
+    int q = 0;
+    if (lane == 0) q = atomicAdd(P.queue, 1);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    if (q >= ngroup) break;
+    const int m0 = q * B;
+    const int ci = P.cosmo ? P.cosmo[m0] : 0;
+    bool ok = ci >= 0 && ci < P.ncosmo;
+    for (int b = 0; b < B; ++b) {
+      const int m = m0 + b;
+      const double k = P.k[m];
+      ok = ok && (P.cosmo ? P.cosmo[m] : 0) == ci && k > 0.0 && isfinite(k);
+      double* dst = P.y_out + (long)m * P.ctl.nout * osz;
+      for (int i = lane; i < P.ctl.nout * osz; i += 32) dst[i] = __longlong_as_double(0x7ff8000000000000LL);
+    }
+    deb::Cosmo c0;
+    if (ok) ok = deb::load_cosmo(P.tables + (long)ci * P.blob_len, P.blob_len, c0) && c0.nq == P.D.nq;
+    deb::Run run;
+    run.rec = nullptr; run.rec_cap = 0; run.nrec = 0; run.acc = 0; run.rej = 0; run.status = deb::ST_BAD_INPUT;
+    if (ok) {
+      const double* tau_out = P.tau_out + (long)ci * P.ctl.nout;
+      auto ctx = [&](int b) {
+        deb::ModeCtx<32> x;
+        x.c = c0;
+        deb::mode_const(c0, P.k[m0 + b], x.m);
+        x.w.p = P.ws + (gwarp * B + b) * P.slot_len;
+        x.w.n = P.D.n;
+        x.w.misc0 = deb::V_K0 * P.D.n;
+        x.w.kp = x.w.p + deb::hot_len(P.D);
+        x.w.dp = nullptr;
+        x.tau_out = tau_out;
+        x.yout = P.y_out + (long)(m0 + b) * P.ctl.nout * osz;
+        return x;
+      };
+      deb::group_solve<32>(gp, P.D, c_tab, c_rodas, P.ctl, B, ctx, 1, run);
+    }
+    if (lane == 0)
+      for (int b = 0; b < B; ++b) {
+        const int m = m0 + b;
+        P.status[m] = run.status;
+        if (P.steps) { P.steps[2 * m] = run.acc; P.steps[2 * m + 1] = run.rej; }
+      }
+    __syncwarp();
+  }
+}
+
 __global__ void power_kernel(const double* tables, int ncosmo, int blob_len, const double* k, const int* cosmo, int nmode,
                              int nout, const double* y, int stride, int idx, double* P) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -258,6 +315,8 @@ struct deb_plan {
   int lane_blocks, lane_slots;
   // warp mode
   int warp_block_warps, warp_blocks, warp_smem, warp_k_global, warp_per_sm;
+  // grouped plans (deb_plan_create_grouped): modes per group, warps in flight
+  int group_size, group_warps;
   long warp_smem_bytes;
   double* kws;      // warp mode: stage vectors in global memory
   double* ws;       // lane slots (or warp slots when shared memory is too small)
@@ -422,9 +481,55 @@ int deb_plan_workspace_bytes(const deb_plan* p, size_t* bytes) {
   return DEB_OK;
 }
 
+int deb_plan_create_grouped(const deb_dims* dims, int max_modes, int batch_size, deb_plan** out) {
+  if (!dims || !out || max_modes <= 0 || batch_size < 1 || batch_size > 32) return DEB_ERR_INVALID;
+  *out = nullptr;
+  if (dims->linear_solver != DEB_SOLVE_STRUCTURED || dims->return_full) return DEB_ERR_INVALID;
+  if (dims->lmaxg < 3 || dims->lmaxgp < 3 || dims->lmaxr < 3 || dims->lmaxnu < 3 || dims->nqmax < 1 || dims->nout < 1)
+    return DEB_ERR_INVALID;
+  if (dims->lmaxg > deb::LMAX_TABLE || dims->lmaxgp > deb::LMAX_TABLE || dims->lmaxr > deb::LMAX_TABLE ||
+      dims->lmaxnu > deb::LMAX_TABLE)
+    return DEB_ERR_INVALID;
+  int rc = upload_constants();
+  if (rc) return rc;
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return DEB_ERR_CUDA;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return DEB_ERR_CUDA;
+  deb_plan* p = new deb_plan();
+  p->D = deb::make_dims(dims->lmaxg, dims->lmaxgp, dims->lmaxr, dims->lmaxnu, dims->nqmax);
+  p->dense = 0;
+  p->return_full = 0;
+  p->nout = dims->nout;
+  p->exec_mode = DEB_EXEC_WARP;
+  p->max_modes = max_modes;
+  p->nsm = nsm;
+  p->slot_len = deb::slot_len(p->D);
+  p->dense_len = 0;
+  p->group_size = batch_size;
+  const long groups = ((long)max_modes + batch_size - 1) / batch_size;
+  long warps = (long)nsm * kMaxWarpBlocksPerSM;
+  const long mem_cap = (16L << 30) / (p->slot_len * 8 * batch_size);
+  if (warps > mem_cap) warps = mem_cap;
+  if (warps > groups) warps = groups;
+  if (warps < 1) { delete p; return DEB_ERR_NOMEM; }
+  p->group_warps = (int)warps;
+  p->ws_bytes = (size_t)warps * batch_size * p->slot_len * sizeof(double);
+  if (cudaMalloc(&p->ws, p->ws_bytes) != cudaSuccess) { delete p; return DEB_ERR_NOMEM; }
+  if (cudaMalloc(&p->queue, sizeof(int) * 4) != cudaSuccess) { cudaFree(p->ws); delete p; return DEB_ERR_NOMEM; }
+  if (cudaMalloc(&p->order_dev, sizeof(int)) != cudaSuccess) {
+    cudaFree(p->ws); cudaFree(p->queue); delete p; return DEB_ERR_NOMEM;
+  }
+  *out = p;
+  return DEB_OK;
+}
+
 int deb_plan_launch_info(const deb_plan* p, deb_launch_cfg* cfg, int* modes_in_flight) {
   if (!p || !cfg || !modes_in_flight) return DEB_ERR_INVALID;
-  if (p->exec_mode == DEB_EXEC_LANE) {
+  if (p->group_size > 0) {
+    cfg->stage_vectors = DEB_STAGE_GLOBAL;
+    cfg->modes_per_sm = 0;
+    *modes_in_flight = p->group_warps * p->group_size;
+  } else if (p->exec_mode == DEB_EXEC_LANE) {
     cfg->stage_vectors = DEB_STAGE_GLOBAL;
     cfg->modes_per_sm = 0;
     *modes_in_flight = p->lane_slots;
@@ -462,6 +567,7 @@ int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, in
                    double* d_y_out, int* d_status, int* d_steps, double* d_record, int rec_len, int* d_nrec,
                    int record, int replay, void* stream) {
   if (!p || !cfg || ncosmo <= 0 || nset <= 0 || nmode < 0 || blob_len <= deb::HDR_LEN) return DEB_ERR_INVALID;
+  if (p->group_size > 0) return DEB_ERR_INVALID;   // a grouped plan serves deb_forward_grouped only
   if (nmode == 0) return DEB_OK;
   if (!d_tables || !d_k || !d_tau_out || !d_y_out || !d_status) return DEB_ERR_INVALID;
   if ((long)nmode * nset > p->max_modes) return DEB_ERR_CAPACITY;
@@ -516,6 +622,37 @@ int deb_forward(deb_plan* p, const double* d_tables, int ncosmo, int blob_len, c
                 double* d_y_out, int* d_status, int* d_steps, void* stream) {
   return launch_forward(p, d_tables, ncosmo, 1, blob_len, d_k, d_cosmo_of_mode, nmode, d_tau_out, cfg, d_y_out,
                         d_status, d_steps, nullptr, 0, nullptr, 0, 0, stream);
+}
+
+int deb_forward_grouped(deb_plan* p, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
+                        const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+                        double* d_y_out, int* d_status, int* d_steps, void* stream) {
+  if (!p || !cfg || p->group_size <= 0 || ncosmo <= 0 || nmode < 0 || blob_len <= deb::HDR_LEN) return DEB_ERR_INVALID;
+  if (nmode == 0) return DEB_OK;
+  if (!d_tables || !d_k || !d_tau_out || !d_y_out || !d_status) return DEB_ERR_INVALID;
+  if (nmode % p->group_size) return DEB_ERR_INVALID;
+  if (nmode > p->max_modes) return DEB_ERR_CAPACITY;
+  if (!(cfg->rtol >= 0.0) || !(cfg->atol >= 0.0) || cfg->max_steps <= 0 || !(cfg->error_order > 0.0)) return DEB_ERR_INVALID;
+  if (cfg->step_to_outputs) return DEB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  KParams P{};
+  P.tables = d_tables; P.ncosmo = ncosmo; P.blob_len = blob_len; P.k = d_k; P.cosmo = d_cosmo_of_mode;
+  P.nmode = nmode; P.tau_out = d_tau_out; P.y_out = d_y_out; P.status = d_status; P.steps = d_steps;
+  P.ws = p->ws; P.slot_len = p->slot_len; P.queue = p->queue; P.D = p->D; P.nset = 1;
+  P.ctl.rtol = cfg->rtol; P.ctl.atol = cfg->atol;
+  P.ctl.b1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / cfg->error_order;
+  P.ctl.b2 = -(cfg->pcoeff + 2.0 * cfg->dcoeff) / cfg->error_order;
+  P.ctl.b3 = cfg->dcoeff / cfg->error_order;
+  P.ctl.safety = cfg->safety; P.ctl.fmin = cfg->factormin; P.ctl.fmax = cfg->factormax;
+  P.ctl.max_steps = cfg->max_steps; P.ctl.hist_on_reject = cfg->hist_on_reject;
+  P.ctl.dense = 0; P.ctl.return_full = 0; P.ctl.nout = p->nout;
+  P.ctl.record = 0; P.ctl.replay = 0; P.ctl.step_ts = 0;
+  if (cudaMemsetAsync(p->queue, 0, sizeof(int), s) != cudaSuccess) return DEB_ERR_CUDA;
+  const int ngroup = nmode / p->group_size;
+  const int blocks = ngroup < p->group_warps ? ngroup : p->group_warps;
+  forward_group_kernel<<<blocks, 32, 0, s>>>(P, p->group_size);
+  if (cudaGetLastError() != cudaSuccess) return DEB_ERR_CUDA;
+  return DEB_OK;
 }
 
 int deb_forward_record(deb_plan* p, const double* d_tables, int ncosmo, int blob_len, const double* d_k,

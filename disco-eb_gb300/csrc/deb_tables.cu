@@ -1,0 +1,91 @@
+// deb_tables.cu -- the perturbation path's input tables produced on the GPU:
+// background densities, the RECFAST thermal history and the seven natural
+// cubic splines, packed into the table blob of include/discoeb_gb300.h.
+//
+// One block of one warp per parameter set (deb_tables_core.cuh holds the
+// per-set work).  The ionisation history is a sequential adaptive
+// integration over the sampling intervals and runs on lane 0; everything
+// indexed by a sample (neutrino momentum sums, HeII Saha fractions, sound
+// speeds, the Romberg integrals of d tau / d a, the spline coefficients) is
+// spread over the lanes.
+
+#include <cuda_runtime.h>
+
+#include "deb_tables_core.cuh"
+
+namespace {
+
+using debt::TParams;
+
+__global__ void __launch_bounds__(32) tables_kernel(TParams P) {
+  extern __shared__ double sh[];
+  debt::produce_set(P, blockIdx.x, threadIdx.x, 32, sh);
+}
+
+// tau(a) of each set at the output scale factors: the tau_of_a spline of
+// the blob in the A/B form (perturbations.py:975 via tables.tau_of_a)
+__global__ void tau_out_kernel(const double* tables, int nset, int blob_len, const double* aexp, int nout, double* tau) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nset * nout) return;
+  const int s = t / nout, o = t - s * nout;
+  const double* b = tables + (long)s * blob_len;
+  long p = DEB_HDR_LEN;
+  for (int q = 0; q < 5; ++q) p += 3L * (long)b[20 + q];
+  const int n = (int)b[25];
+  tau[t] = debt::spl_ab(b + p, b + p + n, b + p + 2 * n, n, aexp[o]);
+}
+
+}  // namespace
+
+extern "C" {
+
+int deb_tau_of_a(const double* d_tables, int nset, int blob_len, const double* d_aexp, int nout, double* d_tau,
+                 void* stream) {
+  if (!d_tables || !d_aexp || !d_tau || nset < 0 || nout < 0 || blob_len <= DEB_HDR_LEN) return DEB_ERR_INVALID;
+  const int tot = nset * nout;
+  if (tot == 0) return DEB_OK;
+  tau_out_kernel<<<(tot + 127) / 128, 128, 0, (cudaStream_t)stream>>>(d_tables, nset, blob_len, d_aexp, nout, d_tau);
+  return cudaGetLastError() == cudaSuccess ? DEB_OK : DEB_ERR_CUDA;
+}
+
+int deb_tables_blob_len(int num_thermo, int num_nu, int nqmax) {
+  if (num_thermo < 4 || num_nu < 4 || nqmax < 1) return DEB_ERR_INVALID;
+  const int sizes[7] = {num_thermo, num_thermo, num_nu, num_nu, num_thermo, num_thermo, num_thermo};
+  long L = DEB_HDR_LEN + 2L * nqmax;
+  for (int s = 0; s < 7; ++s) L += 3L * sizes[s] + 4L * (sizes[s] - 1) + (sizes[s] + 1) / 2;
+  return (int)L;
+}
+
+int deb_evolve_background(const deb_bg_cfg* cfg, const double* d_params, int nset, const double* d_consts,
+                          const double* d_grid, double* d_tables, int blob_len, int* d_status, void* stream) {
+  if (!cfg || !d_params || !d_consts || !d_grid || !d_tables || nset < 0) return DEB_ERR_INVALID;
+  if (nset == 0) return DEB_OK;
+  const int N = cfg->num_thermo, NN = cfg->num_nu;
+  if (cfg->nq_bg < 1 || cfg->max_steps < 1 || !(cfg->amin > 0.0)) return DEB_ERR_INVALID;
+  const int L = deb_tables_blob_len(N, NN, cfg->nqmax);
+  if (L < 0 || blob_len != L) return DEB_ERR_INVALID;
+  TParams P{};
+  P.params = d_params; P.nset = nset; P.consts = d_consts;
+  // grid: a_nu [NN], log a_nu [NN], (q, w) background [2 nq_bg], (q, w) perturbations [2 nqmax],
+  // a_thermo [N + 1], log a_thermo[1:] [N]
+  const double* g = d_grid;
+  P.a_nu = g; g += NN;
+  P.la_nu = g; g += NN;
+  P.qw_bg = g; g += 2 * cfg->nq_bg;
+  P.qw = g; g += 2 * cfg->nqmax;
+  P.a_th = g; g += N + 1;
+  P.la_th = g;
+  P.num_nu = NN; P.num_thermo = N; P.nq_bg = cfg->nq_bg; P.nqmax = cfg->nqmax; P.max_steps = cfg->max_steps;
+  P.amin = cfg->amin; P.rtol = cfg->rtol; P.atol = cfg->atol;
+  P.tables = d_tables; P.blob_len = blob_len; P.status = d_status;
+  const size_t smem = (size_t)debt::tables_smem_doubles(N, NN) * sizeof(double);
+  if (smem > 48 * 1024) {
+    if (cudaFuncSetAttribute(tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return DEB_ERR_INVALID;
+  }
+  tables_kernel<<<nset, 32, smem, (cudaStream_t)stream>>>(P);
+  if (cudaGetLastError() != cudaSuccess) return DEB_ERR_CUDA;
+  return DEB_OK;
+}
+
+}  // extern "C"

@@ -75,24 +75,47 @@ def perturbed_params(cosmo, theta=THETA, rel_step=1e-4):
     return out
 
 
+TABLE_NAMES = ("tab0", "tau0", "tabs", "taus")
+SMALL_NAMES = ("k", "com", "eps", "inv_As", "lnk")
+
+
 def _host_inputs(plist, backgrounds, pert, kmodes, aexp_out, nqmax, theta):
-    """Packed host arrays of one gradient problem (tables, output times, k,
-    cosmology index, eps per parameter, 1/A_s and ln(k/k_p) per mode)."""
+    """Packed host arrays of one gradient problem: k, cosmology index, eps per
+    parameter, 1/A_s and ln(k/k_p) per mode, and -- unless ``backgrounds``
+    is ``"gpu"`` -- the table blobs and output times of every set."""
     nc, num_k = len(plist), kmodes.shape[0]
-    nominal = [b[0] for b in backgrounds]
-    sets = [b[1:] for b in backgrounds]
     com = np.repeat(np.arange(nc, dtype=np.int32), num_k)
     kp = np.array([p.get("k_p", 0.05) for p in plist], dtype=np.float64)[com]
     As = np.array([p["A_s"] for p in plist], dtype=np.float64)[com]
     k = np.tile(kmodes, nc)
-    return dict(
-        tab0=_tables.pack_batch(nominal, nqmax),
-        tau0=np.stack([_tables.tau_of_a(b, aexp_out) for b in nominal]),
-        tabs=_tables.pack_batch([q for st in sets for q in st], nqmax),
-        taus=np.stack([_tables.tau_of_a(q, aexp_out) for st in sets for q in st]),
-        k=k, com=com,
-        eps=np.ascontiguousarray(np.array([[e for (_, e, _, _) in pp] for pp in pert], dtype=np.float64)[com].T),
-        inv_As=(1.0 / As)[:, None], lnk=np.log(k / kp)[:, None])
+    h = dict(k=k, com=com,
+             eps=np.ascontiguousarray(np.array([[e for (_, e, _, _) in pp] for pp in pert], dtype=np.float64)[com].T),
+             inv_As=(1.0 / As)[:, None], lnk=np.log(k / kp)[:, None])
+    if not _gpu_tables(backgrounds):
+        nominal = [b[0] for b in backgrounds]
+        sets = [b[1:] for b in backgrounds]
+        h.update(tab0=_tables.pack_batch(nominal, nqmax),
+                 tau0=np.stack([_tables.tau_of_a(b, aexp_out) for b in nominal]),
+                 tabs=_tables.pack_batch([q for st in sets for q in st], nqmax),
+                 taus=np.stack([_tables.tau_of_a(q, aexp_out) for st in sets for q in st]))
+    return h
+
+
+def _gpu_tables(backgrounds):
+    return isinstance(backgrounds, str) and backgrounds == "gpu"
+
+
+def _device_tables(plist, pert, aexp_out, nqmax, out=None):
+    """Tables and output times of the nominal and every theta +- eps set,
+    produced on the GPU from the parameter dicts (two producer launches);
+    ``out`` = (tab0, tau0, tabs, taus) fills existing buffers."""
+    from . import tables_gpu
+
+    sets = [q for pp in pert for (_, _, a, b) in pp for q in (a, b)]
+    o = out or (None, None, None, None)
+    tab0, tau0, st0 = tables_gpu.evolve_background_tables(plist, nqmax, aexp_out=aexp_out, out=o[0], tau_out=o[1])
+    tabs, taus, st1 = tables_gpu.evolve_background_tables(sets, nqmax, aexp_out=aexp_out, out=o[2], tau_out=o[3])
+    return dict(tab0=tab0, tau0=tau0, tabs=tabs, taus=taus), (st0, st1)
 
 
 class GradientProblem:
@@ -100,7 +123,9 @@ class GradientProblem:
 
     ``backgrounds``: per cosmology the evolved ``param`` dicts
     [nominal, theta_1 + eps_1, theta_1 - eps_1, ...] (see
-    :func:`perturbed_params`).  :meth:`run` enqueues the recorded nominal
+    :func:`perturbed_params`), or ``"gpu"``: the tables of all those sets
+    are then produced on the GPU from ``plist`` and ``pert``
+    (:mod:`tables_gpu`), with no host background solve.  :meth:`run` enqueues the recorded nominal
     solve, the replay of every perturbed set, ``get_power`` and the
     difference quotients on one stream, without synchronising;
     :meth:`capture` records that sequence once as a CUDA graph and
@@ -126,15 +151,19 @@ class GradientProblem:
         self.nset = 2 * self.npar
         self.idx = idx
         h = _host_inputs(plist, backgrounds, pert, self.kmodes, aexp_out, nqmax, self.theta)
-        self.host_tab0, self.host_tau0, self.host_tabs, self.host_taus = h["tab0"], h["tau0"], h["tabs"], h["taus"]
         self.host_k, self.host_com = h["k"], h["com"]
         self.nmode = self.host_k.shape[0]
         dev = torch.device("cuda", torch.cuda.current_device())
         self.device = dev
-        # pinned staging copies of every per-call input, and their device twins
-        self._names = ("tab0", "tau0", "tabs", "taus", "k", "com", "eps", "inv_As", "lnk")
+        # pinned staging copies of every per-call host input, and their device twins
+        self.gpu_tables = _gpu_tables(backgrounds)
+        self._names = SMALL_NAMES + (() if self.gpu_tables else TABLE_NAMES)
         self._pinned = {n: torch.from_numpy(np.ascontiguousarray(h[n])).pin_memory() for n in self._names}
         self._dev = {n: self._pinned[n].to(dev) for n in self._names}
+        if self.gpu_tables:
+            dt, self._table_status = _device_tables(plist, pert, aexp_out, nqmax)
+            self._dev.update(dt)
+        self.blob_len = int(self._dev["tab0"].shape[1])
         self.d_tab0, self.d_tabs = self._dev["tab0"], self._dev["tabs"]
         self.d_k, self.d_com = self._dev["k"], self._dev["com"]
         self.d_tau0, self.d_taus = self._dev["tau0"], self._dev["taus"]
@@ -165,9 +194,14 @@ class GradientProblem:
         """Copy the inputs of another set of cosmologies of the same shape
         (same count, k-grid, output times count, table lengths) into this
         problem's device buffers: host packing, then one pinned host-to-device
-        copy per input array on ``stream``.  Returns the bytes copied."""
+        copy per input array on ``stream``; with GPU tables the producer
+        writes the new tables into the same buffers.  Returns the bytes
+        copied from the host."""
         import torch
 
+        if _gpu_tables(backgrounds) != self.gpu_tables:
+            raise ValueError("load: the problem was built with tables from the " +
+                             ("GPU" if self.gpu_tables else "host"))
         h = _host_inputs(plist, backgrounds, pert, self.kmodes, self.aexp_out, self.nqmax, self.theta)
         s = stream if stream is not None else torch.cuda.current_stream()
         if self._copied is not None:
@@ -184,14 +218,30 @@ class GradientProblem:
                 nbytes += a.nbytes
             self._copied = torch.cuda.Event()
             self._copied.record(s)
-        self.host_tab0, self.host_tau0, self.host_tabs, self.host_taus = h["tab0"], h["tau0"], h["tabs"], h["taus"]
+            if self.gpu_tables:
+                from . import tables_gpu
+
+                _, self._table_status = _device_tables(plist, pert, self.aexp_out, self.nqmax,
+                                                       out=tuple(self._dev[n] for n in TABLE_NAMES))
+                nbytes += tables_gpu.param_matrix(plist).nbytes * (1 + self.nset)
         return nbytes
+
+    def input_bytes(self) -> int:
+        """Host bytes one call copies to the device: the packed tables and
+        small per-mode arrays, or with GPU tables the parameter rows of
+        every set plus the small arrays."""
+        from . import tables_gpu
+
+        n = sum(int(self._pinned[k].numel() * self._pinned[k].element_size()) for k in self._names)
+        if self.gpu_tables:
+            n += self.nc * (1 + self.nset) * len(tables_gpu.PARAM_KEYS) * 8
+        return n
 
     def _record(self, plan, s):
         L = _native.load()
         c = lambda t: ctypes.c_void_p(t.data_ptr())
         _native.check(_pt.launch_ordered(plan, self.order, self.nmode, lambda: L.deb_forward_record(
-            plan.ptr, c(self.d_tab0), self.nc, self.host_tab0.shape[1], c(self.d_k), c(self.d_com), self.nmode,
+            plan.ptr, c(self.d_tab0), self.nc, self.blob_len, c(self.d_k), c(self.d_com), self.nmode,
             c(self.d_tau0), ctypes.byref(self.cfg), c(self.d_y0), c(self.d_st0), c(self.d_steps), c(self.d_rec),
             self.rec_len, c(self.d_nrec), ctypes.c_void_p(s.cuda_stream))), "deb_forward_record")
 
@@ -219,7 +269,7 @@ class GradientProblem:
         self._record(self.plan, s)
         if events:
             events[1].record(s)
-        _native.check(L.deb_replay(self.plan.ptr, c(self.d_tabs), self.nc, self.nset, self.host_tabs.shape[1],
+        _native.check(L.deb_replay(self.plan.ptr, c(self.d_tabs), self.nc, self.nset, self.blob_len,
                                    c(self.d_k), c(self.d_com), self.nmode, c(self.d_taus), ctypes.byref(self.cfg),
                                    c(self.d_rec), self.rec_len, c(self.d_nrec), c(self.d_ys), c(self.d_sts), sp),
                       "deb_replay")
@@ -236,7 +286,7 @@ class GradientProblem:
                     self.d_dl[:, :, j] = self.d_lnk
                 else:
                     self.d_dl[:, :, j] = dl_ode[self.ode_names.index(name)]
-        _native.check(L.deb_get_power(c(self.d_tab0), self.nc, self.host_tab0.shape[1], c(self.d_k), c(self.d_com),
+        _native.check(L.deb_get_power(c(self.d_tab0), self.nc, self.blob_len, c(self.d_k), c(self.d_com),
                                       self.nmode, self.nout, c(self.d_y0), 20, self.idx, c(self.d_P), sp),
                       "deb_get_power")
         return self.d_P, self.d_dl
@@ -286,7 +336,7 @@ def _run_cached(plist, backgrounds, pert, kmodes, aexp_out, opts):
 
     aexp = np.atleast_1d(np.asarray(aexp_out, dtype=np.float64))
     key = (torch.cuda.current_device(), len(plist), np.asarray(kmodes, dtype=np.float64).tobytes(), aexp.shape[0],
-           tuple(sorted(opts.items())), tuple(n for (n, _, _, _) in pert[0]))
+           tuple(sorted(opts.items())), tuple(n for (n, _, _, _) in pert[0]), _gpu_tables(backgrounds))
     gp = _problems.get(key)
     if gp is not None:
         try:
@@ -316,7 +366,8 @@ def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num
                               atol: float = 1e-4, pcoeff: float = 0.25, icoeff: float = 0.80, dcoeff: float = 0.0,
                               factormax: float = 20.0, factormin: float = 0.3, max_steps: int = 2048, idx: int = 4,
                               theta=THETA, rel_step: float = 1e-4, dologk: bool = True, processes=None,
-                              backgrounds=None, throw: bool = True, step_to_outputs: bool = False):
+                              backgrounds=None, throw: bool = True, step_to_outputs: bool = False,
+                              tables: str = "host"):
     """P(k, a) and d log P / d theta for one or many cosmologies.
 
     ``params``: input parameter dict(s) as given to ``evolve_background``
@@ -325,6 +376,9 @@ def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num
     kmodes)``; with a single dict the cosmology axis is dropped.
     ``backgrounds`` may pass precomputed host tables: a list (per cosmology)
     of [nominal, +eps_1, -eps_1, +eps_2, ...] evolved ``param`` dicts.
+    Without them the tables of all those sets come from the host producer
+    (``tables="host"``, a process pool) or from the GPU producer in one
+    launch (``tables="gpu"``).
     With the reference's output semantics (linear interpolation inside the
     step) an interior output's derivative includes the slope of that
     interpolant; ``step_to_outputs=True`` lands steps on the output times.
@@ -335,7 +389,9 @@ def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num
     kmodes = np.geomspace(kmin, kmax, num_k) if dologk else np.linspace(kmin, kmax, num_k)
     pert = [perturbed_params(p, theta, rel_step) for p in plist]
     nset = 2 * len(pert[0])
-    if backgrounds is None:
+    if backgrounds is None and tables == "gpu":
+        backgrounds = "gpu"
+    elif backgrounds is None:
         flat = []
         for p, pp in zip(plist, pert):
             flat.append(p)

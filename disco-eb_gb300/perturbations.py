@@ -276,28 +276,79 @@ def evolve_perturbations(*, param, aexp_out, kmin: float, kmax: float, num_k: in
     return y, kmodes, param
 
 
+def solve_grouped(tables, kmodes, tau_out, batch_size: int, cosmo_of_mode=None, *, lmaxg=11, lmaxgp=11, lmaxr=11,
+                  lmaxnu=8, nqmax=3, rtol=1e-4, atol=1e-4, pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0,
+                  factormin=0.3, max_steps=2048, throw=True, return_stats=False, output="numpy"):
+    """Groups of ``batch_size`` consecutive modes sharing one start time and one
+    step sequence (``deb_forward_grouped``); y [nmode, nout, 20]."""
+    torch = _torch()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    as_t = lambda a, dt: (a if torch.is_tensor(a) else torch.as_tensor(np.ascontiguousarray(a))).to(dev, dt).contiguous()
+    tabs = as_t(np.atleast_2d(tables) if not torch.is_tensor(tables) else tables, torch.float64)
+    k = as_t(kmodes, torch.float64)
+    tau = as_t(np.atleast_2d(tau_out) if not torch.is_tensor(tau_out) else tau_out, torch.float64)
+    nmode, nout = int(k.shape[0]), int(tau.shape[1])
+    if nmode % batch_size:
+        raise ValueError("the number of modes must be divisible by batch_size")
+    com = as_t(np.zeros(nmode, dtype=np.int32) if cosmo_of_mode is None else cosmo_of_mode, torch.int32)
+    dims = _dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, nout, False, "structured", "warp")
+    key = ("grouped", torch.cuda.current_device(), lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, nout, int(batch_size))
+    plan = _plans.get(key)
+    if plan is None or plan.max_modes < nmode:
+        plan = _native.Plan(dims, max(nmode, 1), batch_size=int(batch_size))
+        _plans[key] = plan
+    cfg = _cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps)
+    y = torch.empty((nmode, nout, 20), dtype=torch.float64, device=dev)
+    status = torch.empty((nmode,), dtype=torch.int32, device=dev)
+    steps = torch.empty((nmode, 2), dtype=torch.int32, device=dev)
+    c = lambda t: ctypes.c_void_p(t.data_ptr())
+    _native.check(_native.load().deb_forward_grouped(plan.ptr, c(tabs), int(tabs.shape[0]), int(tabs.shape[1]), c(k),
+                                                     c(com), nmode, c(tau), ctypes.byref(cfg), c(y), c(status), c(steps),
+                                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+                  "deb_forward_grouped")
+    st = status.cpu().numpy()
+    _check_status(st, k.cpu().numpy(), throw)
+    out = y if output == "torch" else y.cpu().numpy()
+    if return_stats:
+        return out, {"status": st, "steps": steps.cpu().numpy()}
+    return out
+
+
 def evolve_perturbations_batched(*, param, aexp_out, kmin: float, kmax: float, num_k: int, lmaxg: int = 11,
                                  lmaxgp: int = 11, lmaxr: int = 11, lmaxnu: int = 8, nqmax: int = 3, rtol: float = 1e-4,
                                  atol: float = 1e-4, pcoeff: float = 0.25, icoeff: float = 0.80, dcoeff: float = 0.0,
                                  factormax: float = 20.0, factormin: float = 0.3, max_steps: int = 2048,
-                                 batch_size: int = 16, throw: bool = True, output: str = "numpy"):
-    """Signature of ``perturbations.py:1000-1061``; returns ``(y, kmodes)``.
+                                 batch_size: int = 16, throw: bool = True, output: str = "numpy",
+                                 grouped: bool = True):
+    """Signature and semantics of ``perturbations.py:1000-1061``; returns ``(y, kmodes)``.
 
-    The reference groups ``batch_size`` modes under one shared start time
-    and one shared step sequence so they fit a vmapped dense solver.  The GPU
-    kernel needs no such grouping: every mode keeps its own start time and
-    step sequence (the ``evolve_perturbations`` semantics), so results equal
-    :func:`evolve_perturbations` and differ from the reference's batched
-    variant by that variant's own grouping error.  ``batch_size`` must
-    divide ``num_k`` as in the reference.
+    As in the reference, ``batch_size`` consecutive modes (of the geomspace
+    grid) form a group that starts at the group's smallest start time and
+    takes one shared step sequence, controlled by one error norm over all its
+    modes (``deb_forward_grouped``, one warp per group).  ``grouped=False``
+    gives every mode its own start time and steps instead (the
+    :func:`evolve_perturbations` semantics, the persistent per-mode kernel).
+    ``batch_size`` must divide ``num_k`` as in the reference (1 to 32 here).
     """
     if num_k % batch_size != 0:
         raise ValueError("num_k must be divisible by batch_size")
-    y, kmodes, _ = evolve_perturbations(param=dict(param), aexp_out=aexp_out, kmin=kmin, kmax=kmax, num_k=num_k,
-                                        lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr, lmaxnu=lmaxnu, nqmax=nqmax, rtol=rtol,
-                                        atol=atol, pcoeff=pcoeff, icoeff=icoeff, dcoeff=dcoeff, factormax=factormax,
-                                        factormin=factormin, max_steps=max_steps, throw=throw, output=output)
-    param["nout"] = np.atleast_1d(aexp_out).shape[0]
+    if not grouped:
+        y, kmodes, _ = evolve_perturbations(param=dict(param), aexp_out=aexp_out, kmin=kmin, kmax=kmax, num_k=num_k,
+                                            lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr, lmaxnu=lmaxnu, nqmax=nqmax,
+                                            rtol=rtol, atol=atol, pcoeff=pcoeff, icoeff=icoeff, dcoeff=dcoeff,
+                                            factormax=factormax, factormin=factormin, max_steps=max_steps,
+                                            throw=throw, output=output)
+        param["nout"] = np.atleast_1d(aexp_out).shape[0]
+        return y, kmodes
+    kmodes = np.geomspace(kmin, kmax, num_k)
+    aexp_out = np.atleast_1d(np.asarray(aexp_out, dtype=np.float64))
+    tau_out = _tables.tau_of_a(param, aexp_out)
+    blob = _tables.pack_cosmology(param, nqmax)
+    y = solve_grouped(blob[None, :], kmodes, tau_out[None, :], batch_size, None, lmaxg=lmaxg, lmaxgp=lmaxgp,
+                      lmaxr=lmaxr, lmaxnu=lmaxnu, nqmax=nqmax, rtol=rtol, atol=atol, pcoeff=pcoeff, icoeff=icoeff,
+                      dcoeff=dcoeff, factormax=factormax, factormin=factormin, max_steps=max_steps, throw=throw,
+                      output=output)
+    param["nout"] = aexp_out.shape[0]
     return y, kmodes
 
 

@@ -1,0 +1,122 @@
+"""Input tables produced on the GPU (``deb_evolve_background``).
+
+The RECFAST branch of ``evolve_background`` (``src/discoeb/background.py:140-342``
+with ``thermodynamics_recfast.py:124-501``) for many parameter sets in one
+launch, written straight into the table blobs the solver reads.  The
+algorithm is the one of :mod:`background` / :mod:`recfast` on the host: the
+same sampling grids, quadrature nodes and constants are passed to the kernel
+from those modules, so host and device tables agree to rounding.
+
+:func:`evolve_background_tables` is the entry point: parameter dicts in (the
+keys ``evolve_background`` reads), ``[nset, blob_len]`` device tables out,
+optionally with ``tau_of_a`` at given scale factors.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import _native
+from . import background as _bg
+from . import recfast as _rf
+from . import tables as _tables
+
+# order of deb_tables_const in include/discoeb_gb300.h
+CONST_NAMES = (
+    "G_N", "M_H", "M_E", "MHE_MH", "C_LIGHT", "H_PLANCK", "K_B", "BIG_H", "DENS_FAC", "E_ION_HE12S", "LAMBDA_H",
+    "LAMBDA_HE", "L_HE1_ION", "L_HE_2P", "A2P_S", "A2P_T", "L_HE_2PT", "SIGMA_HE_2PS", "SIGMA_HE_2PT", "AGAUSS1",
+    "AGAUSS2", "ZGAUSS1", "ZGAUSS2", "WGAUSS1", "WGAUSS2", "H_FRAC", "CDB", "CDB_HE", "CB1", "CR", "CK", "CK_HE",
+    "CL", "CL_HE", "CT", "BFACT", "CL_PST", "HCL_HE2ST_KB", "HCL_HE2ST_ION_KB", "A_PPB", "B_PPB", "C_PPB", "D_PPB",
+    "A_VF", "B_VF", "T_0", "T_1", "A_TRIP", "B_TRIP", "FU", "_G", "_G21", "_G31", "_G32", "_G41", "_G42", "_G43",
+    "_A21", "_A31", "_A32", "_CH1", "_CH2", "_CH3", "_C1", "_C2", "_C3", "_C4")
+# order of deb_bg_param
+PARAM_KEYS = ("Omegam", "Omegab", "H0", "Tcmb", "YHe", "Neff", "Nmnu", "mnu", "w_DE_0", "w_DE_a", "cs2_DE", "A_s",
+              "n_s", "k_p", "Omegak")
+PARAM_DEFAULTS = {"cs2_DE": 1.0, "k_p": 0.05, "Omegak": 0.0}
+
+AMIN, AMAX = 1e-9, 1.01      # evolve_background's range (background.py:191-200)
+NUM_NU, NQ_BG = 512, 8       # neutrino table points and momentum bins (background.py:158, 47)
+
+
+class DebBgCfg(ctypes.Structure):
+    _fields_ = [("num_thermo", ctypes.c_int), ("num_nu", ctypes.c_int), ("nq_bg", ctypes.c_int), ("nqmax", ctypes.c_int),
+                ("max_steps", ctypes.c_int), ("amin", ctypes.c_double), ("rtol", ctypes.c_double),
+                ("atol", ctypes.c_double)]
+
+
+def constants() -> np.ndarray:
+    """The RECFAST constants, fitting parameters and GRK4A coefficients of the
+    host producer, plus pi, sqrt(pi) and the neutrino mass conversion."""
+    vals = [float(getattr(_rf, n)) for n in CONST_NAMES] + [math.pi, math.sqrt(math.pi), _bg.C2OK]
+    return np.array(vals, dtype=np.float64)
+
+
+def grid(num_thermo: int, nqmax: int) -> np.ndarray:
+    """Parameter-independent inputs: neutrino table scale factors and logs,
+    both momentum quadratures, the RECFAST sampling and its logs."""
+    a_nu = np.geomspace(AMIN * 0.9, AMAX * 1.1, NUM_NU)
+    q_bg, w_bg = _bg.get_neutrino_momentum_bins(NQ_BG)
+    q, w = _bg.get_neutrino_momentum_bins(nqmax)
+    a_th = _rf.adaptive_sampling(AMIN, AMAX, num_thermo + 1)
+    return np.ascontiguousarray(np.concatenate([a_nu, np.log(a_nu), q_bg, w_bg, q, w, a_th, np.log(a_th[1:])]))
+
+
+def param_matrix(params) -> np.ndarray:
+    rows = []
+    for p in params:
+        rows.append([float(p["H0"]) if k == "H0" else float(p.get(k, PARAM_DEFAULTS.get(k, np.nan))) for k in PARAM_KEYS])
+    m = np.array(rows, dtype=np.float64)
+    if np.isnan(m).any():
+        missing = [k for j, k in enumerate(PARAM_KEYS) if np.isnan(m[:, j]).any()]
+        raise KeyError(f"parameter set(s) missing {missing}")
+    return m
+
+
+def blob_len(num_thermo: int, nqmax: int) -> int:
+    return _tables.blob_length([num_thermo, num_thermo, NUM_NU, NUM_NU, num_thermo, num_thermo, num_thermo], nqmax)
+
+
+_static = {}
+
+
+def evolve_background_tables(params, nqmax: int, *, num_thermo: int = 256, aexp_out=None, rtol: float = 1e-3,
+                             atol: float = 1e-6, max_steps: int = 128, stream=None, out=None, tau_out=None):
+    """Table blobs of every parameter set on the current CUDA device.
+
+    ``params``: list of dicts with the keys ``evolve_background`` reads.
+    Returns ``(tables [nset, blob_len], tau [nset, nout] or None, status
+    [nset])`` as torch tensors on the device (stream-ordered, no host sync);
+    ``out`` / ``tau_out`` may pass preallocated buffers.  A nonzero status
+    means an interval of the ionisation history used up its step budget.
+    """
+    import torch
+
+    L = _native.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    s = stream if stream is not None else torch.cuda.current_stream()
+    key = (dev.index, num_thermo, nqmax)
+    if key not in _static:
+        _static[key] = (torch.as_tensor(constants()).to(dev), torch.as_tensor(grid(num_thermo, nqmax)).to(dev))
+    consts, grd = _static[key]
+    pm = torch.as_tensor(param_matrix(params)).to(dev, non_blocking=True)
+    nset = pm.shape[0]
+    bl = blob_len(num_thermo, nqmax)
+    rc_len = L.deb_tables_blob_len(num_thermo, NUM_NU, nqmax)
+    if rc_len != bl:
+        raise RuntimeError(f"blob length mismatch: host {bl}, library {rc_len}")
+    tabs = out if out is not None else torch.empty((nset, bl), dtype=torch.float64, device=dev)
+    status = torch.empty((nset,), dtype=torch.int32, device=dev)
+    cfg = DebBgCfg(num_thermo, NUM_NU, NQ_BG, nqmax, max_steps, AMIN, rtol, atol)
+    c = lambda t: ctypes.c_void_p(t.data_ptr())
+    with torch.cuda.stream(s):
+        _native.check(L.deb_evolve_background(ctypes.byref(cfg), c(pm), nset, c(consts), c(grd), c(tabs), bl, c(status),
+                                              ctypes.c_void_p(s.cuda_stream)), "deb_evolve_background")
+        tau = None
+        if aexp_out is not None:
+            aexp = torch.as_tensor(np.atleast_1d(np.asarray(aexp_out, dtype=np.float64))).to(dev)
+            tau = tau_out if tau_out is not None else torch.empty((nset, aexp.shape[0]), dtype=torch.float64, device=dev)
+            _native.check(L.deb_tau_of_a(c(tabs), nset, bl, c(aexp), int(aexp.shape[0]), c(tau),
+                                         ctypes.c_void_p(s.cuda_stream)), "deb_tau_of_a")
+    return tabs, tau, status

@@ -190,6 +190,25 @@ int deb_replay(deb_plan* plan, const double* d_tables, int ncosmo, int nset, int
                const double* d_record, int rec_len, const int* d_nrec, double* d_y_out, int* d_status, void* stream);
 
 /*
+ * The reference's batched variant, evolve_perturbations_batched
+ * (perturbations.py:1000-1061 with evolve_modes_batched :835-922 and
+ * Rodas5Batched, ode_integrators_stiff.py:846-1010): groups of batch_size
+ * consecutive modes start together at the smallest of their start times
+ * (:786-803), take one step sequence, and the PID controller sees one error
+ * norm, the RMS over the six filtered entries of every mode of the group
+ * (rms_norm_filtered_batched, :690-694).  A grouped plan (batch_size 1..32;
+ * structured solver, 20 output fields) serves deb_forward_grouped only; its
+ * arguments mean what they mean for deb_forward, nmode must be a multiple of
+ * batch_size and every group must lie in one cosmology (else the group's
+ * modes get DEB_MODE_BAD_INPUT); step_to_outputs must be 0.  Every mode of a
+ * group reports the group's status and step counts.
+ */
+int deb_plan_create_grouped(const deb_dims* dims, int max_modes, int batch_size, deb_plan** plan);
+int deb_forward_grouped(deb_plan* plan, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
+                        const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+                        double* d_y_out, int* d_status, int* d_steps, void* stream);
+
+/*
  * get_power (perturbations.py:1101-1123):
  *   P[m, o] = 2 pi^2 A_s (k_m/k_p)^(n_s-1) k_m^-3 y[m, o, idx]^2
  * with A_s, n_s, k_p read from the mode's cosmology blob.
@@ -259,6 +278,59 @@ int deb_fftlog_phase(int nfreq, double log_kmax_over_kmin, int ell, double* d_ph
 int deb_forward_static(const deb_dims* dims, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
                        const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
                        double* d_y_out, int* d_status, int* d_steps, void* stream);
+
+/*
+ * Input tables on the GPU: the RECFAST branch of evolve_background
+ * (background.py:140-342 with thermodynamics_recfast.py:124-501) for nset
+ * parameter sets at once, written straight into table blobs.  One warp per
+ * set; the adaptive GRK4A ionisation history runs on one lane, the sampled
+ * quantities (neutrino tables, Saha fractions, sound speed, Romberg tau
+ * integrals, spline coefficients) on all 32.
+ *
+ *   d_params [nset, DEB_BG_NPARAM]   input parameters in the order below
+ *   d_consts [DEB_TC_COUNT]          RECFAST physical constants, fitting
+ *                                    parameters and GRK4A coefficients (the
+ *                                    host passes the numbers its own
+ *                                    producer uses, so both agree)
+ *   d_grid   parameter-independent grids, concatenated:
+ *            a_nu[num_nu], log a_nu[num_nu] (neutrino tables),
+ *            q[nq_bg], w[nq_bg] (their momentum quadrature),
+ *            q[nqmax], w[nqmax] (the perturbations' momentum bins),
+ *            a_thermo[num_thermo + 1] (RECFAST sampling), log a_thermo[1:]
+ *   d_tables [nset, blob_len] output blobs, blob_len = deb_tables_blob_len()
+ *   d_status [nset] (may be NULL): 1 if an interval's step budget ran out
+ */
+enum deb_bg_param {
+  DEB_BG_OMEGAM = 0, DEB_BG_OMEGAB, DEB_BG_H0, DEB_BG_TCMB, DEB_BG_YHE, DEB_BG_NEFF, DEB_BG_NMNU, DEB_BG_MNU,
+  DEB_BG_W0, DEB_BG_WA, DEB_BG_CS2DE, DEB_BG_AS, DEB_BG_NS, DEB_BG_KP, DEB_BG_OMEGAK, DEB_BG_NPARAM
+};
+enum deb_tables_const {
+  DEB_TC_G_N = 0, DEB_TC_MH, DEB_TC_ME, DEB_TC_MHE_MH, DEB_TC_C, DEB_TC_H_PLANCK, DEB_TC_KB, DEB_TC_BIG_H,
+  DEB_TC_DENS_FAC, DEB_TC_E_ION_HE12S, DEB_TC_LAMBDA_H, DEB_TC_LAMBDA_HE, DEB_TC_L_HE1_ION, DEB_TC_L_HE_2P,
+  DEB_TC_A2P_S, DEB_TC_A2P_T, DEB_TC_L_HE_2PT, DEB_TC_SIGMA_HE_2PS, DEB_TC_SIGMA_HE_2PT, DEB_TC_AGAUSS1,
+  DEB_TC_AGAUSS2, DEB_TC_ZGAUSS1, DEB_TC_ZGAUSS2, DEB_TC_WGAUSS1, DEB_TC_WGAUSS2, DEB_TC_H_FRAC, DEB_TC_CDB,
+  DEB_TC_CDB_HE, DEB_TC_CB1, DEB_TC_CR, DEB_TC_CK, DEB_TC_CK_HE, DEB_TC_CL, DEB_TC_CL_HE, DEB_TC_CT, DEB_TC_BFACT,
+  DEB_TC_CL_PST, DEB_TC_HCL_HE2ST_KB, DEB_TC_HCL_HE2ST_ION_KB, DEB_TC_A_PPB, DEB_TC_B_PPB, DEB_TC_C_PPB,
+  DEB_TC_D_PPB, DEB_TC_A_VF, DEB_TC_B_VF, DEB_TC_T0, DEB_TC_T1, DEB_TC_A_TRIP, DEB_TC_B_TRIP, DEB_TC_FU,
+  DEB_TC_G, DEB_TC_G21, DEB_TC_G31, DEB_TC_G32, DEB_TC_G41, DEB_TC_G42, DEB_TC_G43, DEB_TC_A21, DEB_TC_A31,
+  DEB_TC_A32, DEB_TC_CH1, DEB_TC_CH2, DEB_TC_CH3, DEB_TC_C1, DEB_TC_C2, DEB_TC_C3, DEB_TC_C4, DEB_TC_PI,
+  DEB_TC_SQRT_PI, DEB_TC_C2OK, DEB_TC_COUNT
+};
+typedef struct deb_bg_cfg {
+  int num_thermo;   /* RECFAST samples (evolve_background's num_thermo, 256) */
+  int num_nu;       /* neutrino table points (512) */
+  int nq_bg;        /* momentum bins of the background neutrino sums (8) */
+  int nqmax;        /* momentum bins written into the blob for the perturbations */
+  int max_steps;    /* GRK4A steps per sampling interval (128) */
+  double amin;      /* 1e-9: taumin = amin / adotrad */
+  double rtol, atol;/* GRK4A tolerances (1e-3, 1e-6) */
+} deb_bg_cfg;
+int deb_tables_blob_len(int num_thermo, int num_nu, int nqmax);
+int deb_evolve_background(const deb_bg_cfg* cfg, const double* d_params, int nset, const double* d_consts,
+                          const double* d_grid, double* d_tables, int blob_len, int* d_status, void* stream);
+/* tau_of_a (perturbations.py:975) of each blob at nout scale factors: d_tau [nset, nout] */
+int deb_tau_of_a(const double* d_tables, int nset, int blob_len, const double* d_aexp, int nout, double* d_tau,
+                 void* stream);
 
 /* Measured-peak helper for roofline reporting: runs independent FP64 FMA
    chains on every SM and returns the achieved FP64 FLOP/s (FMA = 2).

@@ -44,6 +44,8 @@ def lib():
         ip = ctypes.POINTER(ctypes.c_int)
         L.oracle_solve.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp, ip, ctypes.c_int, dp, ctypes.c_int, ip, dp,
                                    ctypes.c_int, ctypes.c_int, dp, ip, ctypes.c_int]
+        L.oracle_solve_grouped.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp, ip, ctypes.c_int, dp, ctypes.c_int, ip,
+                                           dp, ctypes.c_int, ctypes.c_int, dp, ip, ctypes.c_int]
         L.oracle_rhs.argtypes = [dp, ip, ctypes.c_double, ctypes.c_double, dp, dp]
         L.oracle_jacobian.argtypes = [dp, ip, ctypes.c_double, ctypes.c_double, dp, dp, dp]
         L.oracle_initial.argtypes = [dp, ip, ctypes.c_double, ctypes.c_double, dp, dp]
@@ -88,6 +90,30 @@ def solve(tables, kmodes, tau_out, *, cosmo_of_mode=None, lmaxg=11, lmaxgp=11, l
                             1 if return_full else 0, _p(y), _p(stats, ctypes.c_int), int(nthreads))
     if rc != 0:
         raise RuntimeError(f"oracle_solve returned {rc}")
+    return y, stats
+
+
+def solve_grouped(tables, kmodes, tau_out, batch_size, *, cosmo_of_mode=None, lmaxg=11, lmaxgp=11, lmaxr=11,
+                  lmaxnu=8, nqmax=3, rtol=1e-4, atol=1e-4, pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0,
+                  factormin=0.3, max_steps=2048, error_order=5.0, safety=0.9, hist_on_reject=False, nthreads=0):
+    """The reference's batched variant (groups of batch_size consecutive modes
+    sharing one start time and one step sequence).  Returns (y [nmode, nout,
+    20], stats [nmode, 3])."""
+    tables = np.ascontiguousarray(np.atleast_2d(tables), dtype=np.float64)
+    kmodes = np.ascontiguousarray(kmodes, dtype=np.float64)
+    tau_out = np.ascontiguousarray(np.atleast_2d(tau_out), dtype=np.float64)
+    nmode, nout = kmodes.shape[0], tau_out.shape[1]
+    com = np.ascontiguousarray(np.zeros(nmode) if cosmo_of_mode is None else cosmo_of_mode, dtype=np.int32)
+    dims = np.array([lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax], dtype=np.int32)
+    cfg = np.array([rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, error_order, safety,
+                    1.0 if hist_on_reject else 0.0, 0.0], dtype=np.float64)
+    y = np.empty((nmode, nout, 20), dtype=np.float64)
+    stats = np.zeros((nmode, 3), dtype=np.int32)
+    rc = lib().oracle_solve_grouped(_p(tables), tables.shape[0], tables.shape[1], _p(kmodes), _p(com, ctypes.c_int),
+                                    nmode, _p(tau_out), nout, _p(dims, ctypes.c_int), _p(cfg), int(max_steps),
+                                    int(batch_size), _p(y), _p(stats, ctypes.c_int), int(nthreads))
+    if rc != 0:
+        raise RuntimeError(f"oracle_solve_grouped returned {rc}")
     return y, stats
 
 

@@ -547,9 +547,159 @@ ModeResult solve_mode(const Cosmo& c, const Dims& D, double k, const double* tau
   return R;
 }
 
+// evolve_modes_batched (perturbations.py:835-922) with Rodas5Batched
+// (ode_integrators_stiff.py:846-1010): B modes start together at the smallest
+// of their start times (perturbations.py:786-803), take one step sequence,
+// and the PID controller sees the RMS over the six filtered entries of all B
+// modes (rms_norm_filtered_batched, perturbations.py:690-694).  Each mode's
+// Rodas5 step is the per-mode step above.
+ModeResult solve_group(const Cosmo& c, const Dims& D, const double* ks, int B, const double* tau_out, int nout,
+                       const Cfg& cfg, double* yout /* [B, nout, 20] */) {
+  const int n = D.n;
+  ModeResult R{ST_OK, 0, 0};
+  double tau_max = tau_out[0], tau_min_out = tau_out[0];
+  for (int i = 1; i < nout; ++i) { tau_max = std::max(tau_max, tau_out[i]); tau_min_out = std::min(tau_min_out, tau_out[i]); }
+  double t0 = 1e300;
+  for (int b = 0; b < B; ++b) t0 = std::min(t0, 0.99 * std::min(tau_min_out, start_time(c, ks[b])));
+  std::vector<std::vector<double>> y(B, std::vector<double>(n)), y1(B, std::vector<double>(n)), K(B, std::vector<double>((size_t)8 * n));
+  std::vector<double> u(n), du(n), dT(n), J((size_t)n * n), sc(n);
+  std::vector<int> piv(n);
+  std::vector<Dual> yd(n), fd(n);
+  for (int b = 0; b < B; ++b) initial_conditions(c, D, ks[b], t0, y[b].data());
+  std::vector<int> order(nout);
+  for (int i = 0; i < nout; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return tau_out[a] < tau_out[b]; });
+  int next_out = 0;
+  const double T1 = tau_max;
+  double t1 = std::min(t0 + std::min(t0 / 4.0, 0.5 * (T1 - t0)), T1);
+  double prev_inv = 1.0, prev_prev_inv = 1.0;
+  const double beta1 = (cfg.icoeff + cfg.pcoeff + cfg.dcoeff) / cfg.error_order;
+  const double beta2 = -(cfg.pcoeff + 2.0 * cfg.dcoeff) / cfg.error_order;
+  const double beta3 = cfg.dcoeff / cfg.error_order;
+  static const int err_idx[6] = {0, 2, 3, 5, 6, 7};
+  int steps = 0;
+  while (t0 < T1) {
+    if (steps >= cfg.max_steps) { R.status = ST_MAX_STEPS; break; }
+    const double dt = t1 - t0;
+    double ss = 0.0;
+    for (int b = 0; b < B; ++b) {
+      const double k = ks[b];
+      jacobian(c, D, k, t0, y[b].data(), J.data(), yd, fd);
+      const double dtg = dt * R_gamma;
+      for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) J[(size_t)i * n + j] = (i == j ? 1.0 / dtg : 0.0) - J[(size_t)i * n + j];
+      lu_factor(J.data(), n, piv.data());
+      dfdt(c, D, k, t0, y[b].data(), dT.data(), yd, fd);
+      double* Kb = K[b].data();
+      for (int st = 0; st < 8; ++st) {
+        double* kst = &Kb[(size_t)st * n];
+        if (st == 0) {
+          for (int i = 0; i < n; ++i) u[i] = y[b][i];
+        } else if (st <= 5) {
+          for (int i = 0; i < n; ++i) { double acc = y[b][i]; for (int j = 0; j < st; ++j) acc += R_a[st][j] * Kb[(size_t)j * n + i]; u[i] = acc; }
+        } else {
+          for (int i = 0; i < n; ++i) u[i] += Kb[(size_t)(st - 1) * n + i];
+        }
+        rhs<double>(c, D, k, t0 + R_c[st] * dt, u.data(), du.data());
+        for (int i = 0; i < n; ++i) {
+          double r = du[i];
+          if (st <= 4) r += dt * R_d[st] * dT[i];
+          double acc = 0.0;
+          for (int j = 0; j < st; ++j) acc += (R_C[st][j] / dt) * Kb[(size_t)j * n + i];
+          kst[i] = r + acc;
+        }
+        lu_solve(J.data(), n, piv.data(), kst);
+      }
+      const double* k8 = &Kb[(size_t)7 * n];
+      bool nan = false;
+      for (int i = 0; i < n; ++i) { y1[b][i] = u[i] + k8[i]; if (!std::isfinite(y1[b][i])) nan = true; }
+      const double err_w[6] = {1.0, k * k, 1.0, 1.0, 1.0 / (k * k), 1.0};
+      for (int m = 0; m < 6; ++m) {
+        int i = err_idx[m];
+        double yc = nan ? y[b][i] : y1[b][i];
+        double s = k8[i] / (cfg.atol + std::max(std::fabs(y[b][i]), std::fabs(yc)) * cfg.rtol);
+        s *= err_w[m];
+        ss += s * s;
+      }
+    }
+    double err = std::sqrt(ss / (6.0 * B));
+    if (!std::isfinite(err)) { R.status = ST_NONFINITE; break; }
+    bool keep = err < 1.0;
+    double inv = 1.0 / err;
+    double f1 = beta1 == 0.0 ? 1.0 : std::pow(inv, beta1);
+    double f2 = beta2 == 0.0 ? 1.0 : std::pow(prev_inv, beta2);
+    double f3 = beta3 == 0.0 ? 1.0 : std::pow(prev_prev_inv, beta3);
+    double factor = cfg.safety * f1 * f2 * f3;
+    double fmin = keep ? 1.0 : cfg.fmin;
+    factor = std::min(std::max(factor, fmin), cfg.fmax);
+    double dtn = dt * factor;
+    if (inv == 0.0 || std::isinf(inv)) inv = 1.0;
+    ++steps;
+    if (keep) {
+      ++R.accepted;
+      while (next_out < nout && tau_out[order[next_out]] <= t1) {
+        double tt = tau_out[order[next_out]];
+        double cf = (tt - t0) / (t1 - t0);
+        for (int b = 0; b < B; ++b) {
+          for (int i = 0; i < n; ++i) sc[i] = y[b][i] + cf * (y1[b][i] - y[b][i]);
+          outputs(c, D, ks[b], sc.data(), yout + ((size_t)b * nout + order[next_out]) * 20);
+        }
+        ++next_out;
+      }
+      for (int b = 0; b < B; ++b) std::swap(y[b], y1[b]);
+      t0 = t1;
+      prev_prev_inv = prev_inv;
+      prev_inv = inv;
+    } else {
+      ++R.rejected;
+      if (cfg.hist_on_reject) { prev_prev_inv = prev_inv; prev_inv = inv; }
+    }
+    double tn = t0 + dtn;
+    if (tn > T1 - 1e-10) tn = T1;
+    if (!(tn > t0)) { if (t0 < T1) { R.status = ST_DT_UNDERFLOW; break; } }
+    t1 = tn;
+  }
+  return R;
+}
+
 }  // namespace
 
 extern "C" {
+
+// Groups of batch_size consecutive modes of one cosmology sharing one step
+// sequence (evolve_perturbations_batched, perturbations.py:1000-1061);
+// arguments as oracle_solve, nmode a multiple of batch_size, no return_full.
+int oracle_solve_grouped(const double* tables, int ncosmo, int blob_len, const double* kmodes, const int* cosmo_of_mode,
+                         int nmode, const double* tau_out, int nout, const int* dims, const double* cfgv, int max_steps,
+                         int batch_size, double* y_out, int* stats, int nthreads) {
+  if (ncosmo <= 0 || nmode < 0 || nout <= 0 || batch_size < 1 || nmode % batch_size) return -1;
+  std::vector<Cosmo> cs(ncosmo);
+  for (int i = 0; i < ncosmo; ++i) if (!load_cosmo(tables + (size_t)i * blob_len, cs[i])) return -2;
+  Dims D = make_dims(dims[0], dims[1], dims[2], dims[3], dims[4]);
+  if (D.lg < 3 || D.lgp < 3 || D.lr < 3 || D.lnu < 3) return -3;
+  for (int i = 0; i < ncosmo; ++i) if (cs[i].nq != D.nq) return -4;
+  Cfg cfg{cfgv[0], cfgv[1], cfgv[2], cfgv[3], cfgv[4], cfgv[5], cfgv[6], cfgv[7], cfgv[8], max_steps, (int)cfgv[9], 0};
+  const int ngroup = nmode / batch_size;
+  for (int g = 0; g < ngroup; ++g) {
+    const int c0 = cosmo_of_mode ? cosmo_of_mode[g * batch_size] : 0;
+    for (int b = 1; b < batch_size; ++b) if ((cosmo_of_mode ? cosmo_of_mode[g * batch_size + b] : 0) != c0) return -5;
+  }
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int g = 0; g < ngroup; ++g) {
+    const int m0 = g * batch_size;
+    const int ci = cosmo_of_mode ? cosmo_of_mode[m0] : 0;
+    double* dst = y_out + (size_t)m0 * nout * 20;
+    std::fill(dst, dst + (size_t)batch_size * nout * 20, std::numeric_limits<double>::quiet_NaN());
+    ModeResult r = solve_group(cs[ci], D, kmodes + m0, batch_size, tau_out + (size_t)ci * nout, nout, cfg, dst);
+    for (int b = 0; b < batch_size; ++b) {
+      stats[3 * (m0 + b)] = r.status; stats[3 * (m0 + b) + 1] = r.accepted; stats[3 * (m0 + b) + 2] = r.rejected;
+    }
+  }
+  (void)nthreads;
+  return 0;
+}
 
 int oracle_n_vars(int lg, int lgp, int lr, int lnu, int nq) { return make_dims(lg, lgp, lr, lnu, nq).n; }
 

@@ -139,4 +139,40 @@ int h_solve(const double* tables, int ncosmo, int blob_len, const double* kmodes
   return 0;
 }
 
+// groups of batch_size consecutive modes sharing one step sequence (the
+// kernel's group driver); nmode must be a multiple of batch_size
+int h_solve_grouped(const double* tables, int ncosmo, int blob_len, const double* kmodes, const int* cosmo, int nmode,
+                    const double* tau_out, int nout, const int* dims, const double* cfg, int max_steps, int batch_size,
+                    double* y_out, int* stats) {
+  if (batch_size < 1 || batch_size > 32 || nmode % batch_size) return -1;
+  Ctl ctl;
+  ctl.rtol = cfg[0]; ctl.atol = cfg[1];
+  ctl.b1 = (cfg[3] + cfg[2] + cfg[4]) / cfg[7]; ctl.b2 = -(cfg[2] + 2.0 * cfg[4]) / cfg[7]; ctl.b3 = cfg[4] / cfg[7];
+  ctl.fmax = cfg[5]; ctl.fmin = cfg[6]; ctl.safety = cfg[8]; ctl.hist_on_reject = (int)cfg[9];
+  ctl.max_steps = max_steps; ctl.dense = 0; ctl.return_full = 0; ctl.nout = nout;
+  ctl.record = 0; ctl.replay = 0; ctl.step_ts = (int)cfg[10];
+  const int B = batch_size;
+  Tab T; Rodas R; fill_tables(T); fill_rodas(R);
+  const Dims D = make_dims(dims[0], dims[1], dims[2], dims[3], dims[4]);
+  for (int m0 = 0; m0 < nmode; m0 += B) {
+    std::vector<Ctx> xs(B);
+    const int ci = cosmo ? cosmo[m0] : 0;
+    for (int b = 0; b < B; ++b) {
+      if ((cosmo ? cosmo[m0 + b] : 0) != ci) return -3;
+      if (!setup(xs[b], tables + (long)ci * blob_len, blob_len, dims, kmodes[m0 + b], false)) return -2;
+      double* dst = y_out + (long)(m0 + b) * nout * 20;
+      for (int i = 0; i < nout * 20; ++i) dst[i] = std::numeric_limits<double>::quiet_NaN();
+    }
+    auto ctx = [&](int b) {
+      ModeCtx<1> x{xs[b].c, xs[b].m, xs[b].w, tau_out + (long)ci * nout, y_out + (long)(m0 + b) * nout * 20};
+      return x;
+    };
+    Run r;
+    r.rec = nullptr; r.rec_cap = 0; r.nrec = 0;
+    group_solve<1>(GP, D, T, R, ctl, B, ctx, 1, r);
+    for (int b = 0; b < B; ++b) { stats[3 * (m0 + b)] = r.status; stats[3 * (m0 + b) + 1] = r.acc; stats[3 * (m0 + b) + 2] = r.rej; }
+  }
+  return 0;
+}
+
 }  // extern "C"

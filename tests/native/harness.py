@@ -7,6 +7,9 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _SRC = os.path.join(_HERE, "core_harness.cpp")
+_TSRC = os.path.join(_HERE, "tables_harness.cpp")
+_TCORE = os.path.join(_HERE, "..", "..", "disco-eb_gb300", "csrc", "deb_tables_core.cuh")
+_INC = os.path.join(_HERE, "..", "..", "include")
 _CORE = os.path.join(_HERE, "..", "..", "disco-eb_gb300", "csrc", "deb_core.cuh")
 _LIB = os.path.join(_HERE, "_build", "libcore_harness.so")
 _lib = None
@@ -18,8 +21,9 @@ def lib():
     global _lib
     if _lib is None:
         os.makedirs(os.path.dirname(_LIB), exist_ok=True)
-        if not os.path.exists(_LIB) or os.path.getmtime(_LIB) < max(os.path.getmtime(_SRC), os.path.getmtime(_CORE)):
-            subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", _LIB, _SRC])
+        deps = (_SRC, _CORE, _TSRC, _TCORE)
+        if not os.path.exists(_LIB) or os.path.getmtime(_LIB) < max(os.path.getmtime(d) for d in deps):
+            subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", _INC, "-o", _LIB, _SRC, _TSRC])
         L = ctypes.CDLL(_LIB)
         L.h_rhs.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, ctypes.c_double, dp, dp, dp]
         L.h_solve_W.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, ctypes.c_double, dp, ctypes.c_double, dp, dp, ctypes.c_int]
@@ -29,8 +33,26 @@ def lib():
         L.h_start.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, dp, dp]
         L.h_solve.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp, ip, ctypes.c_int, dp, ctypes.c_int, ip, dp, ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, dp, ip]
+        ci, cd = ctypes.c_int, ctypes.c_double
+        L.h_solve_grouped.argtypes = [dp, ci, ci, dp, ip, ci, dp, ci, ip, dp, ci, ci, dp, ip]
+        L.h_tables.argtypes = [dp, ci, dp, dp, ci, ci, ci, ci, ci, cd, cd, cd, dp, ci, ip]
         _lib = L
     return _lib
+
+
+def tables(params, nqmax, num_thermo=256, rtol=1e-3, atol=1e-6, max_steps=128):
+    """Table blobs of the GPU producer's code run on the host (one lane)."""
+    from discoeb_gb300 import tables_gpu as tg
+
+    pm = np.ascontiguousarray(tg.param_matrix(params))
+    consts, grid = tg.constants(), tg.grid(num_thermo, nqmax)
+    L = tg.blob_len(num_thermo, nqmax)
+    out = np.zeros((pm.shape[0], L))
+    st = np.zeros(pm.shape[0], dtype=np.int32)
+    rc = lib().h_tables(_p(pm), pm.shape[0], _p(consts), _p(grid), num_thermo, tg.NUM_NU, tg.NQ_BG, nqmax, max_steps,
+                        tg.AMIN, rtol, atol, _p(out), L, _p(st, ctypes.c_int))
+    assert rc == 0, rc
+    return out, st
 
 
 def _p(a, t=ctypes.c_double):
@@ -111,3 +133,22 @@ def solve_rr(tables, nset, kmodes, tau_out, *, rec=None, nrec=None, record=False
                           _p(nrec, ctypes.c_int), int(record), int(replay), _p(y), _p(st, ctypes.c_int))
     assert rc == 0, rc
     return y, st, rec, nrec
+
+
+def solve_grouped(tables, kmodes, tau_out, batch_size, *, cosmo_of_mode=None, lmaxg=11, lmaxgp=11, lmaxr=11, lmaxnu=8,
+                  nqmax=3, rtol=1e-4, atol=1e-4, pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3,
+                  max_steps=2048):
+    """The kernel's group driver on the host: y [nmode, nout, 20], stats [nmode, 3]."""
+    tables = np.ascontiguousarray(np.atleast_2d(tables), dtype=np.float64)
+    kmodes = np.ascontiguousarray(kmodes, dtype=np.float64)
+    tau_out = np.ascontiguousarray(np.atleast_2d(tau_out), dtype=np.float64)
+    nmode, nout = kmodes.shape[0], tau_out.shape[1]
+    com = np.ascontiguousarray(np.zeros(nmode) if cosmo_of_mode is None else cosmo_of_mode, dtype=np.int32)
+    cfg = np.array([rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, 5.0, 0.9, 0.0, 0.0])
+    y = np.empty((nmode, nout, 20))
+    st = np.zeros((nmode, 3), dtype=np.int32)
+    rc = lib().h_solve_grouped(_p(tables), tables.shape[0], tables.shape[1], _p(kmodes), _p(com, ctypes.c_int), nmode,
+                               _p(tau_out), nout, _p(_d([lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax]), ctypes.c_int), _p(cfg),
+                               int(max_steps), int(batch_size), _p(y), _p(st, ctypes.c_int))
+    assert rc == 0, rc
+    return y, st

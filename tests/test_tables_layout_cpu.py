@@ -1,0 +1,74 @@
+"""Host side of the GPU table producer: constants order, grids and blob length (no GPU)."""
+import os
+import re
+
+import numpy as np
+
+from discoeb_gb300 import recfast, tables, tables_gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _enum(name):
+    txt = open(os.path.join(ROOT, "include", "discoeb_gb300.h")).read()
+    body = re.search(r"enum %s \{(.*?)\};" % name, txt, re.S).group(1)
+    return [x.split("=")[0].strip() for x in body.replace("\n", " ").split(",") if x.strip()]
+
+
+def test_constants_follow_the_header_order():
+    names = _enum("deb_tables_const")
+    assert names[-1] == "DEB_TC_COUNT"
+    py = list(tables_gpu.CONST_NAMES) + ["PI", "SQRT_PI", "C2OK"]
+    assert len(py) == len(names) - 1 == tables_gpu.constants().shape[0]
+    norm = lambda s: s.replace("DEB_TC_", "").replace("_", "").upper()
+    alias = {"GN": "GN", "MH": "MH", "ME": "ME", "CLIGHT": "C", "KB": "KB", "T0": "T0", "T1": "T1"}
+    for a, b in zip(py, names[:-1]):
+        assert alias.get(norm(a), norm(a)) == norm(b), (a, b)
+    assert tables_gpu.constants()[names.index("DEB_TC_CR")] == recfast.CR
+
+
+def test_params_follow_the_header_order():
+    names = _enum("deb_bg_param")
+    assert names[-1] == "DEB_BG_NPARAM" and len(names) - 1 == len(tables_gpu.PARAM_KEYS)
+    m = tables_gpu.param_matrix([dict(Omegam=0.3, Omegab=0.05, H0=70.0, Tcmb=2.7255, YHe=0.248, Neff=3.046, Nmnu=0,
+                                      mnu=0.0, w_DE_0=-0.9, w_DE_a=0.0, A_s=2e-9, n_s=0.96)])
+    assert m.shape == (1, len(tables_gpu.PARAM_KEYS))
+    assert m[0, tables_gpu.PARAM_KEYS.index("cs2_DE")] == 1.0 and m[0, tables_gpu.PARAM_KEYS.index("k_p")] == 0.05
+
+
+def test_grid_and_blob_length_match_the_host_producer():
+    g = tables_gpu.grid(256, 15)
+    assert g.shape[0] == 2 * tables_gpu.NUM_NU + 2 * tables_gpu.NQ_BG + 2 * 15 + 257 + 256
+    a_th = g[2 * 512 + 16 + 30:2 * 512 + 16 + 30 + 257]
+    np.testing.assert_array_equal(a_th, recfast.adaptive_sampling(1e-9, 1.01, 257))
+    assert tables_gpu.blob_len(256, 15) == tables.blob_length([256, 256, 512, 512, 256, 256, 256], 15)
+
+
+def test_producer_code_on_the_host_equals_the_python_producer():
+    """The GPU producer's per-set code (deb_tables_core.cuh) built for the host
+    against the Python producer (background.py + recfast.py): same algorithm,
+    same math library, so agreement to rounding (1e-10 of each array's
+    largest value; second derivatives 1e-9)."""
+    import sys
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from native import harness as H
+    from discoeb_gb300 import background as bg
+    from discoeb_gb300.workloads import fiducial_mnu_param, lcdm_massless_param, sample_cosmologies
+
+    ps = [lcdm_massless_param(), fiducial_mnu_param()] + sample_cosmologies(1, seed=5)[0]
+    dev, st = H.tables(ps, 15)
+    host = np.stack([tables.pack_cosmology(bg.evolve_background(param=p), 15) for p in ps])
+    assert (st == 0).all() and dev.shape == host.shape
+    np.testing.assert_array_equal(dev[:, 19:32], host[:, 19:32])
+    np.testing.assert_allclose(dev[:, :19], host[:, :19], rtol=1e-13, atol=1e-300)
+    sizes = host[0, 20:27].astype(int)
+    p = 32
+    for n in sizes:
+        for part in range(3):
+            h, d = host[:, p:p + n], dev[:, p:p + n]
+            scale = np.abs(h).max(axis=1, keepdims=True)
+            assert (np.abs(d - h) <= (1e-9 if part == 2 else 1e-10) * scale).all(), (n, part)
+            p += n
+    p += 2 * int(host[0, 19])
+    np.testing.assert_array_equal(dev[:, 32 + 3 * sizes.sum():p], host[:, 32 + 3 * sizes.sum():p])
