@@ -79,7 +79,7 @@ TABLE_NAMES = ("tab0", "tau0", "tabs", "taus")
 SMALL_NAMES = ("k", "com", "eps", "inv_As", "lnk")
 
 
-def _host_inputs(plist, backgrounds, pert, kmodes, aexp_out, nqmax, theta):
+def _host_inputs(plist, backgrounds, pert, kmodes, aexp_out, nqmax):
     """Packed host arrays of one gradient problem: k, cosmology index, eps per
     parameter, 1/A_s and ln(k/k_p) per mode, and -- unless ``backgrounds``
     is ``"gpu"`` -- the table blobs and output times of every set."""
@@ -150,7 +150,7 @@ class GradientProblem:
         self.npar = len(pert[0])
         self.nset = 2 * self.npar
         self.idx = idx
-        h = _host_inputs(plist, backgrounds, pert, self.kmodes, aexp_out, nqmax, self.theta)
+        h = _host_inputs(plist, backgrounds, pert, self.kmodes, aexp_out, nqmax)
         self.host_k, self.host_com = h["k"], h["com"]
         self.nmode = self.host_k.shape[0]
         dev = torch.device("cuda", torch.cuda.current_device())
@@ -188,7 +188,6 @@ class GradientProblem:
         self.order = torch.as_tensor(_pt.schedule_order(self.host_k)).to(dev, torch.int32)
         self.graph = None
         self._copied = None
-        self.key = None
 
     def load(self, plist, backgrounds, pert, stream=None):
         """Copy the inputs of another set of cosmologies of the same shape
@@ -202,7 +201,7 @@ class GradientProblem:
         if _gpu_tables(backgrounds) != self.gpu_tables:
             raise ValueError("load: the problem was built with tables from the " +
                              ("GPU" if self.gpu_tables else "host"))
-        h = _host_inputs(plist, backgrounds, pert, self.kmodes, self.aexp_out, self.nqmax, self.theta)
+        h = _host_inputs(plist, backgrounds, pert, self.kmodes, self.aexp_out, self.nqmax)
         s = stream if stream is not None else torch.cuda.current_stream()
         if self._copied is not None:
             self._copied.synchronize()   # the previous load's copies have left the pinned buffers
