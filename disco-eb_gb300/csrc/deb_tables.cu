@@ -11,6 +11,9 @@
 
 #include <cuda_runtime.h>
 
+#include <thread>
+#include <vector>
+
 #include "deb_tables_core.cuh"
 
 namespace {
@@ -56,19 +59,23 @@ int deb_tables_blob_len(int num_thermo, int num_nu, int nqmax) {
   return (int)L;
 }
 
-int deb_evolve_background(const deb_bg_cfg* cfg, const double* d_params, int nset, const double* d_consts,
-                          const double* d_grid, double* d_tables, int blob_len, int* d_status, void* stream) {
-  if (!cfg || !d_params || !d_consts || !d_grid || !d_tables || nset < 0) return DEB_ERR_INVALID;
-  if (nset == 0) return DEB_OK;
+}  // extern "C"
+
+namespace {
+
+// The producer's arguments, checked; the same for the device and the host entry.
+int make_params(const deb_bg_cfg* cfg, const double* params, int nset, const double* consts, const double* grid,
+                double* tables, int blob_len, int* status, TParams& P) {
+  if (!cfg || !params || !consts || !grid || !tables || nset < 0) return DEB_ERR_INVALID;
   const int N = cfg->num_thermo, NN = cfg->num_nu;
   if (cfg->nq_bg < 1 || cfg->max_steps < 1 || !(cfg->amin > 0.0)) return DEB_ERR_INVALID;
   const int L = deb_tables_blob_len(N, NN, cfg->nqmax);
   if (L < 0 || blob_len != L) return DEB_ERR_INVALID;
-  TParams P{};
-  P.params = d_params; P.nset = nset; P.consts = d_consts;
+  P = TParams{};
+  P.params = params; P.nset = nset; P.consts = consts;
   // grid: a_nu [NN], log a_nu [NN], (q, w) background [2 nq_bg], (q, w) perturbations [2 nqmax],
   // a_thermo [N + 1], log a_thermo[1:] [N]
-  const double* g = d_grid;
+  const double* g = grid;
   P.a_nu = g; g += NN;
   P.la_nu = g; g += NN;
   P.qw_bg = g; g += 2 * cfg->nq_bg;
@@ -77,14 +84,48 @@ int deb_evolve_background(const deb_bg_cfg* cfg, const double* d_params, int nse
   P.la_th = g;
   P.num_nu = NN; P.num_thermo = N; P.nq_bg = cfg->nq_bg; P.nqmax = cfg->nqmax; P.max_steps = cfg->max_steps;
   P.amin = cfg->amin; P.rtol = cfg->rtol; P.atol = cfg->atol;
-  P.tables = d_tables; P.blob_len = blob_len; P.status = d_status;
-  const size_t smem = (size_t)debt::tables_smem_doubles(N, NN) * sizeof(double);
+  P.tables = tables; P.blob_len = blob_len; P.status = status;
+  return DEB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int deb_evolve_background(const deb_bg_cfg* cfg, const double* d_params, int nset, const double* d_consts,
+                          const double* d_grid, double* d_tables, int blob_len, int* d_status, void* stream) {
+  TParams P;
+  const int rc = make_params(cfg, d_params, nset, d_consts, d_grid, d_tables, blob_len, d_status, P);
+  if (rc) return rc;
+  if (nset == 0) return DEB_OK;
+  const size_t smem = (size_t)debt::tables_smem_doubles(P.num_thermo, P.num_nu) * sizeof(double);
   if (smem > 48 * 1024) {
     if (cudaFuncSetAttribute(tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
       return DEB_ERR_INVALID;
   }
   tables_kernel<<<nset, 32, smem, (cudaStream_t)stream>>>(P);
   if (cudaGetLastError() != cudaSuccess) return DEB_ERR_CUDA;
+  return DEB_OK;
+}
+
+int deb_evolve_background_host(const deb_bg_cfg* cfg, const double* params, int nset, const double* consts,
+                               const double* grid, double* tables, int blob_len, int* status, int nthreads) {
+  TParams P;
+  const int rc = make_params(cfg, params, nset, consts, grid, tables, blob_len, status, P);
+  if (rc) return rc;
+  if (nset == 0) return DEB_OK;
+  int nt = nthreads > 0 ? nthreads : (int)std::thread::hardware_concurrency();
+  if (nt < 1) nt = 1;
+  if (nt > nset) nt = nset;
+  const size_t nsh = (size_t)debt::tables_smem_doubles(P.num_thermo, P.num_nu);
+  auto work = [&](int t) {
+    std::vector<double> sh(nsh);
+    for (int s = t; s < nset; s += nt) debt::produce_set(P, s, 0, 1, sh.data());
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
   return DEB_OK;
 }
 

@@ -91,7 +91,14 @@ def _host_inputs(plist, backgrounds, pert, kmodes, aexp_out, nqmax):
     h = dict(k=k, com=com,
              eps=np.ascontiguousarray(np.array([[e for (_, e, _, _) in pp] for pp in pert], dtype=np.float64)[com].T),
              inv_As=(1.0 / As)[:, None], lnk=np.log(k / kp)[:, None])
-    if not _gpu_tables(backgrounds):
+    if _native_tables(backgrounds):
+        from . import tables_gpu
+
+        sets = [q for pp in pert for (_, _, a, b) in pp for q in (a, b)]
+        tabs_all, _ = tables_gpu.evolve_background_tables_host(list(plist) + sets, nqmax)
+        h.update(tab0=tabs_all[:nc], tau0=_tables.tau_of_a_blob(tabs_all[:nc], aexp_out),
+                 tabs=tabs_all[nc:], taus=_tables.tau_of_a_blob(tabs_all[nc:], aexp_out))
+    elif not _gpu_tables(backgrounds):
         nominal = [b[0] for b in backgrounds]
         sets = [b[1:] for b in backgrounds]
         h.update(tab0=_tables.pack_batch(nominal, nqmax),
@@ -105,17 +112,26 @@ def _gpu_tables(backgrounds):
     return isinstance(backgrounds, str) and backgrounds == "gpu"
 
 
+def _native_tables(backgrounds):
+    return isinstance(backgrounds, str) and backgrounds == "native"
+
+
 def _device_tables(plist, pert, aexp_out, nqmax, out=None):
     """Tables and output times of the nominal and every theta +- eps set,
-    produced on the GPU from the parameter dicts (two producer launches);
-    ``out`` = (tab0, tau0, tabs, taus) fills existing buffers."""
+    produced on the GPU from the parameter dicts in one producer launch (its
+    time is one set's latency, whatever the number of sets).  The sets are
+    laid out nominal rows first, then the perturbed rows of cosmology c at
+    c * nset + s, so tab0 and tabs are the two contiguous halves of one
+    buffer.  ``out`` = (tables, tau) of an earlier call fills those buffers."""
     from . import tables_gpu
 
     sets = [q for pp in pert for (_, _, a, b) in pp for q in (a, b)]
-    o = out or (None, None, None, None)
-    tab0, tau0, st0 = tables_gpu.evolve_background_tables(plist, nqmax, aexp_out=aexp_out, out=o[0], tau_out=o[1])
-    tabs, taus, st1 = tables_gpu.evolve_background_tables(sets, nqmax, aexp_out=aexp_out, out=o[2], tau_out=o[3])
-    return dict(tab0=tab0, tau0=tau0, tabs=tabs, taus=taus), (st0, st1)
+    o = out or (None, None)
+    tabs_all, tau_all, st = tables_gpu.evolve_background_tables(list(plist) + sets, nqmax, aexp_out=aexp_out,
+                                                                out=o[0], tau_out=o[1])
+    nc = len(plist)
+    return dict(tables_all=tabs_all, tau_all=tau_all, tab0=tabs_all[:nc], tau0=tau_all[:nc], tabs=tabs_all[nc:],
+                taus=tau_all[nc:]), st
 
 
 class GradientProblem:
@@ -123,9 +139,10 @@ class GradientProblem:
 
     ``backgrounds``: per cosmology the evolved ``param`` dicts
     [nominal, theta_1 + eps_1, theta_1 - eps_1, ...] (see
-    :func:`perturbed_params`), or ``"gpu"``: the tables of all those sets
-    are then produced on the GPU from ``plist`` and ``pert``
-    (:mod:`tables_gpu`), with no host background solve.  :meth:`run` enqueues the recorded nominal
+    :func:`perturbed_params`), or ``"native"`` / ``"gpu"``: the tables of all
+    those sets are then produced from ``plist`` and ``pert`` by the
+    library's table producer on the host cores or on the GPU
+    (:mod:`tables_gpu`).  :meth:`run` enqueues the recorded nominal
     solve, the replay of every perturbed set, ``get_power`` and the
     difference quotients on one stream, without synchronising;
     :meth:`capture` records that sequence once as a CUDA graph and
@@ -157,6 +174,7 @@ class GradientProblem:
         self.device = dev
         # pinned staging copies of every per-call host input, and their device twins
         self.gpu_tables = _gpu_tables(backgrounds)
+        self.table_source = backgrounds if isinstance(backgrounds, str) else "dicts"
         self._names = SMALL_NAMES + (() if self.gpu_tables else TABLE_NAMES)
         self._pinned = {n: torch.from_numpy(np.ascontiguousarray(h[n])).pin_memory() for n in self._names}
         self._dev = {n: self._pinned[n].to(dev) for n in self._names}
@@ -198,9 +216,8 @@ class GradientProblem:
         copied from the host."""
         import torch
 
-        if _gpu_tables(backgrounds) != self.gpu_tables:
-            raise ValueError("load: the problem was built with tables from the " +
-                             ("GPU" if self.gpu_tables else "host"))
+        if (backgrounds if isinstance(backgrounds, str) else "dicts") != self.table_source:
+            raise ValueError(f"load: the problem was built with {self.table_source} tables")
         h = _host_inputs(plist, backgrounds, pert, self.kmodes, self.aexp_out, self.nqmax)
         s = stream if stream is not None else torch.cuda.current_stream()
         if self._copied is not None:
@@ -221,7 +238,7 @@ class GradientProblem:
                 from . import tables_gpu
 
                 _, self._table_status = _device_tables(plist, pert, self.aexp_out, self.nqmax,
-                                                       out=tuple(self._dev[n] for n in TABLE_NAMES))
+                                                       out=(self._dev["tables_all"], self._dev["tau_all"]))
                 nbytes += tables_gpu.param_matrix(plist).nbytes * (1 + self.nset)
         return nbytes
 
@@ -335,7 +352,8 @@ def _run_cached(plist, backgrounds, pert, kmodes, aexp_out, opts):
 
     aexp = np.atleast_1d(np.asarray(aexp_out, dtype=np.float64))
     key = (torch.cuda.current_device(), len(plist), np.asarray(kmodes, dtype=np.float64).tobytes(), aexp.shape[0],
-           tuple(sorted(opts.items())), tuple(n for (n, _, _, _) in pert[0]), _gpu_tables(backgrounds))
+           tuple(sorted(opts.items())), tuple(n for (n, _, _, _) in pert[0]),
+           backgrounds if isinstance(backgrounds, str) else "dicts")
     gp = _problems.get(key)
     if gp is not None:
         try:
@@ -366,7 +384,7 @@ def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num
                               factormax: float = 20.0, factormin: float = 0.3, max_steps: int = 2048, idx: int = 4,
                               theta=THETA, rel_step: float = 1e-4, dologk: bool = True, processes=None,
                               backgrounds=None, throw: bool = True, step_to_outputs: bool = False,
-                              tables: str = "host"):
+                              tables: str = "native"):
     """P(k, a) and d log P / d theta for one or many cosmologies.
 
     ``params``: input parameter dict(s) as given to ``evolve_background``
@@ -375,9 +393,10 @@ def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num
     kmodes)``; with a single dict the cosmology axis is dropped.
     ``backgrounds`` may pass precomputed host tables: a list (per cosmology)
     of [nominal, +eps_1, -eps_1, +eps_2, ...] evolved ``param`` dicts.
-    Without them the tables of all those sets come from the host producer
-    (``tables="host"``, a process pool) or from the GPU producer in one
-    launch (``tables="gpu"``).
+    Without them the tables of all those sets come from the library's
+    producer on the host cores (``tables="native"``, C++ threads, a few ms
+    per set; the default), on the GPU in one launch (``tables="gpu"``), or
+    from the Python producer in a process pool (``tables="python"``).
     With the reference's output semantics (linear interpolation inside the
     step) an interior output's derivative includes the slope of that
     interpolant; ``step_to_outputs=True`` lands steps on the output times.
@@ -388,8 +407,10 @@ def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num
     kmodes = np.geomspace(kmin, kmax, num_k) if dologk else np.linspace(kmin, kmax, num_k)
     pert = [perturbed_params(p, theta, rel_step) for p in plist]
     nset = 2 * len(pert[0])
-    if backgrounds is None and tables == "gpu":
-        backgrounds = "gpu"
+    if tables not in ("native", "gpu", "python"):
+        raise ValueError(f"tables must be 'native', 'gpu' or 'python', not {tables!r}")
+    if backgrounds is None and tables in ("native", "gpu"):
+        backgrounds = tables
     elif backgrounds is None:
         flat = []
         for p, pp in zip(plist, pert):

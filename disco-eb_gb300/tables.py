@@ -143,3 +143,22 @@ def tau_of_a(param: dict, aexp) -> np.ndarray:
     s = SplineInterpolation.__new__(SplineInterpolation)
     s._x_, s._y_, s._S_full_ = _arr(sp._x_), _arr(sp._y_), _arr(sp._S_full_)
     return s.evaluate(np.atleast_1d(np.asarray(aexp, dtype=np.float64)))
+
+
+def tau_of_a_blob(blobs: np.ndarray, aexp) -> np.ndarray:
+    """tau(a) at the scale factors ``aexp`` from the tau_of_a spline stored in
+    each blob of ``blobs`` [nset, blob_len] (the A/B form of
+    spline_interpolation.py:130-153); returns [nset, len(aexp)]."""
+    from .spline import SplineInterpolation
+
+    blobs = np.atleast_2d(blobs)
+    aexp = np.atleast_1d(np.asarray(aexp, dtype=np.float64))
+    out = np.empty((blobs.shape[0], aexp.shape[0]))
+    for i, b in enumerate(blobs):
+        sizes = b[H_NSPL0:H_NSPL0 + 7].astype(int)
+        p = HDR_LEN + 3 * int(sizes[:SP_TAU_OF_A].sum())
+        n = int(sizes[SP_TAU_OF_A])
+        s = SplineInterpolation.__new__(SplineInterpolation)
+        s._x_, s._y_, s._S_full_ = b[p:p + n], b[p + n:p + 2 * n], b[p + 2 * n:p + 3 * n]
+        out[i] = s.evaluate(aexp)
+    return out

@@ -120,3 +120,28 @@ def evolve_background_tables(params, nqmax: int, *, num_thermo: int = 256, aexp_
             _native.check(L.deb_tau_of_a(c(tabs), nset, bl, c(aexp), int(aexp.shape[0]), c(tau),
                                          ctypes.c_void_p(s.cuda_stream)), "deb_tau_of_a")
     return tabs, tau, status
+
+
+def evolve_background_tables_host(params, nqmax: int, *, num_thermo: int = 256, rtol: float = 1e-3,
+                                  atol: float = 1e-6, max_steps: int = 128, nthreads: int = 0, out=None):
+    """The same producer on the host cores (``deb_evolve_background_host``):
+    ``[nset, blob_len]`` numpy blobs (written into ``out``, e.g. pinned
+    memory, when given) and the status per set.  One CPU core builds a set
+    in a few milliseconds; worker threads split the sets."""
+    L = _native.load()
+    pm = np.ascontiguousarray(param_matrix(params))
+    nset = pm.shape[0]
+    bl = blob_len(num_thermo, nqmax)
+    key = ("host", num_thermo, nqmax)
+    if key not in _static:
+        _static[key] = (constants(), grid(num_thermo, nqmax))
+    consts, grd = _static[key]
+    tabs = out if out is not None else np.empty((nset, bl), dtype=np.float64)
+    if tabs.shape != (nset, bl) or tabs.dtype != np.float64 or not tabs.flags.c_contiguous:
+        raise ValueError(f"out must be a C-contiguous float64 array of shape {(nset, bl)}")
+    status = np.zeros(nset, dtype=np.int32)
+    cfg = DebBgCfg(num_thermo, NUM_NU, NQ_BG, nqmax, max_steps, AMIN, rtol, atol)
+    p = lambda a: ctypes.c_void_p(a.ctypes.data)
+    _native.check(L.deb_evolve_background_host(ctypes.byref(cfg), p(pm), nset, p(consts), p(grd), p(tabs), bl,
+                                               p(status), int(nthreads)), "deb_evolve_background_host")
+    return tabs, status

@@ -264,7 +264,7 @@ int deb_fftlog_phase(int nfreq, double log_kmax_over_kmin, int ell, double* d_ph
  *
  *   - structured solver only (dims->linear_solver must be
  *     DEB_SOLVE_STRUCTURED); one warp per mode with its state in the array;
- *   - modes in flight are limited by the array (e.g. 348 at nvar 323, 1339 at
+ *   - modes in flight are limited by the array (e.g. 380 at nvar 323, 1376 at
  *     nvar 80); any nmode is processed through the work queue;
  *   - returns DEB_ERR_STATIC_SCRATCH when one mode's state does not fit the
  *     array;
@@ -328,6 +328,13 @@ typedef struct deb_bg_cfg {
 int deb_tables_blob_len(int num_thermo, int num_nu, int nqmax);
 int deb_evolve_background(const deb_bg_cfg* cfg, const double* d_params, int nset, const double* d_consts,
                           const double* d_grid, double* d_tables, int blob_len, int* d_status, void* stream);
+/* The same producer on the host cores (same code, compiled for the CPU): HOST
+   buffers, nthreads worker threads over the sets (<= 0: one per hardware
+   thread).  A RECFAST history is one long sequential chain of small FP64
+   steps, which a CPU core runs far faster than one GPU lane; for a few
+   hundred sets this is the faster producer. */
+int deb_evolve_background_host(const deb_bg_cfg* cfg, const double* params, int nset, const double* consts,
+                               const double* grid, double* tables, int blob_len, int* status, int nthreads);
 /* tau_of_a (perturbations.py:975) of each blob at nout scale factors: d_tau [nset, nout] */
 int deb_tau_of_a(const double* d_tables, int nset, int blob_len, const double* d_aexp, int nout, double* d_tau,
                  void* stream);

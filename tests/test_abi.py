@@ -44,3 +44,30 @@ def test_host_side_argument_checks_without_gpu():
     assert L.deb_forward(None, None, 1, 40, None, None, 4, None, None, None, None, None, None) == -1
     assert L.deb_error_string(-5) == b"plan capacity exceeded"
     assert L.deb_nvar(ctypes.byref(_native.DebDims(12, 12, 17, 17, 15, 1, 0, 0))) == 323
+
+
+def test_new_entry_points_check_their_arguments_without_gpu():
+    """Argument checks of the launch-shape, grouped and table-producer entry
+    points return before touching the device."""
+    from discoeb_gb300 import _native, tables_gpu
+
+    L = _native.load()
+    dims = _native.DebDims(12, 12, 17, 17, 15, 1, 0, 0, 0)
+    plan = ctypes.c_void_p()
+    bad_shape = _native.DebLaunchCfg(7, 0)
+    assert L.deb_plan_create_ex(ctypes.byref(dims), 8, ctypes.byref(bad_shape), ctypes.byref(plan)) == -1
+    assert L.deb_plan_create_ex(ctypes.byref(dims), 8, ctypes.byref(_native.DebLaunchCfg(0, -1)),
+                                ctypes.byref(plan)) == -1
+    for bs in (0, 33):
+        assert L.deb_plan_create_grouped(ctypes.byref(dims), 64, bs, ctypes.byref(plan)) == -1
+    dense = _native.DebDims(12, 12, 17, 17, 15, 1, 0, 1, 0)
+    assert L.deb_plan_create_grouped(ctypes.byref(dense), 64, 16, ctypes.byref(plan)) == -1
+    assert L.deb_forward_grouped(None, None, 1, 40, None, None, 16, None, None, None, None, None, None) == -1
+    assert L.deb_plan_launch_info(None, None, None) == -1
+    assert L.deb_tables_blob_len(2, 512, 15) == -1
+    assert L.deb_tables_blob_len(256, 512, 15) == tables_gpu.blob_len(256, 15)
+    cfg = tables_gpu.DebBgCfg(256, 512, 8, 15, 128, 1e-9, 1e-3, 1e-6)
+    # wrong blob length is refused by both producers
+    assert L.deb_evolve_background(ctypes.byref(cfg), 1, 1, 1, 1, 1, 123, None, None) == -1
+    assert L.deb_evolve_background_host(ctypes.byref(cfg), 1, 1, 1, 1, 1, 123, None, 1) == -1
+    assert L.deb_tau_of_a(None, 1, 100, None, 1, None, None) == -1

@@ -121,8 +121,13 @@ def test_gradient_from_gpu_tables_matches_host_tables():
     small = dict(lmaxg=8, lmaxgp=8, lmaxr=10, lmaxnu=8, nqmax=3)
     p = fiducial_mnu_param()
     kw = dict(aexp_out=[1.0], kmin=1e-3, kmax=1.0, num_k=6, rtol=1e-5, atol=1e-5, max_steps=8000, **small)
-    Ph, Dh, _ = deb.evolve_perturbations_grad(params=p, tables="host", processes=4, **kw)
+    Ph, Dh, _ = deb.evolve_perturbations_grad(params=p, tables="python", processes=4, **kw)
     Pg, Dg, _ = deb.evolve_perturbations_grad(params=p, tables="gpu", **kw)
+    Pn, Dn, _ = deb.evolve_perturbations_grad(params=p, tables="native", **kw)
+    scale = np.abs(Dh).max(axis=(0, 1))
+    # the library's producer on the host cores: tables equal to the Python producer's to rounding
+    np.testing.assert_allclose(Pn, Ph, rtol=1e-5)
+    assert (np.abs(Dn - Dh) <= 1e-3 * scale + 1e-12).all(), (np.abs(Dn - Dh).max(axis=(0, 1)) / scale).tolist()
     np.testing.assert_allclose(Pg, Ph, rtol=1e-5)
     scale = np.abs(Dh).max(axis=(0, 1))
     assert (np.abs(Dg - Dh) <= 1e-3 * scale + 1e-12).all(), (np.abs(Dg - Dh).max(axis=(0, 1)) / scale).tolist()

@@ -72,3 +72,28 @@ def test_producer_code_on_the_host_equals_the_python_producer():
             p += n
     p += 2 * int(host[0, 19])
     np.testing.assert_array_equal(dev[:, 32 + 3 * sizes.sum():p], host[:, 32 + 3 * sizes.sum():p])
+
+
+def test_library_host_producer_equals_the_python_producer():
+    """deb_evolve_background_host (the producer's code compiled into the CUDA
+    library's host side, worker threads over the sets) against the Python
+    producer, and tau(a) read back from the blobs."""
+    from discoeb_gb300 import background as bg
+    from discoeb_gb300.workloads import fiducial_mnu_param, sample_cosmologies
+
+    ps = [fiducial_mnu_param()] + sample_cosmologies(3, seed=9)[0]
+    got, st = tables_gpu.evolve_background_tables_host(ps, 15, nthreads=3)
+    assert (st == 0).all()
+    evolved = [bg.evolve_background(param=p) for p in ps]
+    ref = np.stack([tables.pack_cosmology(e, 15) for e in evolved])
+    np.testing.assert_array_equal(got[:, 19:32], ref[:, 19:32])
+    np.testing.assert_allclose(got[:, :19], ref[:, :19], rtol=1e-13, atol=1e-300)
+    sizes = ref[0, 20:27].astype(int)
+    p = 32
+    for n in sizes:   # rounding only: values 1e-10 of each array's largest, second derivatives 1e-9
+        for part in range(3):
+            h, d = ref[:, p:p + n], got[:, p:p + n]
+            assert (np.abs(d - h) <= (1e-9 if part == 2 else 1e-10) * np.abs(h).max(axis=1, keepdims=True)).all()
+            p += n
+    tau = tables.tau_of_a_blob(got, [0.25, 1.0])
+    np.testing.assert_allclose(tau, np.stack([tables.tau_of_a(e, [0.25, 1.0]) for e in evolved]), rtol=1e-12)
