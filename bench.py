@@ -309,7 +309,8 @@ def run_ours(args):
                    if args.exec_mode != "auto" else "auto",
                    "cuda_graph": "queue reset + persistent launch + get_power captured once, replayed per step",
                    "launch_shape": launch, "autotune_ms": {f"{a}/{b}": round(v, 2) for (a, b), v in tune_ms.items()},
-                   "l2": "flushed before every timed step (256 MB write); per-mode state in shared memory",
+                   "l2": "flushed before every timed step (256 MB write); per-mode state in shared memory "
+                         "(stage vectors in L2 with the global launch shape)",
                    "aexp_out": inp["aexp"], "cosmology": inp["cosmo_kind"], "step_to_outputs": inp["step_ts"],
                    "redrawn_cosmologies": inp["rejected"]},
         "e2e": {"value": total_cosmo / t_e2e if world == 1 else None, "unit": "cosmology solves/s",
@@ -477,7 +478,7 @@ def run_gradient(args, inp, world, rank, local):
                                                     "sets": len(all_sets)}},
         "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
-                     "note": "FP64-pipe bound (state in shared memory); peak = FP64 FMA microkernel measured in this run; "
+                     "note": "FP64-pipe bound (state in shared memory / L2, DRAM idle); peak = FP64 FMA microkernel measured in this run; "
                              "achieved = algorithmic FLOPs of the structured Rodas5 step x (attempted + replayed steps)"},
         "gpu_launches": 4 * args.steps,
         "clocks": clk.summary(),

@@ -1,15 +1,19 @@
-"""Input tables produced on the GPU (``deb_evolve_background``).
+"""The library's table producer (``deb_evolve_background`` on the GPU,
+``deb_evolve_background_host`` on the host cores).
 
 The RECFAST branch of ``evolve_background`` (``src/discoeb/background.py:140-342``
-with ``thermodynamics_recfast.py:124-501``) for many parameter sets in one
-launch, written straight into the table blobs the solver reads.  The
-algorithm is the one of :mod:`background` / :mod:`recfast` on the host: the
-same sampling grids, quadrature nodes and constants are passed to the kernel
-from those modules, so host and device tables agree to rounding.
+with ``thermodynamics_recfast.py:124-501``) for many parameter sets at once,
+written straight into the table blobs the solver reads.  The algorithm is the
+one of :mod:`background` / :mod:`recfast`: the same sampling grids, quadrature
+nodes and constants are passed to the compiled code from those modules, so
+its tables agree with theirs to rounding.
 
-:func:`evolve_background_tables` is the entry point: parameter dicts in (the
-keys ``evolve_background`` reads), ``[nset, blob_len]`` device tables out,
-optionally with ``tau_of_a`` at given scale factors.
+:func:`evolve_background_tables` (GPU, one warp per set: parameter dicts in,
+``[nset, blob_len]`` device tables out, optionally ``tau_of_a`` at given scale
+factors) and :func:`evolve_background_tables_host` (the same code on worker
+threads, numpy blobs out).  One RECFAST history is a long sequential chain of
+small FP64 steps: a CPU core builds a set in ~2 ms, one GPU lane in ~130 ms,
+so the host producer is the faster one for the set counts of a gradient call.
 """
 from __future__ import annotations
 
