@@ -55,3 +55,26 @@ def test_groups_must_divide_the_modes(case):
     blob, tau, k = case
     with pytest.raises(RuntimeError):
         oracle.solve_grouped(blob, k[:7], tau, 4, **DIMS)
+
+
+def test_groups_over_several_cosmologies_and_outputs():
+    """Groups never straddle cosmologies; each group runs on its own
+    cosmology's tables and output times (two cosmologies, two outputs)."""
+    from discoeb_gb300.workloads import sample_cosmologies
+
+    ps = [bg.evolve_background(param=p) for p in sample_cosmologies(2, seed=3)[0]]
+    tabs = tb.pack_batch(ps, 3)
+    taus = np.stack([tb.tau_of_a(p, [0.5, 1.0]) for p in ps])
+    k = np.tile(np.geomspace(1e-3, 1.0, 4), 2)
+    com = np.repeat(np.arange(2, dtype=np.int32), 4)
+    yo, so = oracle.solve_grouped(tabs, k, taus, 2, cosmo_of_mode=com, rtol=1e-4, atol=1e-4, **DIMS)
+    yh, sh = H.solve_grouped(tabs, k, taus, 2, cosmo_of_mode=com, rtol=1e-4, atol=1e-4, **DIMS)
+    assert (so[:, 0] == 0).all() and (sh[:, 0] == 0).all()
+    np.testing.assert_allclose(yh[:, 1, 4] ** 2, yo[:, 1, 4] ** 2, rtol=1e-6)
+    np.testing.assert_allclose(yh[:, 0, 4] ** 2, yo[:, 0, 4] ** 2, rtol=1e-3)   # a = 0.5: in-step interpolation
+    # each group equals that group solved alone
+    for g in range(4):
+        sl = slice(2 * g, 2 * g + 2)
+        c = int(com[2 * g])
+        y1, _ = oracle.solve_grouped(tabs[c], k[sl], taus[c], 2, rtol=1e-4, atol=1e-4, **DIMS)
+        np.testing.assert_array_equal(y1, yo[sl])
