@@ -1,6 +1,6 @@
 // discoeb_oracle.cpp -- CPU oracle for the DISCO-EB perturbation hot path.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU path is
+// TEST INFRASTRUCTURE ONLY.  This file is the oracle the GPU path is
 // compared against (and the timed CPU baseline); nothing in the shipped
 // library links, loads or calls it.
 //
