@@ -97,3 +97,23 @@ def test_library_host_producer_equals_the_python_producer():
             p += n
     tau = tables.tau_of_a_blob(got, [0.25, 1.0])
     np.testing.assert_allclose(tau, np.stack([tables.tau_of_a(e, [0.25, 1.0]) for e in evolved]), rtol=1e-12)
+
+
+import pytest  # noqa: E402
+
+
+@pytest.mark.parametrize("nqmax", [3, 4, 5, 8, 15])
+def test_library_host_producer_momentum_bins(nqmax):
+    """The blob's momentum nodes for CAMB's 3/4/5-bin tables and for
+    generalised Gauss-Laguerre, as the Python producer packs them."""
+    from discoeb_gb300 import background as bg
+    from discoeb_gb300.workloads import fiducial_mnu_param
+
+    p = fiducial_mnu_param()
+    got, st = tables_gpu.evolve_background_tables_host([p], nqmax, nthreads=1)
+    ref = tables.pack_cosmology(bg.evolve_background(param=p), nqmax)
+    assert st[0] == 0 and got.shape == (1, ref.shape[0])
+    sizes = ref[20:27].astype(int)
+    p0 = 32 + 3 * int(sizes.sum())
+    np.testing.assert_array_equal(got[0, p0:p0 + 2 * nqmax], ref[p0:p0 + 2 * nqmax])
+    np.testing.assert_array_equal(got[0, 19:32], ref[19:32])
