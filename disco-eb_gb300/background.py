@@ -166,18 +166,28 @@ def setup_background_evolution(*, amin: float, amax: float, param: dict) -> dict
     return param
 
 
-def evolve_background(*, param: dict, thermo_module: str = "RECFAST", num_thermo: int = 256, **_unused) -> dict:
+def evolve_background(*, param: dict, thermo_module: str = "RECFAST", num_thermo: int = 256,
+                      producer: str = "python", **_unused) -> dict:
     """Background + RECFAST thermal history, filling the splines the path reads.
 
     Mirrors ``evolve_background`` (``background.py:191-305``) for
     ``thermo_module='RECFAST'``.  Produces ``tau_of_a``, ``a_of_tau``,
     ``xe_of_tau``, ``xe_of_loga`` and ``cs2a_of_loga`` splines plus the
     scalars written by :func:`setup_background_evolution`.
+    ``producer="native"`` builds the same tables with the library's compiled
+    producer (~100x faster; the dict then carries what the perturbation path
+    reads, see ``tables_gpu.param_from_blob``).
     """
     from .recfast import evaluate_thermo
 
     if thermo_module != "RECFAST":
         raise NotImplementedError("only thermo_module='RECFAST' is produced on the host")
+    if producer == "native":
+        from .tables_gpu import evolve_backgrounds_native
+
+        return evolve_backgrounds_native([param], num_thermo=num_thermo)[0]
+    if producer != "python":
+        raise ValueError(f"producer must be 'python' or 'native', not {producer!r}")
     param = dict(param)
     param.setdefault("Omegak", 0.0)
     amin, amax = 1e-9, 1.01

@@ -54,8 +54,14 @@ def _evolve(param):
     return _bg.evolve_background(param=param)
 
 
-def evolve_backgrounds(params, processes=None):
-    """Host table production for many parameter dicts (process pool, spawn)."""
+def evolve_backgrounds(params, processes=None, producer: str = "python"):
+    """Host table production for many parameter dicts: the Python producer in
+    a process pool (spawn), or the library's compiled producer on worker
+    threads (``producer="native"``, a few ms per set)."""
+    if producer == "native":
+        from .tables_gpu import evolve_backgrounds_native
+
+        return evolve_backgrounds_native(list(params))
     processes = processes if processes is not None else min(len(params), os.cpu_count() or 1)
     if processes <= 1 or len(params) <= 1:
         return [_evolve(p) for p in params]

@@ -149,3 +149,46 @@ def evolve_background_tables_host(params, nqmax: int, *, num_thermo: int = 256, 
     _native.check(L.deb_evolve_background_host(ctypes.byref(cfg), p(pm), nset, p(consts), p(grd), p(tabs), bl,
                                                p(status), int(nthreads)), "deb_evolve_background_host")
     return tabs, status
+
+
+def param_from_blob(inputs: dict, blob: np.ndarray) -> dict:
+    """A ``param`` dict as ``evolve_background`` returns it, read back from a
+    produced blob: the input keys, the scalars the perturbation path reads,
+    ``adotrad``, the seven splines (fields ``_x_``, ``_y_``, ``_S_full_``; the
+    second derivatives are the producer's) and the ``a``, ``aexp``, ``tau``,
+    ``xe``, ``cs2`` arrays.  The ionisation fractions by species, T_m, mu,
+    ``taumax`` and the splines the path does not read are not in a blob and
+    are not set."""
+    from .spline import SplineInterpolation
+
+    b = np.asarray(blob, dtype=np.float64)
+    out = dict(inputs)
+    out.setdefault("Omegak", 0.0)
+    for i, key in enumerate(_tables.SCALAR_KEYS):
+        out[key] = float(b[i])
+    out["adotrad"] = math.sqrt((out["grhog"] + out["grhor"] * (out["Neff"] + out["Nmnu"])) / 3.0)
+    sizes = b[_tables.H_NSPL0:_tables.H_NSPL0 + 7].astype(int)
+    p = _tables.HDR_LEN
+    for key, n in zip(_tables.SPLINE_KEYS, sizes):
+        sp = SplineInterpolation.__new__(SplineInterpolation)
+        sp._x_, sp._y_, sp._S_full_ = b[p:p + n].copy(), b[p + n:p + 2 * n].copy(), b[p + 2 * n:p + 3 * n].copy()
+        sp._n_ = int(n)
+        out[key] = sp
+        p += 3 * n
+    out["aexp"] = out["tau_of_a_spline"]._x_.copy()
+    out["tau"] = out["tau_of_a_spline"]._y_.copy()
+    out["xe"] = out["xe_of_tau_spline"]._y_.copy()
+    out["cs2"] = out["cs2a_of_loga_spline"]._y_ / out["aexp"]
+    out["a"] = np.exp(out["logrhonu_of_loga_spline"]._x_)
+    out["amin"], out["amax"] = AMIN, AMAX
+    return out
+
+
+def evolve_backgrounds_native(params, *, num_thermo: int = 256, nthreads: int = 0):
+    """``evolve_background`` of many parameter dicts by the library's
+    producer on the host cores (a few milliseconds per set); returns the
+    ``param`` dicts of :func:`param_from_blob`."""
+    blobs, status = evolve_background_tables_host(params, 3, num_thermo=num_thermo, nthreads=nthreads)
+    if (status != 0).any():
+        raise RuntimeError(f"{int((status != 0).sum())} parameter set(s): an ionisation interval ran out of steps")
+    return [param_from_blob(p, b) for p, b in zip(params, blobs)]

@@ -117,3 +117,24 @@ def test_library_host_producer_momentum_bins(nqmax):
     p0 = 32 + 3 * int(sizes.sum())
     np.testing.assert_array_equal(got[0, p0:p0 + 2 * nqmax], ref[p0:p0 + 2 * nqmax])
     np.testing.assert_array_equal(got[0, 19:32], ref[19:32])
+
+
+def test_native_evolve_background_gives_the_path_the_same_inputs():
+    """evolve_background(producer="native") returns a param dict that packs
+    to the same blob (to rounding) and has the same output times as the
+    Python producer's."""
+    from discoeb_gb300 import background as bg
+    from discoeb_gb300.workloads import reference_test_param
+
+    p = reference_test_param()
+    fast = bg.evolve_background(param=p, producer="native")
+    slow = bg.evolve_background(param=p)
+    bf, bs = tables.pack_cosmology(fast, 5), tables.pack_cosmology(slow, 5)
+    np.testing.assert_array_equal(bf[19:32], bs[19:32])
+    scale = np.abs(bs).max()
+    assert np.abs(bf - bs).max() <= 1e-9 * scale
+    np.testing.assert_allclose(tables.tau_of_a(fast, [0.1, 1.0]), tables.tau_of_a(slow, [0.1, 1.0]), rtol=1e-12)
+    for key in ("OmegaDE", "taumin", "amnu", "adotrad", "grhom"):
+        np.testing.assert_allclose(fast[key], slow[key], rtol=1e-13)
+    np.testing.assert_allclose(fast["xe"], slow["xe"], rtol=1e-9)
+    np.testing.assert_allclose(fast["cs2"], slow["cs2"], rtol=1e-8)
