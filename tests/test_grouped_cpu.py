@@ -78,3 +78,13 @@ def test_groups_over_several_cosmologies_and_outputs():
         c = int(com[2 * g])
         y1, _ = oracle.solve_grouped(tabs[c], k[sl], taus[c], 2, rtol=1e-4, atol=1e-4, **DIMS)
         np.testing.assert_array_equal(y1, yo[sl])
+
+
+def test_group_failure_statuses(case):
+    """A step budget that runs out stops the whole group with MAX_STEPS (1);
+    the kernel's group driver and the oracle agree on it."""
+    blob, tau, k = case
+    yo, so = oracle.solve_grouped(blob, k, tau, 4, rtol=1e-4, atol=1e-4, max_steps=5, **DIMS)
+    yh, sh = H.solve_grouped(blob, k, tau, 4, rtol=1e-4, atol=1e-4, max_steps=5, **DIMS)
+    assert (so[:, 0] == 1).all() and (sh[:, 0] == 1).all()
+    assert (sh[:, 1] + sh[:, 2] == 5).all()
