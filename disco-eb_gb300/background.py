@@ -167,7 +167,7 @@ def setup_background_evolution(*, amin: float, amax: float, param: dict) -> dict
 
 
 def evolve_background(*, param: dict, thermo_module: str = "RECFAST", num_thermo: int = 256,
-                      producer: str = "python", **_unused) -> dict:
+                      producer: str = "python", recfast_stage_times: bool = False, **_unused) -> dict:
     """Background + RECFAST thermal history, filling the splines the path reads.
 
     Mirrors ``evolve_background`` (``background.py:191-305``) for
@@ -177,6 +177,10 @@ def evolve_background(*, param: dict, thermo_module: str = "RECFAST", num_thermo
     ``producer="native"`` builds the same tables with the library's compiled
     producer (~100x faster; the dict then carries what the perturbation path
     reads, see ``tables_gpu.param_from_blob``).
+    ``recfast_stage_times=True`` (Python producer only) integrates the
+    ionisation history with GRK4A's stages at their own times instead of the
+    reference's all-stages-at-t0 step (``ode_integrators_stiff.py:192-200``):
+    the accurate solution of the same equations, not the reference's tables.
     """
     from .recfast import evaluate_thermo
 
@@ -188,11 +192,14 @@ def evolve_background(*, param: dict, thermo_module: str = "RECFAST", num_thermo
         return evolve_backgrounds_native([param], num_thermo=num_thermo)[0]
     if producer != "python":
         raise ValueError(f"producer must be 'python' or 'native', not {producer!r}")
+    if recfast_stage_times and producer != "python":
+        raise ValueError("recfast_stage_times needs producer='python'")
     param = dict(param)
     param.setdefault("Omegak", 0.0)
     amin, amax = 1e-9, 1.01
     param = setup_background_evolution(amin=amin, amax=amax, param=param)
-    tau, aexp, cs2, Tm, mu, xe, xeHI, xeHeI, xeHeII = evaluate_thermo(param=param, num_thermo=num_thermo)
+    tau, aexp, cs2, Tm, mu, xe, xeHI, xeHeI, xeHeII = evaluate_thermo(param=param, num_thermo=num_thermo,
+                                                                     stage_times=recfast_stage_times)
     param["aexp"] = aexp
     param["tau"] = tau
     param["xe"] = xe

@@ -15,10 +15,13 @@
 
 #include <cuda_runtime.h>
 
+#include <cuda.h>
+
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <cmath>
+#include <mutex>
 
 #include "deb_core.cuh"
 #include "discoeb_gb300.h"
@@ -286,21 +289,79 @@ __global__ void fp64_peak_kernel(double* out, int iters, double a, double b) {
   if (s == 12345.678) out[0] = s;  // keeps the chains live
 }
 
-bool g_consts_ready[64] = {false};
+// Per-device state that lives in a CUDA context (constant tables, kernel
+// attributes) is remembered together with the id of the context it was set
+// in: after cudaDeviceReset (or with another context current) the id
+// differs and the state is set again.  Guarded by g_state_mu.
+std::mutex g_state_mu;
+unsigned long long g_consts_ctx[64] = {0};
+unsigned long long g_attr_ctx[64] = {0};
 // largest dynamic shared memory size set on forward_warp_kernel, per device
 long g_warp_smem_attr[64] = {0};
+
+using PFN_ctxGetCurrent = CUresult (*)(CUcontext*);
+using PFN_ctxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique id of the current thread's CUDA context (never reused within a
+// process), 0 if it cannot be determined.  The driver entry points are found
+// through the runtime, so the library needs no link to libcuda.
+unsigned long long current_ctx_id() {
+  static PFN_ctxGetCurrent get_cur = nullptr;
+  static PFN_ctxGetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_cur = (PFN_ctxGetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (PFN_ctxGetId)f;
+  });
+  if (!get_cur || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  if (get_cur(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  unsigned long long id = 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id + 1;   // 0 stays "unknown"
+}
 
 int upload_constants() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return DEB_ERR_CUDA;
-  if (dev >= 0 && dev < 64 && g_consts_ready[dev]) return DEB_OK;
+  unsigned long long ctx = current_ctx_id();
+  if (ctx == 0) {
+    // no context current on this thread yet: let the runtime make the
+    // device's primary context current, then ask again
+    if (cudaFree(nullptr) != cudaSuccess) return DEB_ERR_CUDA;
+    ctx = current_ctx_id();
+  }
+  std::lock_guard<std::mutex> lock(g_state_mu);
+  if (dev >= 0 && dev < 64 && ctx != 0 && g_consts_ctx[dev] == ctx) return DEB_OK;
   deb::Tab T;
   deb::Rodas R;
   deb::fill_tables(T);
   deb::fill_rodas(R);
   if (cudaMemcpyToSymbol(c_tab, &T, sizeof(T)) != cudaSuccess) return DEB_ERR_CUDA;
   if (cudaMemcpyToSymbol(c_rodas, &R, sizeof(R)) != cudaSuccess) return DEB_ERR_CUDA;
-  if (dev >= 0 && dev < 64) g_consts_ready[dev] = true;
+  if (dev >= 0 && dev < 64) g_consts_ctx[dev] = ctx;
+  return DEB_OK;
+}
+
+// Raise forward_warp_kernel's dynamic shared memory limit to at least
+// `bytes` in the current context (only ever raised, so that plans made
+// earlier with a larger slot stay launchable).
+int ensure_warp_smem(int dev, long bytes) {
+  const unsigned long long ctx = current_ctx_id();
+  std::lock_guard<std::mutex> lock(g_state_mu);
+  const bool known = dev >= 0 && dev < 64 && ctx != 0 && g_attr_ctx[dev] == ctx;
+  if (known && g_warp_smem_attr[dev] >= bytes) return DEB_OK;
+  const long want = known && g_warp_smem_attr[dev] > bytes ? g_warp_smem_attr[dev] : bytes;
+  if (cudaFuncSetAttribute(forward_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want) != cudaSuccess)
+    return DEB_ERR_CUDA;
+  if (dev >= 0 && dev < 64) { g_attr_ctx[dev] = ctx; g_warp_smem_attr[dev] = want; }
   return DEB_OK;
 }
 
@@ -440,14 +501,10 @@ int deb_plan_create_ex(const deb_dims* dims, int max_modes, const deb_launch_cfg
     p->warp_blocks = (int)nw;
     nslots = nw;
     p->warp_smem_bytes = smem_bytes;
-    // the attribute belongs to the kernel, not to the plan: only ever raise
-    // it, so that plans made earlier with a larger slot stay launchable
-    if (p->warp_smem && (dev < 0 || dev >= 64 || g_warp_smem_attr[dev] < smem_bytes)) {
-      if (cudaFuncSetAttribute(forward_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes) != cudaSuccess) {
-        delete p;
-        return DEB_ERR_CUDA;
-      }
-      if (dev >= 0 && dev < 64) g_warp_smem_attr[dev] = smem_bytes;
+    // the attribute belongs to the kernel, not to the plan
+    if (p->warp_smem && ensure_warp_smem(dev, smem_bytes) != DEB_OK) {
+      delete p;
+      return DEB_ERR_CUDA;
     }
   }
   const bool need_ws = mode == DEB_EXEC_LANE || !p->warp_smem;
@@ -687,7 +744,6 @@ int deb_get_power(const double* d_tables, int ncosmo, int blob_len, const double
 // Scratch of deb_forward_static: bytes [0, 256) hold the work-queue counter,
 // the rest holds one warp-mode slot per mode in flight.
 static __device__ __align__(256) double g_static_scratch[DEB_STATIC_SCRATCH_BYTES / sizeof(double)];
-static double* g_static_scratch_addr[64] = {nullptr};
 
 int deb_forward_static(const deb_dims* dims, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
                        const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
@@ -710,13 +766,12 @@ int deb_forward_static(const deb_dims* dims, const double* d_tables, int ncosmo,
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DEB_ERR_CUDA;
   int rc = upload_constants();
   if (rc) return rc;
-  if (!g_static_scratch_addr[dev]) {
-    void* ptr = nullptr;
-    if (cudaGetSymbolAddress(&ptr, g_static_scratch) != cudaSuccess || !ptr) return DEB_ERR_CUDA;
-    g_static_scratch_addr[dev] = (double*)ptr;
-  }
+  // the array's device address in the current context, looked up on every
+  // call (cheap): a cached pointer would outlive a cudaDeviceReset
+  void* ptr = nullptr;
+  if (cudaGetSymbolAddress(&ptr, g_static_scratch) != cudaSuccess || !ptr) return DEB_ERR_CUDA;
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return DEB_ERR_CUDA;
-  double* base = g_static_scratch_addr[dev];
+  double* base = (double*)ptr;
   cudaStream_t s = (cudaStream_t)stream;
   KParams P{};
   P.tables = d_tables; P.ncosmo = ncosmo; P.blob_len = blob_len; P.k = d_k; P.cosmo = d_cosmo_of_mode;

@@ -244,12 +244,47 @@ def _grk4a_step(t0, dt, y0, P, aH):
     return y1, err
 
 
-def solve_ionization(astart, aend, ystart, P, aH_of, rtol=1e-3, atol=1e-6, max_steps=128):
+# Stage abscissae and summed gammas of GRK4A for the non-autonomous form
+# (Kaps & Rentrop 1979; Hairer & Wanner, Solving ODEs II, IV.7):
+# alpha_i = sum_j alpha_ij, gamma_i = gamma + sum_j gamma_ij.
+_ALPHA2, _ALPHA3 = _A21, _A31 + _A32
+_GAM1 = _G
+_GAM2 = _G + _G21
+_GAM3 = _G + _G31 + _G32
+_GAM4 = _G + _G41 + _G42 + _G43
+
+
+def _grk4a_step_timed(t0, dt, y0, P, aH_of):
+    """One GRK4A step of the non-autonomous problem: stage i at
+    t0 + alpha_i dt, plus the gamma_i dt^2 df/dt terms (df/dt by a central
+    difference in a).  Not the reference's step (which keeps every stage at
+    t0); used to measure what that choice costs."""
+    f = lambda t, y: np.array(ionization_rhs(t, list(y), P, aH_of(t)), dtype=np.float64) * dt
+    J = _jac3(t0, list(y0), P, aH_of(t0)) * dt
+    ht = 1e-7 * t0
+    ft = (f(t0 + ht, y0) - f(t0 - ht, y0)) * (dt / (2.0 * ht))
+    Ainv = np.linalg.inv(np.eye(3) - _G * J)
+    k1 = Ainv @ (f(t0, y0) + _GAM1 * ft)
+    Jk1 = J @ k1
+    k2 = Ainv @ (f(t0 + _ALPHA2 * dt, y0 + _A21 * k1) + _G21 * Jk1 + _GAM2 * ft)
+    Jk2 = J @ k2
+    f2 = f(t0 + _ALPHA3 * dt, y0 + _A31 * k1 + _A32 * k2)
+    k3 = Ainv @ (f2 + _G31 * Jk1 + _G32 * Jk2 + _GAM3 * ft)
+    Jk3 = J @ k3
+    k4 = Ainv @ (f2 + _G41 * Jk1 + _G42 * Jk2 + _G43 * Jk3 + _GAM4 * ft)
+    y1 = y0 + _C1 * k1 + _C2 * k2 + _C3 * k3 + _C4 * k4
+    err = (_C1 - _CH1) * k1 + (_C2 - _CH2) * k2 + (_C3 - _CH3) * k3 + _C4 * k4
+    return y1, err
+
+
+def solve_ionization(astart, aend, ystart, P, aH_of, rtol=1e-3, atol=1e-6, max_steps=128, stage_times=False):
     """Adaptive GRK4A from astart to aend (``thermodynamics_recfast.py:283-300``).
 
     I-controller of diffrax defaults (safety 0.9, factor in [0.2, 10],
     error order 3 as GRKT4 declares), RMS norm over the three components.
     Returns (x_H, x_He, T_m, dx_H/da, dx_He/da, dT_m/da) at aend.
+    ``stage_times=True`` integrates the non-autonomous problem properly
+    (:func:`_grk4a_step_timed`) instead of the reference's step.
     """
     t0 = astart
     t1 = min(astart + abs(astart) * 1e-3, aend)
@@ -257,8 +292,10 @@ def solve_ionization(astart, aend, ystart, P, aH_of, rtol=1e-3, atol=1e-6, max_s
     steps = 0
     while t0 < aend and steps < max_steps:
         dt = t1 - t0
-        aH = aH_of(t0)
-        y1, err = _grk4a_step(t0, dt, y, P, aH)
+        if stage_times:
+            y1, err = _grk4a_step_timed(t0, dt, y, P, aH_of)
+        else:
+            y1, err = _grk4a_step(t0, dt, y, P, aH_of(t0))
         y1c = y if np.isnan(y1).any() else y1
         sc = err / (atol + rtol * np.maximum(np.abs(y), np.abs(y1c)))
         e = math.sqrt(float(np.mean(sc * sc)))
@@ -311,7 +348,7 @@ def adaptive_sampling(a0: float, a1: float, N: int) -> np.ndarray:
     ])
 
 
-def compute_thermal_history(*, a0, a1, N, param, rtol=1e-3, atol=1e-6):
+def compute_thermal_history(*, a0, a1, N, param, rtol=1e-3, atol=1e-6, stage_times=False):
     """Ionisation history sampled on N adaptive points (``thermodynamics_recfast.py:362-452``)."""
     a = adaptive_sampling(a0, a1, N + 1)
     H = param["H0"] / 100.0
@@ -339,19 +376,20 @@ def compute_thermal_history(*, a0, a1, N, param, rtol=1e-3, atol=1e-6):
         elif i > 0 and y_prev[0] > 0.99:
             rhs = math.exp(1.5 * math.log(CR * Tcmb / (1.0 + zend)) - CB1 / (Tcmb * (1.0 + zend))) / Nnow
             xH0 = 0.5 * (math.sqrt(rhs**2 + 4.0 * rhs) - rhs)
-            new = solve_ionization(astart, aend, y_prev, param, aH_of, rtol, atol)
+            new = solve_ionization(astart, aend, y_prev, param, aH_of, rtol, atol, stage_times=stage_times)
             new[0] = xH0
             new[3] = 0.0
         else:
-            new = solve_ionization(astart, aend, y_prev, param, aH_of, rtol, atol)
+            new = solve_ionization(astart, aend, y_prev, param, aH_of, rtol, atol, stage_times=stage_times)
         out[:, i] = new
     return out, a[1:]
 
 
-def evaluate_thermo(*, param: dict, num_thermo: int = 256):
+def evaluate_thermo(*, param: dict, num_thermo: int = 256, stage_times: bool = False):
     """x_e, T_m, c_s^2 and tau on the sampled scale factors (``thermodynamics_recfast.py:455-501``)."""
     param["fHe"] = param["YHe"] / (MHE_MH * (1.0 - param["YHe"]))
-    y, a = compute_thermal_history(a0=param["amin"], a1=param["amax"], N=num_thermo, param=param)
+    y, a = compute_thermal_history(a0=param["amin"], a1=param["amax"], N=num_thermo, param=param,
+                                   stage_times=stage_times)
     xeHI = y[0]
     xeHeI = y[1]
     xeHeII = np.array([saha_heii(ai, param) for ai in a])

@@ -268,9 +268,10 @@ int deb_fftlog_phase(int nfreq, double log_kmax_over_kmin, int ell, double* d_ph
  *     nvar 80); any nmode is processed through the work queue;
  *   - returns DEB_ERR_STATIC_SCRATCH when one mode's state does not fit the
  *     array;
- *   - the first call on a device (with that device current) looks up the
- *     array's device address with cudaGetSymbolAddress and uploads the
- *     constant tables; make that first call before any stream capture;
+ *   - every call looks up the array's device address in the current context
+ *     (cudaGetSymbolAddress); the first call in a context also uploads the
+ *     constant tables (a synchronous copy): make that first call before any
+ *     stream capture;
  *   - every call reuses the same array and resets the counter it needs, so
  *     calls that overlap on the GPU (e.g. on two streams) race: serialise them.
  */
