@@ -1402,7 +1402,32 @@ struct Run {
   int rec_cap, nrec;
   double scale;   // replay: tau_start / nominal tau_start
   int t1_out;     // index of the output time the current step is clipped to, or -1
+  // record with checkpoints (the adjoint's forward states): ck[slot n + j]
+  // holds y after accepted step slot * ck_stride; when the ck_cap slots are
+  // full, every other one is dropped and the stride doubles, so a run keeps
+  // between ck_cap / 2 and ck_cap evenly spaced states.  ck = null: none.
+  double* ck = nullptr;
+  int ck_cap = 0, ck_stride = 1;
 };
+
+// Store the state of vector vec as the checkpoint after accepted step j
+// (j = 0: the initial state), thinning as described at Run::ck.
+template <int G>
+HD void checkpoint_store(const Grp<G>& gp, const WS<G>& w, int n, Run& r, int vec, int j) {
+  if (!r.ck || j % r.ck_stride) return;
+  int slot = j / r.ck_stride;
+  if (slot >= r.ck_cap) {
+    const int half = r.ck_cap / 2;
+    for (int i = 1; i < half; ++i)
+      for (int e = gp.lane; e < n; e += G) r.ck[(long)i * n + e] = r.ck[(long)(2 * i) * n + e];
+    gp.sync();
+    r.ck_stride *= 2;
+    if (j % r.ck_stride) return;
+    slot = j / r.ck_stride;
+  }
+  for (int e = gp.lane; e < n; e += G) r.ck[(long)slot * n + e] = w.v(vec, e);
+  gp.sync();
+}
 
 // replay: end time of recorded step j (1-based) for this table set
 HD double replay_time(const Run& r, const double* tau_out, int j) {
@@ -1451,6 +1476,7 @@ HD void mode_begin(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const D
   }
   r.lprev = 0.0; r.lprev_prev = 0.0;
   r.vy = V_Y; r.vu = V_U; r.steps = 0; r.acc = 0; r.rej = 0; r.status = ST_OK;
+  if (ctl.record && r.ck) { r.ck_stride = 1; checkpoint_store<G>(gp, w, D.n, r, V_Y, 0); }
 }
 
 // Stage S >= 1 before its RHS: u = y0 + sum_q a_Sq k_q (S <= 5) or
@@ -1488,13 +1514,15 @@ HD void stage_prep(const Grp<G>& gp, const Rodas& R, const WS<G>& w, int n, int 
 // PID norm (perturbations.py:701-705, 759-760); bad = y1 not finite.
 template <int G>
 HD double step_attempt(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dims& D, const Tab& T,
-                       const Rodas& R, const Ctl& ctl, const WS<G>& w, const Run& r, bool& bad_out) {
+                       const Rodas& R, const Ctl& ctl, const WS<G>& w, const Run& r, bool& bad_out,
+                       Bg<double>* g0 = nullptr) {
   const int n = D.n, nq = D.nq, iq0 = D.iq0, igp = D.igp, ir = D.ir, lg = D.lg, lgp = D.lgp, lr = D.lr, lnu = D.lnu;
   const double t0 = r.t0, dt = r.t1 - r.t0;
   const int vy = r.vy, vu = r.vu;
   // f(t0, y0) into k1 and d f / d a in one forward-mode pass
   Bg<double> g;
   rhs<Dual, G>(gp, c, m, D, T, t0, w, vy, V_K0, V_JC0, &g);
+  if (g0) *g0 = g;
   const double d = rcp(dt * R.gamma);
   factor_W<G>(gp, c, m, D, T, w, d, t0, g);
   if (ctl.dense) dense_factor<G>(gp, m, D, T, w, d, t0, g);
@@ -1607,6 +1635,7 @@ HD bool step_decide(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const 
     r.lprev_prev = r.lprev;
     r.lprev = linv_kept;
     if (ctl.record && gp.lead() && r.acc < r.rec_cap) r.rec[r.acc] = r.t1_out >= 0 ? -(r.t1_out + 1.0) : r.t1;
+    if (ctl.record && r.ck) checkpoint_store<G>(gp, w, n, r, r.vy, r.acc);
     if (ctl.replay) {
       // next recorded end time; the run ends at this table set's own final
       // output time (the recorded one is the nominal cosmology's)

@@ -8,6 +8,8 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _SRC = os.path.join(_HERE, "core_harness.cpp")
 _TSRC = os.path.join(_HERE, "tables_harness.cpp")
+_ASRC = os.path.join(_HERE, "adjoint_harness.cpp")
+_ACORE = os.path.join(_HERE, "..", "..", "disco-eb_gb300", "csrc", "deb_adjoint.cuh")
 _TCORE = os.path.join(_HERE, "..", "..", "disco-eb_gb300", "csrc", "deb_tables_core.cuh")
 _INC = os.path.join(_HERE, "..", "..", "include")
 _CORE = os.path.join(_HERE, "..", "..", "disco-eb_gb300", "csrc", "deb_core.cuh")
@@ -21,9 +23,10 @@ def lib():
     global _lib
     if _lib is None:
         os.makedirs(os.path.dirname(_LIB), exist_ok=True)
-        deps = (_SRC, _CORE, _TSRC, _TCORE)
+        deps = (_SRC, _CORE, _TSRC, _TCORE, _ASRC, _ACORE)
         if not os.path.exists(_LIB) or os.path.getmtime(_LIB) < max(os.path.getmtime(d) for d in deps):
-            subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", _INC, "-o", _LIB, _SRC, _TSRC])
+            subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", _INC, "-o", _LIB, _SRC, _TSRC,
+                                   _ASRC])
         L = ctypes.CDLL(_LIB)
         L.h_rhs.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, ctypes.c_double, dp, dp, dp]
         L.h_solve_W.argtypes = [dp, ctypes.c_int, ip, ctypes.c_double, ctypes.c_double, dp, ctypes.c_double, dp, dp, ctypes.c_int]
@@ -36,6 +39,14 @@ def lib():
         ci, cd = ctypes.c_int, ctypes.c_double
         L.h_solve_grouped.argtypes = [dp, ci, ci, dp, ip, ci, dp, ci, ip, dp, ci, ci, dp, ip]
         L.h_tables.argtypes = [dp, ci, dp, dp, ci, ci, ci, ci, ci, cd, cd, cd, dp, ci, ip]
+        L.h_adj_phi.argtypes = [dp, ci, ip, cd, cd, dp, dp, dp]
+        L.h_adj_jt.argtypes = [dp, ci, ip, cd, cd, dp, dp, dp, ci]
+        L.h_adj_solve_wt.argtypes = [dp, ci, ip, cd, cd, dp, cd, dp, dp]
+        L.h_adj_outputs.argtypes = [dp, ci, ip, cd, cd, dp, dp, dp]
+        L.h_adjoint.argtypes = [dp, ci, ci, cd, dp, ci, ip, dp, ci, ci, dp, dp, dp, dp, ip, dp]
+        L.h_adj_solve_m.argtypes = [dp, ci, ip, cd, cd, dp, cd, dp, dp, ci]
+        L.h_adj_outputs_pair.argtypes = [dp, ci, ip, cd, dp, dp, dp]
+        L.h_step_adj.argtypes = [dp, ci, ci, ip, cd, cd, cd, dp, dp, dp, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -152,3 +163,102 @@ def solve_grouped(tables, kmodes, tau_out, batch_size, *, cosmo_of_mode=None, lm
                                int(max_steps), int(batch_size), _p(y), _p(st, ctypes.c_int))
     assert rc == 0, rc
     return y, st
+
+
+# ---------------------------------------------------------------- adjoint pieces (deb_adjoint.cuh on the host)
+def adj_phi(blob, dims, k, tau, x, y):
+    """[phi(B(x, y)), x^T f, d phi/da, x^T df/da, d phi/dtau]"""
+    out = np.zeros(5)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    rc = lib().h_adj_phi(_p(blob), blob.shape[0], _p(_d(dims), ctypes.c_int), k, tau, _p(x), _p(y), _p(out))
+    assert rc == 0, rc
+    return out
+
+
+def adj_jt(blob, dims, k, tau, x, y, der=False):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    z = np.zeros_like(y)
+    rc = lib().h_adj_jt(_p(blob), blob.shape[0], _p(_d(dims), ctypes.c_int), k, tau, _p(x), _p(y), _p(z), int(der))
+    assert rc == 0, rc
+    return z
+
+
+def adj_solve_wt(blob, dims, k, tau, y, dt, b):
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    z = np.zeros_like(b)
+    rc = lib().h_adj_solve_wt(_p(blob), blob.shape[0], _p(_d(dims), ctypes.c_int), k, tau, _p(y), dt, _p(b), _p(z))
+    assert rc == 0, rc
+    return z
+
+
+def adj_outputs(blob, dims, k, a, s):
+    s = np.ascontiguousarray(s, dtype=np.float64)
+    r, dr = np.zeros(20), np.zeros(20)
+    rc = lib().h_adj_outputs(_p(blob), blob.shape[0], _p(_d(dims), ctypes.c_int), k, a, _p(s), _p(r), _p(dr))
+    assert rc == 0, rc
+    return r, dr
+
+
+def adjoint(tables, eps, k, tau_out, dims, gy, rtol=1e-5, atol=1e-5, max_steps=20000, ck_cap=32, step_to_outputs=False,
+            pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, debug=False):
+    """One mode: record (with checkpoints) on tables[0], then the adjoint of
+    the cotangent gy [nout, 20]; tables [1 + 2 npar, L] (nominal, then +eps,
+    -eps per parameter), tau_out [1 + 2 npar, nout].  Returns (gtheta [npar],
+    y_out [nout, 20], (status, nrec, ck_stride), adjoint status)."""
+    tables = np.ascontiguousarray(tables, dtype=np.float64)
+    tau_out = np.ascontiguousarray(tau_out, dtype=np.float64)
+    npar = (tables.shape[0] - 1) // 2
+    nout = tau_out.shape[1]
+    cfg = np.array([rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, 5.0, 0.9, 0.0,
+                    1.0 if step_to_outputs else 0.0])
+    gth = np.zeros(npar)
+    y = np.zeros((nout, 20))
+    info = np.zeros(3, dtype=np.int32)
+    eps = np.ascontiguousarray(eps, dtype=np.float64)
+    gy = np.ascontiguousarray(gy, dtype=np.float64)
+    n = 7 + (dims[0] + 1) + (dims[1] + 1) + (dims[2] + 1) + dims[4] * (dims[3] + 1) + 2
+    dbg = np.zeros(n + 1 + nout + max_steps + 1) if debug else None
+    rc = lib().h_adjoint(_p(tables), npar, tables.shape[1], k, _p(tau_out), nout, _p(_d(dims), ctypes.c_int), _p(cfg),
+                         max_steps, ck_cap, _p(eps), _p(gy), _p(gth), _p(y), _p(info, ctypes.c_int),
+                         None if dbg is None else _p(dbg))
+    if debug:
+        return gth, y, tuple(int(v) for v in info), rc, dict(lam0=dbg[:n], dts=dbg[n], dto=dbg[n + 1:n + 1 + nout],
+                                                             rec=dbg[n + 1 + nout:n + 2 + nout + int(info[1])])
+    return gth, y, tuple(int(v) for v in info), rc
+
+
+def step_adj(tables, eps, dims, k, t0, dt, y0, lam=None):
+    """One step on tables[0]: y1; with lam also (ybar0, [tbar0, dtbar], thbar)."""
+    tables = np.ascontiguousarray(tables, dtype=np.float64)
+    npar = (tables.shape[0] - 1) // 2
+    y0 = np.ascontiguousarray(y0, dtype=np.float64)
+    y1 = np.zeros_like(y0)
+    yb, tb, th = np.zeros_like(y0), np.zeros(2), np.zeros(max(npar, 1))
+    eps = np.ascontiguousarray(eps, dtype=np.float64)
+    lp = None if lam is None else np.ascontiguousarray(lam, dtype=np.float64)
+    rc = lib().h_step_adj(_p(tables), npar, tables.shape[1], _p(_d(dims), ctypes.c_int), k, t0, dt, _p(y0), _p(eps),
+                          None if lp is None else _p(lp), _p(y1), _p(yb), _p(tb), _p(th))
+    assert rc == 0, rc
+    return y1 if lam is None else (y1, yb, tb, th[:npar])
+
+
+def adj_solve_m(blob, dims, k, tau, y, dt, b, trans):
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    z = np.zeros_like(b)
+    rc = lib().h_adj_solve_m(_p(blob), blob.shape[0], _p(_d(dims), ctypes.c_int), k, tau, _p(y), dt, _p(b), _p(z),
+                             int(trans))
+    assert rc == 0, rc
+    return z
+
+
+def adj_outputs_pair(blob, dims, k, y):
+    """(fields as the forward kernel converts y, fields as the adjoint does)"""
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    rk, rs = np.zeros(20), np.zeros(20)
+    rc = lib().h_adj_outputs_pair(_p(blob), blob.shape[0], _p(_d(dims), ctypes.c_int), k, _p(y), _p(rk), _p(rs))
+    assert rc == 0, rc
+    return rk, rs
