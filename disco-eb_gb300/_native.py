@@ -42,7 +42,8 @@ EXPORTS = ("deb_nvar", "deb_plan_create", "deb_plan_create_ex", "deb_plan_launch
            "deb_plan_set_order", "deb_forward", "deb_forward_static", "deb_tables_blob_len", "deb_evolve_background",
            "deb_evolve_background_host",
            "deb_tau_of_a", "deb_plan_create_grouped", "deb_forward_grouped",
-           "deb_forward_record", "deb_replay", "deb_get_power", "deb_power_multipoles", "deb_density_velocity",
+           "deb_forward_record", "deb_forward_record_ckpt", "deb_plan_create_adjoint", "deb_adjoint", "deb_replay",
+           "deb_get_power", "deb_power_multipoles", "deb_density_velocity",
            "deb_power_kaiser", "deb_savgol_log", "deb_fftlog_phase",
            "deb_plan_destroy", "deb_measure_fp64_peak", "deb_error_string", "deb_version")
 
@@ -71,6 +72,12 @@ def load(path: str | None = None):
                                      ctypes.POINTER(DebSolverCfg), vp, vp, vp, vp]
     L.deb_forward_record.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp,
                                      ctypes.POINTER(DebSolverCfg), vp, vp, vp, vp, ctypes.c_int, vp, vp]
+    L.deb_forward_record_ckpt.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp,
+                                          ctypes.POINTER(DebSolverCfg), vp, vp, vp, vp, ctypes.c_int, vp, vp,
+                                          ctypes.c_int, vp, vp]
+    L.deb_plan_create_adjoint.argtypes = [ctypes.POINTER(DebDims), ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+    L.deb_adjoint.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, ctypes.c_int, vp, vp,
+                              vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, vp]
     L.deb_replay.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp,
                              ctypes.POINTER(DebSolverCfg), vp, ctypes.c_int, vp, vp, vp, vp]
     L.deb_get_power.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
@@ -105,14 +112,20 @@ def check(rc: int, what: str):
 class Plan:
     """Owns one deb_plan (device workspace sized for max_modes)."""
 
-    def __init__(self, dims: DebDims, max_modes: int, launch: tuple[str, int] | None = None, batch_size: int = 0):
+    def __init__(self, dims: DebDims, max_modes: int, launch: tuple[str, int] | None = None, batch_size: int = 0,
+                 adjoint_seg_cap: int = 0):
         """``launch`` = (stage vectors "auto" | "shared" | "global", modes per SM cap or 0);
-        ``batch_size`` > 0 makes a grouped plan (deb_plan_create_grouped)."""
+        ``batch_size`` > 0 makes a grouped plan (deb_plan_create_grouped);
+        ``adjoint_seg_cap`` > 0 an adjoint plan (deb_plan_create_adjoint)
+        for ``max_modes`` items and checkpoint strides up to that value."""
         self.dims = dims
         self.max_modes = max_modes
         self.batch_size = batch_size
         self.ptr = ctypes.c_void_p()
-        if batch_size > 0:
+        if adjoint_seg_cap > 0:
+            check(load().deb_plan_create_adjoint(ctypes.byref(dims), int(max_modes), int(adjoint_seg_cap),
+                                                 ctypes.byref(self.ptr)), "deb_plan_create_adjoint")
+        elif batch_size > 0:
             check(load().deb_plan_create_grouped(ctypes.byref(dims), int(max_modes), int(batch_size),
                                                  ctypes.byref(self.ptr)), "deb_plan_create_grouped")
         elif launch is None:

@@ -1,0 +1,71 @@
+// deb_internal.h -- library-internal declarations shared by the CUDA
+// translation units (not part of the C ABI).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "deb_core.cuh"
+
+struct deb_plan {
+  deb::Dims D;
+  int dense, return_full, nout, exec_mode;
+  int max_modes, nsm;
+  long slot_len, dense_len;
+  // lane mode
+  int lane_blocks, lane_slots;
+  // warp mode
+  int warp_block_warps, warp_blocks, warp_smem, warp_k_global, warp_per_sm;
+  // grouped plans (deb_plan_create_grouped): modes per group, warps in flight
+  int group_size, group_warps;
+  long warp_smem_bytes;
+  double* kws;      // warp mode: stage vectors in global memory
+  double* ws;       // lane slots (or warp slots when shared memory is too small)
+  double* dws;      // dense matrices
+  int* queue;
+  int* order_dev;   // replay order (max_modes ints)
+  const int* user_order;   // deb_plan_set_order
+  int user_order_n;
+  size_t ws_bytes;
+  // adjoint plans (deb_plan_create_adjoint): warps in flight, states per
+  // segment, per-warp workspace (doubles) and its array
+  int adj, adj_warps, adj_seg_cap;
+  long adj_wslot;
+  double* adj_ws;
+};
+
+
+namespace deb_internal {
+
+using PFN_ctxGetCurrent = CUresult (*)(CUcontext*);
+using PFN_ctxGetId = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique id of the current thread's CUDA context (never reused within a
+// process), 0 if it cannot be determined.  The driver entry points are found
+// through the runtime, so the library needs no link to libcuda.
+inline unsigned long long current_ctx_id() {
+  static PFN_ctxGetCurrent get_cur = nullptr;
+  static PFN_ctxGetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_cur = (PFN_ctxGetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (PFN_ctxGetId)f;
+  });
+  if (!get_cur || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  if (get_cur(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  unsigned long long id = 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id + 1;   // 0 stays "unknown"
+}
+
+}  // namespace deb_internal

@@ -24,6 +24,7 @@
 #include <mutex>
 
 #include "deb_core.cuh"
+#include "deb_internal.h"
 #include "discoeb_gb300.h"
 
 namespace {
@@ -61,6 +62,10 @@ struct KParams {
   // queue order: queue position q takes mode order[q] (forward) or mode
   // order[q / nset], set q % nset (replay); null = index order
   const int* order;
+  // record with checkpoints: ckpt [nmode, ck_cap, n], ckstride [nmode]
+  double* ckpt;
+  int ck_cap;
+  int* ckstride;
   deb::Ctl ctl;
   deb::Dims D;
 };
@@ -91,6 +96,9 @@ __device__ bool prepare_mode(const KParams& P, int q, deb::Cosmo& c, deb::ModeCo
   if (ok) ok = deb::load_cosmo(P.tables + (long)ti * P.blob_len, P.blob_len, c) && c.nq == P.D.nq;
   run.rec = P.rec ? P.rec + (long)m * P.rec_len : nullptr;
   run.rec_cap = P.rec_len - 1;
+  run.ck = (P.ctl.record && P.ckpt) ? P.ckpt + (long)m * P.ck_cap * P.D.n : nullptr;
+  run.ck_cap = P.ck_cap;
+  run.ck_stride = 1;
   run.nrec = (P.ctl.replay && P.nrec) ? P.nrec[m] : 0;
   if (ok && P.ctl.replay) ok = run.nrec >= 1 && run.nrec <= run.rec_cap;
   if (!ok) {
@@ -142,6 +150,7 @@ __global__ void __launch_bounds__(kBlock) forward_lane_kernel(KParams P) {
         P.status[mode] = run.status;
         if (P.steps) { P.steps[2 * mode] = run.acc; P.steps[2 * mode + 1] = run.rej; }
         if (P.ctl.record && P.nrec) P.nrec[mode] = run.status == deb::ST_OK ? run.acc : 0;   // record: set 0, item = mode
+        if (P.ctl.record && P.ckstride) P.ckstride[mode] = run.ck_stride;
         active = fetch();
       }
     }
@@ -178,6 +187,7 @@ __global__ void __launch_bounds__(32) forward_warp_kernel(KParams P) {
       P.status[m] = run.status;
       if (P.steps) { P.steps[2 * m] = run.acc; P.steps[2 * m + 1] = run.rej; }
       if (P.ctl.record && P.nrec) P.nrec[m] = run.status == deb::ST_OK ? run.acc : 0;
+      if (P.ctl.record && P.ckstride) P.ckstride[m] = run.ck_stride;
     }
     __syncwarp();
   }
@@ -299,44 +309,15 @@ unsigned long long g_attr_ctx[64] = {0};
 // largest dynamic shared memory size set on forward_warp_kernel, per device
 long g_warp_smem_attr[64] = {0};
 
-using PFN_ctxGetCurrent = CUresult (*)(CUcontext*);
-using PFN_ctxGetId = CUresult (*)(CUcontext, unsigned long long*);
-
-// Unique id of the current thread's CUDA context (never reused within a
-// process), 0 if it cannot be determined.  The driver entry points are found
-// through the runtime, so the library needs no link to libcuda.
-unsigned long long current_ctx_id() {
-  static PFN_ctxGetCurrent get_cur = nullptr;
-  static PFN_ctxGetId get_id = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      get_cur = (PFN_ctxGetCurrent)f;
-    f = nullptr;
-    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      get_id = (PFN_ctxGetId)f;
-  });
-  if (!get_cur || !get_id) return 0;
-  CUcontext ctx = nullptr;
-  if (get_cur(&ctx) != CUDA_SUCCESS || !ctx) return 0;
-  unsigned long long id = 0;
-  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
-  return id + 1;   // 0 stays "unknown"
-}
-
 int upload_constants() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return DEB_ERR_CUDA;
-  unsigned long long ctx = current_ctx_id();
+  unsigned long long ctx = deb_internal::current_ctx_id();
   if (ctx == 0) {
     // no context current on this thread yet: let the runtime make the
     // device's primary context current, then ask again
     if (cudaFree(nullptr) != cudaSuccess) return DEB_ERR_CUDA;
-    ctx = current_ctx_id();
+    ctx = deb_internal::current_ctx_id();
   }
   std::lock_guard<std::mutex> lock(g_state_mu);
   if (dev >= 0 && dev < 64 && ctx != 0 && g_consts_ctx[dev] == ctx) return DEB_OK;
@@ -354,7 +335,7 @@ int upload_constants() {
 // `bytes` in the current context (only ever raised, so that plans made
 // earlier with a larger slot stay launchable).
 int ensure_warp_smem(int dev, long bytes) {
-  const unsigned long long ctx = current_ctx_id();
+  const unsigned long long ctx = deb_internal::current_ctx_id();
   std::lock_guard<std::mutex> lock(g_state_mu);
   const bool known = dev >= 0 && dev < 64 && ctx != 0 && g_attr_ctx[dev] == ctx;
   if (known && g_warp_smem_attr[dev] >= bytes) return DEB_OK;
@@ -367,27 +348,6 @@ int ensure_warp_smem(int dev, long bytes) {
 
 }  // namespace
 
-struct deb_plan {
-  deb::Dims D;
-  int dense, return_full, nout, exec_mode;
-  int max_modes, nsm;
-  long slot_len, dense_len;
-  // lane mode
-  int lane_blocks, lane_slots;
-  // warp mode
-  int warp_block_warps, warp_blocks, warp_smem, warp_k_global, warp_per_sm;
-  // grouped plans (deb_plan_create_grouped): modes per group, warps in flight
-  int group_size, group_warps;
-  long warp_smem_bytes;
-  double* kws;      // warp mode: stage vectors in global memory
-  double* ws;       // lane slots (or warp slots when shared memory is too small)
-  double* dws;      // dense matrices
-  int* queue;
-  int* order_dev;   // replay order (max_modes ints)
-  const int* user_order;   // deb_plan_set_order
-  int user_order_n;
-  size_t ws_bytes;
-};
 
 extern "C" {
 
@@ -600,6 +560,7 @@ int deb_plan_launch_info(const deb_plan* p, deb_launch_cfg* cfg, int* modes_in_f
 
 void deb_plan_destroy(deb_plan* p) {
   if (!p) return;
+  cudaFree(p->adj_ws);
   cudaFree(p->ws);
   cudaFree(p->dws);
   cudaFree(p->kws);
@@ -622,9 +583,10 @@ namespace {
 int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, int blob_len, const double* d_k,
                    const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
                    double* d_y_out, int* d_status, int* d_steps, double* d_record, int rec_len, int* d_nrec,
-                   int record, int replay, void* stream) {
+                   int record, int replay, void* stream, double* d_ckpt = nullptr, int ck_cap = 0,
+                   int* d_ckstride = nullptr) {
   if (!p || !cfg || ncosmo <= 0 || nset <= 0 || nmode < 0 || blob_len <= deb::HDR_LEN) return DEB_ERR_INVALID;
-  if (p->group_size > 0) return DEB_ERR_INVALID;   // a grouped plan serves deb_forward_grouped only
+  if (p->group_size > 0 || p->adj) return DEB_ERR_INVALID;   // grouped / adjoint plans serve their own calls only
   if (nmode == 0) return DEB_OK;
   if (!d_tables || !d_k || !d_tau_out || !d_y_out || !d_status) return DEB_ERR_INVALID;
   if ((long)nmode * nset > p->max_modes) return DEB_ERR_CAPACITY;
@@ -632,6 +594,7 @@ int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, in
   if ((record || replay) && (!d_record || !d_nrec || rec_len < 2)) return DEB_ERR_INVALID;
   if (record && rec_len < cfg->max_steps + 1) return DEB_ERR_INVALID;
   if (replay && p->exec_mode != DEB_EXEC_WARP) return DEB_ERR_INVALID;
+  if (d_ckpt && (!record || !d_ckstride || ck_cap < 2 || (ck_cap & 1))) return DEB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   KParams P{};
   P.tables = d_tables; P.ncosmo = ncosmo; P.blob_len = blob_len; P.k = d_k; P.cosmo = d_cosmo_of_mode;
@@ -640,6 +603,7 @@ int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, in
   P.smem = p->warp_smem;
   P.kws = p->kws;
   P.rec = d_record; P.rec_len = rec_len; P.nrec = d_nrec; P.nset = nset;
+  P.ckpt = d_ckpt; P.ck_cap = ck_cap; P.ckstride = d_ckstride;
   P.order = (!replay && p->user_order && p->user_order_n == nmode) ? p->user_order : nullptr;
   P.ctl.rtol = cfg->rtol; P.ctl.atol = cfg->atol;
   P.ctl.b1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / cfg->error_order;
@@ -718,6 +682,15 @@ int deb_forward_record(deb_plan* p, const double* d_tables, int ncosmo, int blob
                        void* stream) {
   return launch_forward(p, d_tables, ncosmo, 1, blob_len, d_k, d_cosmo_of_mode, nmode, d_tau_out, cfg, d_y_out,
                         d_status, d_steps, d_record, rec_len, d_nrec, 1, 0, stream);
+}
+
+int deb_forward_record_ckpt(deb_plan* p, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
+                            const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+                            double* d_y_out, int* d_status, int* d_steps, double* d_record, int rec_len, int* d_nrec,
+                            double* d_ckpt, int ck_cap, int* d_ckstride, void* stream) {
+  if (!d_ckpt) return DEB_ERR_INVALID;
+  return launch_forward(p, d_tables, ncosmo, 1, blob_len, d_k, d_cosmo_of_mode, nmode, d_tau_out, cfg, d_y_out,
+                        d_status, d_steps, d_record, rec_len, d_nrec, 1, 0, stream, d_ckpt, ck_cap, d_ckstride);
 }
 
 int deb_replay(deb_plan* p, const double* d_tables, int ncosmo, int nset, int blob_len, const double* d_k,

@@ -140,6 +140,43 @@ def _device_tables(plist, pert, aexp_out, nqmax, out=None):
                 taus=tau_all[nc:]), st
 
 
+def choose_method(method, nout, npar, lmax, linear_solver):
+    """'adjoint' (one reverse sweep per output time and mode, ~3-5 forward
+    steps of work each) or 'replay' (2 npar forward solves of the recorded
+    steps): 'auto' takes the adjoint while nout seeds cost less than the
+    2 npar replays, and when the hierarchy and solver allow it."""
+    ok = linear_solver == "structured" and min(lmax) >= 5
+    if method == "auto":
+        return "adjoint" if ok and 4 * nout <= 2 * npar else "replay"
+    if method not in ("adjoint", "replay"):
+        raise ValueError(f"method must be 'auto', 'adjoint' or 'replay', not {method!r}")
+    if method == "adjoint" and not ok:
+        raise ValueError("the adjoint needs the structured solver and lmaxg, lmaxgp, lmaxr >= 5")
+    return method
+
+
+def seg_cap_for(max_steps, ck_cap):
+    """Largest checkpoint stride a record with ck_cap slots can reach."""
+    return max(1, -(-2 * int(max_steps) // int(ck_cap)))
+
+
+_adj_plans: dict = {}
+
+
+def adjoint_plan(dims, items, seg_cap):
+    """Cached adjoint plan (deb_plan_create_adjoint) for >= items work items."""
+    import torch
+
+    key = (torch.cuda.current_device(), dims.lmaxg, dims.lmaxgp, dims.lmaxr, dims.lmaxnu, dims.nqmax, dims.nout,
+           int(seg_cap))
+    p = _adj_plans.get(key)
+    if p is None or p.max_modes < items:
+        _adj_plans.pop(key, None)
+        p = _native.Plan(dims, max(int(items), 1), adjoint_seg_cap=int(seg_cap))
+        _adj_plans[key] = p
+    return p
+
+
 class GradientProblem:
     """Device-resident inputs, buffers and plan of one gradient launch pair.
 
@@ -159,7 +196,8 @@ class GradientProblem:
 
     def __init__(self, plist, backgrounds, pert, kmodes, aexp_out, *, lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, rtol, atol,
                  pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, max_steps=2048, idx=4,
-                 theta=THETA, step_to_outputs=False, launch=None, linear_solver="structured"):
+                 theta=THETA, step_to_outputs=False, launch=None, linear_solver="structured", method="auto",
+                 ck_cap=32):
         import torch
 
         self.theta = tuple(theta)
@@ -206,12 +244,25 @@ class GradientProblem:
         self.d_dl = torch.empty((nm, no, len(self.theta)), dtype=torch.float64, device=dev)
         self.ode_names = [n for (n, _, _, _) in pert[0]]
         self.dims = _pt._dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, no, False, linear_solver, "warp")
-        self.plan = _pt.get_plan(self.dims, ns * nm, launch)
+        self.method = choose_method(method, no, self.npar, (lmaxg, lmaxgp, lmaxr), linear_solver)
+        self.plan = _pt.get_plan(self.dims, (ns if self.method == "replay" else 1) * nm, launch)
         self.cfg = _pt._cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps,
                             step_to_outputs=step_to_outputs)
         self.order = torch.as_tensor(_pt.schedule_order(self.host_k)).to(dev, torch.int32)
         self.graph = None
         self._copied = None
+        if self.method == "adjoint":
+            n = _pt.nvar(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax)
+            self.ck_cap = int(ck_cap) + (int(ck_cap) & 1)
+            self.d_ckpt = torch.empty((nm, self.ck_cap, n), dtype=torch.float64, device=dev)
+            self.d_ckstride = torch.empty((nm,), dtype=torch.int32, device=dev)
+            # one cotangent seed per output time: seed o is d ln P(k, a_o) / d y
+            self.nseed = no
+            self.d_gy = torch.zeros((no, nm, no, 20), dtype=torch.float64, device=dev)
+            self.d_gth = torch.empty((no, nm, self.npar), dtype=torch.float64, device=dev)
+            self.d_ast = torch.empty((no * nm,), dtype=torch.int32, device=dev)
+            self.eps_c = torch.as_tensor(np.array([[e for (_, e, _, _) in pp] for pp in pert], dtype=np.float64)).to(dev)
+            self.adj_plan = adjoint_plan(self.dims, no * nm, seg_cap_for(max_steps, self.ck_cap))
 
     def load(self, plist, backgrounds, pert, stream=None):
         """Copy the inputs of another set of cosmologies of the same shape
@@ -262,10 +313,69 @@ class GradientProblem:
     def _record(self, plan, s):
         L = _native.load()
         c = lambda t: ctypes.c_void_p(t.data_ptr())
+        if self.method == "adjoint":
+            _native.check(_pt.launch_ordered(plan, self.order, self.nmode, lambda: L.deb_forward_record_ckpt(
+                plan.ptr, c(self.d_tab0), self.nc, self.blob_len, c(self.d_k), c(self.d_com), self.nmode,
+                c(self.d_tau0), ctypes.byref(self.cfg), c(self.d_y0), c(self.d_st0), c(self.d_steps), c(self.d_rec),
+                self.rec_len, c(self.d_nrec), c(self.d_ckpt), self.ck_cap, c(self.d_ckstride),
+                ctypes.c_void_p(s.cuda_stream))), "deb_forward_record_ckpt")
+            return
         _native.check(_pt.launch_ordered(plan, self.order, self.nmode, lambda: L.deb_forward_record(
             plan.ptr, c(self.d_tab0), self.nc, self.blob_len, c(self.d_k), c(self.d_com), self.nmode,
             c(self.d_tau0), ctypes.byref(self.cfg), c(self.d_y0), c(self.d_st0), c(self.d_steps), c(self.d_rec),
             self.rec_len, c(self.d_nrec), ctypes.c_void_p(s.cuda_stream))), "deb_forward_record")
+
+    def _adjoint(self, s, nseed):
+        """deb_adjoint of the first nseed cotangent seeds in d_gy on stream s."""
+        L = _native.load()
+        c = lambda t: ctypes.c_void_p(t.data_ptr())
+        _native.check(L.deb_adjoint(self.adj_plan.ptr, c(self.d_tab0), c(self.d_tabs), self.nc, self.npar,
+                                    self.blob_len, c(self.eps_c), c(self.d_k), c(self.d_com), self.nmode,
+                                    c(self.d_tau0), c(self.d_taus), c(self.d_rec), self.rec_len, c(self.d_nrec),
+                                    c(self.d_ckpt), self.ck_cap, c(self.d_ckstride), c(self.d_gy), int(nseed),
+                                    c(self.d_gth), c(self.d_ast), ctypes.c_void_p(s.cuda_stream)), "deb_adjoint")
+
+    def forward(self, stream=None):
+        """The recorded nominal solve (with checkpoints when the method is the
+        adjoint) and get_power, without gradients; returns P [nmode, nout]."""
+        import torch
+
+        s = stream if stream is not None else torch.cuda.current_stream()
+        self._record(self.plan, s)
+        L = _native.load()
+        c = lambda t: ctypes.c_void_p(t.data_ptr())
+        _native.check(L.deb_get_power(c(self.d_tab0), self.nc, self.blob_len, c(self.d_k), c(self.d_com),
+                                      self.nmode, self.nout, c(self.d_y0), 20, self.idx, c(self.d_P),
+                                      ctypes.c_void_p(s.cuda_stream)), "deb_get_power")
+        return self.d_P
+
+    def vjp(self, gP, stream=None):
+        """Gradient of sum_{k,a} gP P(k, a) over theta, per cosmology
+        [ncosmo, len(theta)], by one adjoint sweep per mode (after
+        :meth:`forward`; adjoint method only)."""
+        import torch
+
+        if self.method != "adjoint":
+            raise RuntimeError("vjp needs a problem built with method='adjoint'")
+        s = stream if stream is not None else torch.cuda.current_stream()
+        with torch.cuda.stream(s):
+            gP = gP.to(self.device, torch.float64).reshape(self.nmode, self.nout)
+            w = gP * self.d_P
+            self.d_gy[0].zero_()
+            self.d_gy[0, :, :, self.idx] = 2.0 * w / self.d_y0[:, :, self.idx]
+        self._adjoint(s, 1)
+        with torch.cuda.stream(s):
+            g = torch.zeros((self.nc, len(self.theta)), dtype=torch.float64, device=self.device)
+            com = self.d_com.long()
+            for j, name in enumerate(self.theta):
+                if name == "A_s":
+                    v = (w * self.d_inv_As).sum(dim=1)
+                elif name == "n_s":
+                    v = (w * self.d_lnk).sum(dim=1)
+                else:
+                    v = self.d_gth[0, :, self.ode_names.index(name)]
+                g[:, j].index_add_(0, com, v)
+        return g
 
     def tune(self, candidates=None):
         """Choose the launch shape by timing the nominal recorded solve with
@@ -291,16 +401,28 @@ class GradientProblem:
         self._record(self.plan, s)
         if events:
             events[1].record(s)
-        _native.check(L.deb_replay(self.plan.ptr, c(self.d_tabs), self.nc, self.nset, self.blob_len,
-                                   c(self.d_k), c(self.d_com), self.nmode, c(self.d_taus), ctypes.byref(self.cfg),
-                                   c(self.d_rec), self.rec_len, c(self.d_nrec), c(self.d_ys), c(self.d_sts), sp),
-                      "deb_replay")
-        if events:
-            events[2].record(s)
+        if self.method == "adjoint":
+            with torch.cuda.stream(s):
+                # seed o: d ln P(k, a_o) / d y = 2 / y_idx at output o
+                for o in range(self.nout):
+                    self.d_gy[o, :, o, self.idx] = 2.0 / self.d_y0[:, o, self.idx]
+            self._adjoint(s, self.nseed)
+            if events:
+                events[2].record(s)
+            with torch.cuda.stream(s):
+                dl_ode = self.d_gth.permute(2, 1, 0)        # [npar, nmode, nout]
+        else:
+            _native.check(L.deb_replay(self.plan.ptr, c(self.d_tabs), self.nc, self.nset, self.blob_len,
+                                       c(self.d_k), c(self.d_com), self.nmode, c(self.d_taus), ctypes.byref(self.cfg),
+                                       c(self.d_rec), self.rec_len, c(self.d_nrec), c(self.d_ys), c(self.d_sts), sp),
+                          "deb_replay")
+            if events:
+                events[2].record(s)
+            with torch.cuda.stream(s):
+                ys = self.d_ys[..., self.idx].reshape(self.nset, self.nmode, self.nout)
+                lp = torch.log(ys * ys)
+                dl_ode = (lp[0::2] - lp[1::2]) / (2.0 * self.eps_m)
         with torch.cuda.stream(s):
-            ys = self.d_ys[..., self.idx].reshape(self.nset, self.nmode, self.nout)
-            lp = torch.log(ys * ys)
-            dl_ode = (lp[0::2] - lp[1::2]) / (2.0 * self.eps_m)
             for j, name in enumerate(self.theta):
                 if name == "A_s":
                     self.d_dl[:, :, j] = self.d_inv_As
@@ -340,7 +462,7 @@ class GradientProblem:
 
     def check(self):
         st0 = self.d_st0.cpu().numpy()
-        sts = self.d_sts.cpu().numpy()
+        sts = (self.d_ast if self.method == "adjoint" else self.d_sts).cpu().numpy()
         if (st0 != 0).any() or (sts != 0).any():
             raise RuntimeError(f"{int((st0 != 0).sum())} nominal / {int((sts != 0).sum())} replayed mode(s) failed")
 
@@ -384,13 +506,34 @@ def _run_cached(plist, backgrounds, pert, kmodes, aexp_out, opts):
     return Pd, Dd, gp
 
 
+def _problem_inputs(plist, *, kmin, kmax, num_k, dologk, theta, rel_step, tables, backgrounds, processes, opts):
+    """k-grid, theta +- eps parameter sets and their tables' source for a
+    gradient problem of the cosmologies ``plist``."""
+    kmodes = np.geomspace(kmin, kmax, num_k) if dologk else np.linspace(kmin, kmax, num_k)
+    pert = [perturbed_params(p, theta, rel_step) for p in plist]
+    nset = 2 * len(pert[0])
+    if tables not in ("native", "gpu", "python"):
+        raise ValueError(f"tables must be 'native', 'gpu' or 'python', not {tables!r}")
+    if backgrounds is None and tables in ("native", "gpu"):
+        backgrounds = tables
+    elif backgrounds is None:
+        flat = []
+        for p, pp in zip(plist, pert):
+            flat.append(p)
+            for (_, _, a, b) in pp:
+                flat += [a, b]
+        ev = evolve_backgrounds(flat, processes)
+        backgrounds = [ev[i * (nset + 1):(i + 1) * (nset + 1)] for i in range(len(plist))]
+    return kmodes, pert, backgrounds, opts
+
+
 def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num_k: int, lmaxg: int = 11,
                               lmaxgp: int = 11, lmaxr: int = 11, lmaxnu: int = 8, nqmax: int = 3, rtol: float = 1e-4,
                               atol: float = 1e-4, pcoeff: float = 0.25, icoeff: float = 0.80, dcoeff: float = 0.0,
                               factormax: float = 20.0, factormin: float = 0.3, max_steps: int = 2048, idx: int = 4,
                               theta=THETA, rel_step: float = 1e-4, dologk: bool = True, processes=None,
                               backgrounds=None, throw: bool = True, step_to_outputs: bool = False,
-                              tables: str = "native"):
+                              tables: str = "native", method: str = "auto"):
     """P(k, a) and d log P / d theta for one or many cosmologies.
 
     ``params``: input parameter dict(s) as given to ``evolve_background``
@@ -410,24 +553,12 @@ def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num
     single = isinstance(params, dict)
     plist = [params] if single else list(params)
     nc = len(plist)
-    kmodes = np.geomspace(kmin, kmax, num_k) if dologk else np.linspace(kmin, kmax, num_k)
-    pert = [perturbed_params(p, theta, rel_step) for p in plist]
-    nset = 2 * len(pert[0])
-    if tables not in ("native", "gpu", "python"):
-        raise ValueError(f"tables must be 'native', 'gpu' or 'python', not {tables!r}")
-    if backgrounds is None and tables in ("native", "gpu"):
-        backgrounds = tables
-    elif backgrounds is None:
-        flat = []
-        for p, pp in zip(plist, pert):
-            flat.append(p)
-            for (_, _, a, b) in pp:
-                flat += [a, b]
-        ev = evolve_backgrounds(flat, processes)
-        backgrounds = [ev[i * (nset + 1):(i + 1) * (nset + 1)] for i in range(nc)]
-    opts = dict(lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr, lmaxnu=lmaxnu, nqmax=nqmax, rtol=rtol, atol=atol,
-                pcoeff=pcoeff, icoeff=icoeff, dcoeff=dcoeff, factormax=factormax, factormin=factormin,
-                max_steps=max_steps, idx=idx, theta=tuple(theta), step_to_outputs=step_to_outputs)
+    kmodes, pert, backgrounds, opts = _problem_inputs(
+        plist, kmin=kmin, kmax=kmax, num_k=num_k, dologk=dologk, theta=theta, rel_step=rel_step, tables=tables,
+        backgrounds=backgrounds, processes=processes,
+        opts=dict(lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr, lmaxnu=lmaxnu, nqmax=nqmax, rtol=rtol, atol=atol,
+                  pcoeff=pcoeff, icoeff=icoeff, dcoeff=dcoeff, factormax=factormax, factormin=factormin,
+                  max_steps=max_steps, idx=idx, theta=tuple(theta), step_to_outputs=step_to_outputs, method=method))
     Pd, Dd, gp = _run_cached(plist, backgrounds, pert, kmodes, aexp_out, opts)
     if throw:
         gp.check()
@@ -469,11 +600,13 @@ class PowerSpectrum:
     float64 tensor [8] in the order of :data:`THETA` (h, not H0), overriding
     those entries of ``base_params``; ``options`` is a dict of the keyword
     arguments of :func:`evolve_perturbations_grad` (aexp_out, kmin, kmax,
-    num_k, hierarchy sizes, tolerances, ...).  Forward runs the recorded
-    solve and the replay of theta +- eps (host tables for the 13 parameter
-    sets, one GPU launch pair) and returns P [num_k, nout] on theta's device;
-    it keeps d ln P / d theta, so backward is grad_theta = sum over (k, a) of
-    grad_P * P * d ln P / d theta, with no further solve.
+    num_k, hierarchy sizes, tolerances, tables, ...).  Forward runs the
+    recorded solve with checkpoints and returns P [num_k, nout] on theta's
+    device; backward is one discrete-adjoint sweep per mode
+    (``deb_adjoint``) with the cotangent grad_P, plus the analytic A_s and n_s
+    terms (``perturbations.py:1123``) -- a vector-Jacobian product whose cost
+    does not grow with the number of parameters or outputs.  Needs the
+    structured solver and lmaxg, lmaxgp, lmaxr >= 5.
     """
 
     _fn = None
@@ -492,17 +625,33 @@ class PowerSpectrum:
                     params = dict(base)
                     for name, v in zip(THETA, vals):
                         params = _with(params, name, float(v))
-                    P, D, _ = evolve_perturbations_grad(params=params, theta=THETA, **opts)
-                    Pt = torch.as_tensor(P, dtype=torch.float64, device=th.device)
-                    Dt = torch.as_tensor(D, dtype=torch.float64, device=th.device)
-                    ctx.save_for_backward(Pt, Dt)
-                    return Pt
+                    o = dict(opts)
+                    pkw = {k: o.pop(k) for k in ("kmin", "kmax", "num_k") if k in o}
+                    aexp_out = o.pop("aexp_out")
+                    throw = o.pop("throw", True)
+                    kmodes, pert, backgrounds, _ = _problem_inputs(
+                        [params], kmin=pkw["kmin"], kmax=pkw["kmax"], num_k=pkw["num_k"],
+                        dologk=o.pop("dologk", True), theta=THETA, rel_step=o.pop("rel_step", 1e-4),
+                        tables=o.pop("tables", "native"), backgrounds=o.pop("backgrounds", None),
+                        processes=o.pop("processes", None), opts=None)
+                    o.pop("method", None)
+                    gp = GradientProblem([params], backgrounds, pert, kmodes, aexp_out, theta=THETA,
+                                         method="adjoint", **o)
+                    P = gp.forward()
+                    if throw:
+                        st0 = gp.d_st0.cpu().numpy()
+                        if (st0 != 0).any():
+                            raise RuntimeError(f"{int((st0 != 0).sum())} mode(s) failed")
+                    ctx.gp = gp
+                    ctx.dev = th.device
+                    return P.detach().clone().to(th.device)
 
                 @staticmethod
                 def backward(ctx, gP):
-                    Pt, Dt = ctx.saved_tensors
-                    g = torch.einsum("ka,kat->t", gP.to(torch.float64) * Pt, Dt)
-                    return g, None, None
+                    g = ctx.gp.vjp(gP)
+                    if (ctx.gp.d_ast[:ctx.gp.nmode] != 0).any():
+                        raise RuntimeError("adjoint sweep failed for some modes")
+                    return g[0].to(ctx.dev), None, None
 
             cls._fn = _Fn
         return cls._fn.apply(theta, base_params, options)

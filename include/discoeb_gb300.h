@@ -190,6 +190,64 @@ int deb_replay(deb_plan* plan, const double* d_tables, int ncosmo, int nset, int
                const double* d_record, int rec_len, const int* d_nrec, double* d_y_out, int* d_status, void* stream);
 
 /*
+ * deb_forward_record that also keeps checkpoints for deb_adjoint: the state
+ * after every ck_stride-th accepted step (and the initial state), at most
+ * ck_cap of them per mode -- when the slots fill up every other one is
+ * dropped and the stride doubles, so a mode keeps between ck_cap / 2 and
+ * ck_cap evenly spaced states (ck_cap even, >= 2).
+ *   d_ckpt [nmode, ck_cap, nvar], d_ckstride [nmode] (the final stride)
+ * No counterpart in the reference (jax.jacfwd keeps no states).
+ */
+int deb_forward_record_ckpt(deb_plan* plan, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
+                            const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
+                            double* d_y_out, int* d_status, int* d_steps, double* d_record, int rec_len, int* d_nrec,
+                            double* d_ckpt, int ck_cap, int* d_ckstride, void* stream);
+
+/*
+ * Discrete adjoint of the recorded solve: for a cotangent of the output
+ * fields, d L / d theta of the nominal solve's frozen-step map -- the
+ * derivative the reference takes with jax.jacfwd through diffrax, whose PID
+ * controller stops gradients through the step factor (perturbations.py:765,
+ * DirectAdjoint; notebooks' compute_matter_power).  The map is: tau_start
+ * and the ICs of each parameter set, the recorded step ends scaled by
+ * tau_start / nominal tau_start (steps clipped to an output follow that
+ * output time, the last step ends at the last output time), the Rodas5
+ * steps (ode_integrators_stiff.py:718-834), SaveAt linear interpolation and
+ * the output fields (perturbations.py:374-523).  One reverse sweep per
+ * (seed, mode) replaces the 2 npar perturbed solves of deb_replay.
+ *
+ * theta enters through the tables: npar parameters, each given by its
+ * theta_p + eps_p and theta_p - eps_p table sets; the adjoint takes the
+ * derivatives of every table-dependent quantity it meets (the RHS
+ * coefficients at each stage point, the output conversion, tau_start, the
+ * ICs, tau_out) as central differences over those sets, everything else
+ * (the integration) exactly.  The log-a splines (x_e, c_s^2 a, log rho_nu,
+ * log p_nu) are evaluated on each set's own knots.
+ *
+ * A plan from deb_plan_create_adjoint (structured solver, 20 output fields,
+ * lmaxg, lmaxgp, lmaxr >= 5, nqmax <= 64, nout <= 64) serves deb_adjoint
+ * only; seg_cap = the largest checkpoint stride it accepts (a mode whose
+ * stride exceeds it gets DEB_MODE_BAD_INPUT), max_items >= nseed * nmode.
+ *   d_tables      [ncosmo, blob_len] nominal tables (those of the record)
+ *   d_tables_pm   [ncosmo * 2 npar, blob_len]: set 2p = +eps_p, 2p+1 = -eps_p
+ *   d_eps         [ncosmo, npar]
+ *   d_tau_out     [ncosmo, nout], d_tau_out_pm [ncosmo * 2 npar, nout]
+ *   d_record, rec_len, d_nrec, d_ckpt, ck_cap, d_ckstride: from
+ *                 deb_forward_record_ckpt on d_tables
+ *   d_gy          [nseed, nmode, nout, 20] cotangents of the output fields
+ *   d_gtheta      [nseed, nmode, npar] dL/dtheta per seed and mode (NaN for
+ *                 a failed item)
+ *   d_status      [nseed * nmode] deb_mode_status
+ * No counterpart in the reference (its gradient is forward mode).
+ */
+int deb_plan_create_adjoint(const deb_dims* dims, int max_items, int seg_cap, deb_plan** plan);
+int deb_adjoint(deb_plan* plan, const double* d_tables, const double* d_tables_pm, int ncosmo, int npar, int blob_len,
+                const double* d_eps, const double* d_k, const int* d_cosmo_of_mode, int nmode,
+                const double* d_tau_out, const double* d_tau_out_pm, const double* d_record, int rec_len,
+                const int* d_nrec, const double* d_ckpt, int ck_cap, const int* d_ckstride, const double* d_gy,
+                int nseed, double* d_gtheta, int* d_status, void* stream);
+
+/*
  * The reference's batched variant, evolve_perturbations_batched
  * (perturbations.py:1000-1061 with evolve_modes_batched :835-922 and
  * Rodas5Batched, ode_integrators_stiff.py:846-1010): groups of batch_size

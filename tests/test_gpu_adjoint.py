@@ -1,0 +1,137 @@
+"""The discrete adjoint on the GPU (deb_forward_record_ckpt + deb_adjoint).
+
+* against the host build of the same code (tests/native, one item at a
+  time): the same reverse sweep, so agreement to rounding amplified by the
+  solve (1e-8 of each parameter's largest |d ln P / d theta|);
+* against the GPU's own replay of the recorded steps on the theta +- eps
+  tables (central differences of the same frozen-step map, the derivative
+  jax.jacfwd takes through diffrax at perturbations.py:765): 1e-6 of each
+  parameter's largest derivative -- on the small hierarchy at one and at
+  eight outputs, and at nvar 323 with 128 k and 8 outputs (steps landing on
+  the outputs), the gradient workload of the fiducial cosmology;
+* the checkpoint count does not change the result (8 vs 1024 slots);
+* PowerSpectrum.backward (one adjoint sweep with grad_P) against the
+  contraction of the replay's Jacobian.
+"""
+import numpy as np
+import pytest
+
+import discoeb_gb300 as deb
+import discoeb_gb300.tables as tb
+from discoeb_gb300 import tables_gpu
+from discoeb_gb300.gradient import THETA, GradientProblem, perturbed_params, _get
+from discoeb_gb300.workloads import fiducial_mnu_param
+from native import harness as H
+
+pytestmark = pytest.mark.gpu
+
+DIMS = dict(lmaxg=8, lmaxgp=8, lmaxr=10, lmaxnu=8, nqmax=3)
+FID = dict(lmaxg=12, lmaxgp=12, lmaxr=17, lmaxnu=17, nqmax=15)
+
+
+@pytest.fixture(scope="module")
+def base():
+    return fiducial_mnu_param()
+
+
+def _both(base, k, a_out, dims, ck_cap=32, **kw):
+    pert = [perturbed_params(base)]
+    ga = GradientProblem([base], "native", pert, k, a_out, method="adjoint", ck_cap=ck_cap, **kw, **dims)
+    _, Da = ga.run()
+    ga.check()
+    gr = GradientProblem([base], "native", pert, k, a_out, method="replay", **kw, **dims)
+    _, Dr = gr.run()
+    gr.check()
+    return ga, Da.cpu().numpy(), Dr.cpu().numpy()
+
+
+def _close(Da, Dr, bar):
+    for j, name in enumerate(THETA):
+        scale = np.abs(Dr[..., j]).max()
+        assert np.abs(Da[..., j] - Dr[..., j]).max() <= bar * scale, (name, np.abs(Da[..., j] - Dr[..., j]).max() / scale)
+
+
+@pytest.mark.parametrize("a_out", [[1.0], list(np.linspace(0.2, 1.0, 8))])
+def test_adjoint_matches_replay_differences(base, a_out):
+    k = np.geomspace(1e-3, 1.0, 6)
+    _, Da, Dr = _both(base, k, a_out, DIMS, rtol=1e-6, atol=1e-9, max_steps=20000)
+    _close(Da, Dr, 1e-6)
+
+
+def test_adjoint_matches_host_build_of_the_same_code(base):
+    a_out = np.array([0.5, 1.0])
+    k = np.geomspace(1e-3, 1.0, 4)
+    kw = dict(rtol=1e-6, atol=1e-9, max_steps=20000)
+    ga, Da, _ = _both(base, k, a_out, DIMS, **kw)
+    pert = perturbed_params(base)
+    sets = [base] + [q for (_, _, a, b) in pert for q in (a, b)]
+    tabs, _ = tables_gpu.evolve_background_tables_host(sets, 3)
+    eps = np.array([e for (_, e, _, _) in pert])
+    taus = tb.tau_of_a_blob(tabs, a_out)
+    y0 = ga.d_y0.cpu().numpy()
+    dims = tuple(DIMS[n] for n in ("lmaxg", "lmaxgp", "lmaxr", "lmaxnu", "nqmax"))
+    for i, kk in enumerate(k):
+        for o in range(a_out.size):
+            gy = np.zeros((a_out.size, 20))
+            gy[o, 4] = 2.0 / y0[i, o, 4]
+            g, _, info, st = H.adjoint(tabs, eps, kk, taus, dims, gy, ck_cap=32, **kw)
+            assert st == 0
+            for p, name in enumerate(ga.ode_names):
+                j = THETA.index(name)
+                assert abs(Da[i, o, j] - g[p]) <= 1e-8 * np.abs(Da[..., j]).max(), (kk, o, name)
+
+
+def test_checkpoint_count_does_not_change_the_gradient(base):
+    k = np.geomspace(1e-3, 1.0, 5)
+    kw = dict(rtol=1e-6, atol=1e-9, max_steps=20000)
+    pert = [perturbed_params(base)]
+    out = []
+    for cap in (8, 1024):
+        gp = GradientProblem([base], "native", pert, k, [1.0], method="adjoint", ck_cap=cap, **kw, **DIMS)
+        _, D = gp.run()
+        gp.check()
+        out.append((D.cpu().numpy(), gp.d_ckstride.cpu().numpy()))
+    assert out[0][1].max() > 1 and out[1][1].max() == 1
+    _close(out[0][0], out[1][0], 1e-9)
+
+
+def test_adjoint_at_the_fiducial_gradient_workload(base):
+    """nvar 323, 128 k in [1e-3, 1], 8 outputs a in [0.2, 1] with steps landing
+    on the outputs, rtol 1e-5: the cosmology and sizes of the gradient
+    workload, adjoint (8 seeds per mode) against the replay."""
+    k = np.geomspace(1e-3, 1.0, 128)
+    ga, Da, Dr = _both(base, k, list(np.linspace(0.2, 1.0, 8)), FID, rtol=1e-5, atol=1e-5, max_steps=20000,
+                       step_to_outputs=True)
+    _close(Da, Dr, 1e-6)
+
+
+def test_power_spectrum_backward_is_one_adjoint_sweep(base):
+    import torch
+
+    opts = dict(aexp_out=[0.5, 1.0], kmin=1e-3, kmax=0.5, num_k=5, rtol=1e-6, atol=1e-9, max_steps=20000, **DIMS)
+    theta = torch.tensor([float(_get(base, n)) for n in THETA], dtype=torch.float64, device="cuda", requires_grad=True)
+    P = deb.PowerSpectrum.apply(theta, base, opts)
+    P0, D0, _ = deb.evolve_perturbations_grad(params=base, method="replay", **opts)
+    np.testing.assert_allclose(P.detach().cpu().numpy(), P0, rtol=1e-12)
+    w = torch.linspace(1.0, 2.0, P.numel(), dtype=torch.float64, device="cuda").reshape(P.shape)
+    (w * P).sum().backward()
+    expect = np.einsum("ka,ka,kat->t", w.cpu().numpy(), P0, D0)
+    got = theta.grad.cpu().numpy()
+    scale = np.abs(np.einsum("ka,ka,kat->kat", w.cpu().numpy(), P0, D0)).sum(axis=(0, 1))
+    assert (np.abs(got - expect) <= 1e-6 * scale).all(), (got, expect)
+
+
+def test_adjoint_reports_bad_items_and_leaves_others():
+    """An invalid k gets a failed status and NaN gradients; the other modes
+    are unaffected."""
+    base = fiducial_mnu_param()
+    k = np.array([1e-3, -1.0, 0.1])
+    pert = [perturbed_params(base)]
+    gp = GradientProblem([base], "native", pert, k, [1.0], method="adjoint", rtol=1e-5, atol=1e-8,
+                         max_steps=20000, **DIMS)
+    _, D = gp.run()
+    ast = gp.d_ast.cpu().numpy()
+    D = D.cpu().numpy()
+    assert ast[1] != 0 and ast[0] == 0 and ast[2] == 0
+    ode = [THETA.index(n) for n in gp.ode_names]
+    assert np.isnan(D[1, 0, ode]).all() and np.isfinite(D[[0, 2]][:, 0, ode]).all()

@@ -251,3 +251,26 @@ def test_more_chains_and_gather_entries_than_lanes():
     assert (st["status"] == 0).all() and (so[:, 0] == 0).all()
     np.testing.assert_allclose(y[:, 0, 4], yo[:, 0, 4], rtol=1e-5)
     np.testing.assert_allclose(y[:, 0, 8], yo[:, 0, 8], rtol=1e-5, atol=1e-9 * np.abs(yo[:, 0, 8]).max())
+
+
+def test_config4_hierarchy_against_the_oracle():
+    """lmax 32 everywhere and 30 momentum bins (nvar 1098, the large batched
+    workload's hierarchy) at rtol 1e-6, three low-k modes and two outputs,
+    against the oracle's dense-LU solve.  At this size a mode's 16 vectors
+    do not fit shared memory with two modes per SM, so the kernel runs its
+    global stage-vector shape."""
+    from discoeb_gb300.workloads import sample_cosmologies
+
+    p = bg.evolve_background(param=sample_cosmologies(1, seed=7)[0][0])
+    d4 = dict(lmaxg=32, lmaxgp=32, lmaxr=32, lmaxnu=32, nqmax=30)
+    assert deb.nvar(**d4) == 1098
+    k = np.array([1e-5, 3e-5, 1e-4])
+    blob = tb.pack_cosmology(p, 30)
+    tau = tb.tau_of_a(p, [0.5, 1.0])
+    y, st = deb.solve(blob[None], k, tau[None], rtol=1e-6, atol=1e-6, return_stats=True, max_steps=4000, **d4)
+    yo, so = oracle.solve(blob, k, tau, rtol=1e-6, atol=1e-6, max_steps=4000, **d4)
+    assert (st["status"] == 0).all() and (so[:, 0] == 0).all()
+    np.testing.assert_allclose(y[:, 1, 4], yo[:, 1, 4], rtol=1e-6)
+    np.testing.assert_allclose(y[:, :, 4], yo[:, :, 4], rtol=1e-4)
+    for f in (8, 10, 12):
+        np.testing.assert_allclose(y[:, 1, f], yo[:, 1, f], rtol=1e-6, atol=1e-9 * np.abs(yo[:, 1, f]).max())
