@@ -9,9 +9,10 @@ FP64 input tables on the host.
 from .perturbations import (evolve_perturbations, evolve_perturbations_batched, evolve_perturbations_multi,
                             get_power, nvar, solve, DeviceProblem)
 from .background import evolve_background, get_neutrino_momentum_bins
-from .gradient import PowerSpectrum, THETA, evolve_perturbations_grad, fisher_matrix
+from .gradient import PowerSpectrum, THETA, evolve_perturbations_grad, fisher_matrix, loglike_grad
 from .tables_gpu import evolve_background_tables, evolve_background_tables_host
 
 __all__ = ["evolve_perturbations", "evolve_perturbations_batched", "evolve_perturbations_multi", "get_power", "nvar",
            "solve", "DeviceProblem", "evolve_background", "get_neutrino_momentum_bins", "evolve_perturbations_grad",
-           "fisher_matrix", "PowerSpectrum", "THETA", "evolve_background_tables", "evolve_background_tables_host"]
+           "fisher_matrix", "PowerSpectrum", "THETA", "evolve_background_tables", "evolve_background_tables_host",
+           "loglike_grad"]

@@ -27,7 +27,7 @@ class DebLaunchCfg(ctypes.Structure):
     _fields_ = [("stage_vectors", ctypes.c_int), ("modes_per_sm", ctypes.c_int)]
 
 
-STAGE_VECTORS = {"auto": 0, "shared": 1, "global": 2}
+STAGE_VECTORS = {"auto": 0, "shared": 1, "global": 2, "all_global": 3}
 
 
 class DebSolverCfg(ctypes.Structure):

@@ -20,8 +20,10 @@ import os
 
 from . import _native
 
-# (stage vectors, modes-per-SM cap); 0 = as many as fit
-CANDIDATES = (("shared", 0), ("shared", 4), ("global", 0), ("global", 6))
+# (stage vectors, modes-per-SM cap); 0 = as many as fit.  "all_global" keeps
+# the whole mode state in L2-resident global memory: at nvar 1098 the shared
+# part alone (72 KB) limits the other shapes to three modes per SM.
+CANDIDATES = (("shared", 0), ("shared", 4), ("global", 0), ("global", 6), ("all_global", 0))
 
 _chosen: dict = {}
 _loaded = False

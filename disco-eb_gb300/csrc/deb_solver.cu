@@ -379,7 +379,7 @@ int deb_plan_create_ex(const deb_dims* dims, int max_modes, const deb_launch_cfg
   if (!dims || !out || max_modes <= 0) return DEB_ERR_INVALID;
   const int stage_where = lc ? lc->stage_vectors : DEB_STAGE_AUTO;
   const int mps_cap = lc ? lc->modes_per_sm : 0;
-  if (stage_where < DEB_STAGE_AUTO || stage_where > DEB_STAGE_GLOBAL || mps_cap < 0) return DEB_ERR_INVALID;
+  if (stage_where < DEB_STAGE_AUTO || stage_where > DEB_STAGE_ALL_GLOBAL || mps_cap < 0) return DEB_ERR_INVALID;
   *out = nullptr;
   if (dims->lmaxg < 3 || dims->lmaxgp < 3 || dims->lmaxr < 3 || dims->lmaxnu < 3 || dims->nqmax < 1 || dims->nout < 1)
     return DEB_ERR_INVALID;
@@ -440,7 +440,7 @@ int deb_plan_create_ex(const deb_dims* dims, int max_modes, const deb_launch_cfg
     }
     smem_bytes = k_global ? hot_bytes : full_bytes;
     p->warp_k_global = k_global ? 1 : 0;
-    p->warp_smem = smem_bytes <= smem_optin;
+    p->warp_smem = smem_bytes <= smem_optin && stage_where != DEB_STAGE_ALL_GLOBAL;
     if (!p->warp_smem) p->warp_k_global = 0;
     p->warp_block_warps = 1;
     // blocks (= modes in flight) per SM limited by shared memory, by
@@ -551,7 +551,7 @@ int deb_plan_launch_info(const deb_plan* p, deb_launch_cfg* cfg, int* modes_in_f
     cfg->modes_per_sm = 0;
     *modes_in_flight = p->lane_slots;
   } else {
-    cfg->stage_vectors = (p->warp_smem && !p->warp_k_global) ? DEB_STAGE_SHARED : DEB_STAGE_GLOBAL;
+    cfg->stage_vectors = !p->warp_smem ? DEB_STAGE_ALL_GLOBAL : (!p->warp_k_global ? DEB_STAGE_SHARED : DEB_STAGE_GLOBAL);
     cfg->modes_per_sm = p->warp_per_sm;
     *modes_in_flight = p->warp_blocks;
   }

@@ -197,7 +197,7 @@ class GradientProblem:
     def __init__(self, plist, backgrounds, pert, kmodes, aexp_out, *, lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, rtol, atol,
                  pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, max_steps=2048, idx=4,
                  theta=THETA, step_to_outputs=False, launch=None, linear_solver="structured", method="auto",
-                 ck_cap=32):
+                 ck_cap=32, jacobian=True):
         import torch
 
         self.theta = tuple(theta)
@@ -238,13 +238,14 @@ class GradientProblem:
         self.d_y0 = torch.empty((nm, no, 20), dtype=torch.float64, device=dev)
         self.d_st0 = torch.empty((nm,), dtype=torch.int32, device=dev)
         self.d_steps = torch.empty((nm, 2), dtype=torch.int32, device=dev)
-        self.d_ys = torch.empty((ns * nm, no, 20), dtype=torch.float64, device=dev)
-        self.d_sts = torch.empty((ns * nm,), dtype=torch.int32, device=dev)
+        self.method = choose_method(method, no, self.npar, (lmaxg, lmaxgp, lmaxr), linear_solver)
+        if self.method == "replay":
+            self.d_ys = torch.empty((ns * nm, no, 20), dtype=torch.float64, device=dev)
+            self.d_sts = torch.empty((ns * nm,), dtype=torch.int32, device=dev)
         self.d_P = torch.empty((nm, no), dtype=torch.float64, device=dev)
         self.d_dl = torch.empty((nm, no, len(self.theta)), dtype=torch.float64, device=dev)
         self.ode_names = [n for (n, _, _, _) in pert[0]]
         self.dims = _pt._dims(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, no, False, linear_solver, "warp")
-        self.method = choose_method(method, no, self.npar, (lmaxg, lmaxgp, lmaxr), linear_solver)
         self.plan = _pt.get_plan(self.dims, (ns if self.method == "replay" else 1) * nm, launch)
         self.cfg = _pt._cfg(rtol, atol, pcoeff, icoeff, dcoeff, factormax, factormin, max_steps,
                             step_to_outputs=step_to_outputs)
@@ -256,13 +257,15 @@ class GradientProblem:
             self.ck_cap = int(ck_cap) + (int(ck_cap) & 1)
             self.d_ckpt = torch.empty((nm, self.ck_cap, n), dtype=torch.float64, device=dev)
             self.d_ckstride = torch.empty((nm,), dtype=torch.int32, device=dev)
-            # one cotangent seed per output time: seed o is d ln P(k, a_o) / d y
-            self.nseed = no
-            self.d_gy = torch.zeros((no, nm, no, 20), dtype=torch.float64, device=dev)
-            self.d_gth = torch.empty((no, nm, self.npar), dtype=torch.float64, device=dev)
-            self.d_ast = torch.empty((no * nm,), dtype=torch.int32, device=dev)
+            # the Jacobian takes one cotangent seed per output time (seed o is
+            # d ln P(k, a_o) / d y); a vector-Jacobian product takes one
+            self.nseed = no if jacobian else 1
+            nsd = self.nseed
+            self.d_gy = torch.zeros((nsd, nm, no, 20), dtype=torch.float64, device=dev)
+            self.d_gth = torch.empty((nsd, nm, self.npar), dtype=torch.float64, device=dev)
+            self.d_ast = torch.empty((nsd * nm,), dtype=torch.int32, device=dev)
             self.eps_c = torch.as_tensor(np.array([[e for (_, e, _, _) in pp] for pp in pert], dtype=np.float64)).to(dev)
-            self.adj_plan = adjoint_plan(self.dims, no * nm, seg_cap_for(max_steps, self.ck_cap))
+            self.adj_plan = adjoint_plan(self.dims, nsd * nm, seg_cap_for(max_steps, self.ck_cap))
 
     def load(self, plist, backgrounds, pert, stream=None):
         """Copy the inputs of another set of cosmologies of the same shape
@@ -365,8 +368,11 @@ class GradientProblem:
             self.d_gy[0, :, :, self.idx] = 2.0 * w / self.d_y0[:, :, self.idx]
         self._adjoint(s, 1)
         with torch.cuda.stream(s):
-            g = torch.zeros((self.nc, len(self.theta)), dtype=torch.float64, device=self.device)
-            com = self.d_com.long()
+            if getattr(self, "d_gvjp", None) is None:
+                self.d_gvjp = torch.zeros((self.nc, len(self.theta)), dtype=torch.float64, device=self.device)
+                self.d_com_l = self.d_com.long()
+            g = self.d_gvjp
+            g.zero_()
             for j, name in enumerate(self.theta):
                 if name == "A_s":
                     v = (w * self.d_inv_As).sum(dim=1)
@@ -374,7 +380,7 @@ class GradientProblem:
                     v = (w * self.d_lnk).sum(dim=1)
                 else:
                     v = self.d_gth[0, :, self.ode_names.index(name)]
-                g[:, j].index_add_(0, com, v)
+                g[:, j].index_add_(0, self.d_com_l, v)
         return g
 
     def tune(self, candidates=None):
@@ -402,6 +408,8 @@ class GradientProblem:
         if events:
             events[1].record(s)
         if self.method == "adjoint":
+            if self.nseed != self.nout:
+                raise RuntimeError("this problem was built for vector-Jacobian products (jacobian=False)")
             with torch.cuda.stream(s):
                 # seed o: d ln P(k, a_o) / d y = 2 / y_idx at output o
                 for o in range(self.nout):
@@ -568,6 +576,156 @@ def evolve_perturbations_grad(*, params, aexp_out, kmin: float, kmax: float, num
     return (P[0], D[0], kmodes) if single else (P, D, kmodes)
 
 
+class LoglikeProblem:
+    """Device-resident Gaussian log-likelihood of P(k, a) and its gradient.
+
+    ln L_c = -1/2 sum_{k,a} w_{k,a} (ln P_c(k, a) - lnP_data_c(k, a))^2 for
+    every cosmology c, and d ln L_c / d theta by one adjoint sweep per mode
+    (:meth:`GradientProblem.vjp`): the cotangent of P is
+    -w (ln P - lnP_data) / P.  :meth:`run` enqueues the recorded solve with
+    checkpoints, get_power, the likelihood and the adjoint on one stream;
+    :meth:`capture` / :meth:`replay` as for :class:`GradientProblem`;
+    :meth:`load` copies another call's tables and data into the same buffers.
+    """
+
+    def __init__(self, plist, backgrounds, pert, kmodes, aexp_out, lnP_data, weights, **opts):
+        import torch
+
+        opts = dict(opts)
+        opts["method"] = "adjoint"
+        opts["jacobian"] = False
+        self.gp = GradientProblem(plist, backgrounds, pert, kmodes, aexp_out, **opts)
+        gp = self.gp
+        dev = gp.device
+        self.shape = (gp.nc, gp.num_k, gp.nout)
+        self._pdata = torch.zeros(self.shape, dtype=torch.float64).pin_memory()
+        self.d_data = torch.empty((gp.nmode, gp.nout), dtype=torch.float64, device=dev)
+        w = np.broadcast_to(np.asarray(weights, dtype=np.float64), (gp.num_k, gp.nout))
+        self.d_w = torch.as_tensor(np.tile(w, (gp.nc, 1))).to(dev)
+        self.d_lnL = torch.zeros((gp.nc,), dtype=torch.float64, device=dev)
+        self.set_data(lnP_data)
+        self.graph = None
+        self.calls = 0
+
+    def set_data(self, lnP_data, stream=None):
+        import torch
+
+        self._pdata.numpy()[...] = np.asarray(lnP_data, dtype=np.float64).reshape(self.shape)
+        s = stream if stream is not None else torch.cuda.current_stream()
+        with torch.cuda.stream(s):
+            self.d_data.copy_(self._pdata.reshape(self.d_data.shape), non_blocking=True)
+        return self._pdata.numel() * 8
+
+    def run(self, stream=None):
+        import torch
+
+        gp = self.gp
+        s = stream if stream is not None else torch.cuda.current_stream()
+        P = gp.forward(s)
+        with torch.cuda.stream(s):
+            r = torch.log(P) - self.d_data
+            gP = -self.d_w * r / P
+            self.d_lnL.zero_()
+            if getattr(self, "_com", None) is None:
+                self._com = gp.d_com.long()
+            self.d_lnL.index_add_(0, self._com, (-0.5 * self.d_w * r * r).sum(dim=1))
+        g = gp.vjp(gP, s)
+        return P, self.d_lnL, g
+
+    def capture(self):
+        import torch
+
+        self.run()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.out = self.run(torch.cuda.current_stream())
+        self.graph = g
+        return g
+
+    def replay(self, stream=None):
+        import torch
+
+        if self.graph is None:
+            self.capture()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        with torch.cuda.stream(s):
+            self.graph.replay()
+        return self.out
+
+    def load(self, plist, backgrounds, pert, lnP_data, stream=None):
+        return self.gp.load(plist, backgrounds, pert, stream) + self.set_data(lnP_data, stream)
+
+    def check(self):
+        st0 = self.gp.d_st0.cpu().numpy()
+        ast = self.gp.d_ast[:self.gp.nmode].cpu().numpy()
+        if (st0 != 0).any() or (ast != 0).any():
+            raise RuntimeError(f"{int((st0 != 0).sum())} forward / {int((ast != 0).sum())} adjoint mode(s) failed")
+
+
+_ll_problems: dict = {}
+
+
+def loglike_grad(*, params, lnP_data, weights, aexp_out, kmin: float, kmax: float, num_k: int, lmaxg: int = 11,
+                 lmaxgp: int = 11, lmaxr: int = 11, lmaxnu: int = 8, nqmax: int = 3, rtol: float = 1e-4,
+                 atol: float = 1e-4, pcoeff: float = 0.25, icoeff: float = 0.80, dcoeff: float = 0.0,
+                 factormax: float = 20.0, factormin: float = 0.3, max_steps: int = 2048, idx: int = 4, theta=THETA,
+                 rel_step: float = 1e-4, dologk: bool = True, processes=None, backgrounds=None, throw: bool = True,
+                 step_to_outputs: bool = False, tables: str = "native", ck_cap: int = 32):
+    """Gaussian log-likelihood of P(k, a) and its gradient over theta.
+
+    ln L = -1/2 sum_{k,a} weights (ln P(k, a) - lnP_data)^2 per cosmology,
+    with ``lnP_data`` [ncosmo, num_k, nout] (or [num_k, nout] for a single
+    dict) and ``weights`` broadcastable to [num_k, nout] (e.g. N_k / 2, the
+    inverse variance of ln P of a diagonal Gaussian covariance).  The gradient
+    is one discrete-adjoint sweep per mode (``deb_adjoint``): its cost does
+    not grow with the number of parameters or output times.  Returns
+    ``(P [ncosmo, num_k, nout], lnL [ncosmo], grad [ncosmo, len(theta)],
+    kmodes)``, the cosmology axis dropped for a single dict.  Repeated calls
+    of the same shape replay a captured CUDA graph with the new inputs.
+    """
+    import torch
+
+    single = isinstance(params, dict)
+    plist = [params] if single else list(params)
+    nc = len(plist)
+    opts = dict(lmaxg=lmaxg, lmaxgp=lmaxgp, lmaxr=lmaxr, lmaxnu=lmaxnu, nqmax=nqmax, rtol=rtol, atol=atol,
+                pcoeff=pcoeff, icoeff=icoeff, dcoeff=dcoeff, factormax=factormax, factormin=factormin,
+                max_steps=max_steps, idx=idx, theta=tuple(theta), step_to_outputs=step_to_outputs, ck_cap=ck_cap)
+    kmodes, pert, backgrounds, _ = _problem_inputs(plist, kmin=kmin, kmax=kmax, num_k=num_k, dologk=dologk,
+                                                   theta=theta, rel_step=rel_step, tables=tables,
+                                                   backgrounds=backgrounds, processes=processes, opts=None)
+    aexp = np.atleast_1d(np.asarray(aexp_out, dtype=np.float64))
+    data = np.asarray(lnP_data, dtype=np.float64).reshape(nc, num_k, aexp.shape[0])
+    key = (torch.cuda.current_device(), nc, kmodes.tobytes(), aexp.tobytes(), tuple(sorted(opts.items())),
+           np.asarray(weights, dtype=np.float64).tobytes(), backgrounds if isinstance(backgrounds, str) else "dicts")
+    lp = _ll_problems.get(key)
+    if lp is not None:
+        try:
+            lp.load(plist, backgrounds, pert, data)
+        except ValueError:
+            lp = None
+            _ll_problems.pop(key, None)
+    if lp is None:
+        lp = LoglikeProblem(plist, backgrounds, pert, kmodes, aexp, data, weights, **opts)
+        while len(_ll_problems) >= _MAX_CACHED:
+            _ll_problems.pop(next(iter(_ll_problems)))
+        _ll_problems[key] = lp
+    lp.calls += 1
+    if lp.calls == 1:
+        P, lnL, g = lp.run()
+    elif lp.graph is None:
+        lp.capture()
+        P, lnL, g = lp.out
+    else:
+        P, lnL, g = lp.replay()
+    if throw:
+        lp.check()
+    P = P.reshape(nc, num_k, -1).cpu().numpy()
+    lnL, g = lnL.cpu().numpy(), g.cpu().numpy()
+    return (P[0], lnL[0], g[0], kmodes) if single else (P, lnL, g, kmodes)
+
+
 def fisher_matrix(kmodes, dlogP, volume_mpc3: float):
     """F_ij = sum_{k,a} d_i lnP d_j lnP / sigma^2_lnP with sigma^2_lnP = 2 / N_k,
     N_k = V k^2 dk / (2 pi^2) (diagonal Gaussian covariance, one volume V per
@@ -636,7 +794,7 @@ class PowerSpectrum:
                         processes=o.pop("processes", None), opts=None)
                     o.pop("method", None)
                     gp = GradientProblem([params], backgrounds, pert, kmodes, aexp_out, theta=THETA,
-                                         method="adjoint", **o)
+                                         method="adjoint", jacobian=False, **o)
                     P = gp.forward()
                     if throw:
                         st0 = gp.d_st0.cpu().numpy()

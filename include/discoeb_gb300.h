@@ -126,7 +126,8 @@ int deb_plan_workspace_bytes(const deb_plan* plan, size_t* bytes);
  * times the candidates and picks one.  deb_plan_create uses
  * {DEB_STAGE_AUTO, 0}: shared when two modes fit per SM, else global.
  */
-enum deb_stage_vectors { DEB_STAGE_AUTO = 0, DEB_STAGE_SHARED = 1, DEB_STAGE_GLOBAL = 2 };
+enum deb_stage_vectors { DEB_STAGE_AUTO = 0, DEB_STAGE_SHARED = 1, DEB_STAGE_GLOBAL = 2,
+                         DEB_STAGE_ALL_GLOBAL = 3 /* the whole mode state in global memory (large nvar) */ };
 typedef struct deb_launch_cfg {
   int stage_vectors;   /* enum deb_stage_vectors */
   int modes_per_sm;    /* cap on modes in flight per SM, 0 = no cap */

@@ -241,7 +241,7 @@ int h_adjoint(const double* tables, int npar, int blob_len, double k, const doub
   r.ck = ck.data(); r.ck_cap = ck_cap;
   mode_begin<1>(GP, f.c, f.m, f.D, ctl, f.A.w, tau_out, r);
   while (mode_step<1>(GP, f.c, f.m, f.D, f.T, f.R, ctl, f.A.w, tau_out, y_out, 1, r)) {}
-  info[0] = r.status; info[1] = r.acc; info[2] = r.ck_stride;
+  info[0] = r.status; info[1] = r.acc; info[2] = r.ck_stride; info[3] = r.rej;
   if (r.status != ST_OK) return -4;
   // ck is laid out [slot][n] (stride 1 per element here, as on the GPU)
   Box b;

@@ -203,11 +203,11 @@ def adj_outputs(blob, dims, k, a, s):
 
 
 def adjoint(tables, eps, k, tau_out, dims, gy, rtol=1e-5, atol=1e-5, max_steps=20000, ck_cap=32, step_to_outputs=False,
-            pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, debug=False):
+            pcoeff=0.25, icoeff=0.80, dcoeff=0.0, factormax=20.0, factormin=0.3, debug=False, full_info=False):
     """One mode: record (with checkpoints) on tables[0], then the adjoint of
     the cotangent gy [nout, 20]; tables [1 + 2 npar, L] (nominal, then +eps,
     -eps per parameter), tau_out [1 + 2 npar, nout].  Returns (gtheta [npar],
-    y_out [nout, 20], (status, nrec, ck_stride), adjoint status)."""
+    y_out [nout, 20], (status, accepted, ck_stride, rejected), adjoint status)."""
     tables = np.ascontiguousarray(tables, dtype=np.float64)
     tau_out = np.ascontiguousarray(tau_out, dtype=np.float64)
     npar = (tables.shape[0] - 1) // 2
@@ -216,7 +216,7 @@ def adjoint(tables, eps, k, tau_out, dims, gy, rtol=1e-5, atol=1e-5, max_steps=2
                     1.0 if step_to_outputs else 0.0])
     gth = np.zeros(npar)
     y = np.zeros((nout, 20))
-    info = np.zeros(3, dtype=np.int32)
+    info = np.zeros(4, dtype=np.int32)
     eps = np.ascontiguousarray(eps, dtype=np.float64)
     gy = np.ascontiguousarray(gy, dtype=np.float64)
     n = 7 + (dims[0] + 1) + (dims[1] + 1) + (dims[2] + 1) + dims[4] * (dims[3] + 1) + 2
@@ -225,9 +225,9 @@ def adjoint(tables, eps, k, tau_out, dims, gy, rtol=1e-5, atol=1e-5, max_steps=2
                          max_steps, ck_cap, _p(eps), _p(gy), _p(gth), _p(y), _p(info, ctypes.c_int),
                          None if dbg is None else _p(dbg))
     if debug:
-        return gth, y, tuple(int(v) for v in info), rc, dict(lam0=dbg[:n], dts=dbg[n], dto=dbg[n + 1:n + 1 + nout],
+        return gth, y, tuple(int(v) for v in info[:3]), rc, dict(lam0=dbg[:n], dts=dbg[n], dto=dbg[n + 1:n + 1 + nout],
                                                              rec=dbg[n + 1 + nout:n + 2 + nout + int(info[1])])
-    return gth, y, tuple(int(v) for v in info), rc
+    return gth, y, tuple(int(v) for v in info[:3]) + ((int(info[3]),) if full_info else ()), rc
 
 
 def step_adj(tables, eps, dims, k, t0, dt, y0, lam=None):

@@ -36,5 +36,5 @@ def test_unreadable_cache_is_ignored(tmp_path, monkeypatch):
 
 
 def test_candidates_cover_both_stage_vector_placements():
-    assert {c[0] for c in autotune.CANDIDATES} == {"shared", "global"}
+    assert {c[0] for c in autotune.CANDIDATES} == {"shared", "global", "all_global"}
     assert all(c[1] >= 0 for c in autotune.CANDIDATES)
