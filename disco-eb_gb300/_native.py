@@ -40,7 +40,7 @@ class DebSolverCfg(ctypes.Structure):
 _lib = None
 EXPORTS = ("deb_nvar", "deb_plan_create", "deb_plan_create_ex", "deb_plan_launch_info", "deb_plan_workspace_bytes",
            "deb_plan_set_order", "deb_forward", "deb_forward_static", "deb_tables_blob_len", "deb_evolve_background",
-           "deb_evolve_background_host",
+           "deb_evolve_background_host", "deb_evolve_background_frozen", "deb_evolve_background_frozen_host",
            "deb_tau_of_a", "deb_plan_create_grouped", "deb_forward_grouped",
            "deb_forward_record", "deb_forward_record_ckpt", "deb_plan_create_adjoint", "deb_adjoint", "deb_replay",
            "deb_get_power", "deb_power_multipoles", "deb_density_velocity",
@@ -94,6 +94,8 @@ def load(path: str | None = None):
     L.deb_evolve_background.argtypes = [vp, vp, ci, vp, vp, vp, ci, vp, vp]
     L.deb_tau_of_a.argtypes = [vp, ci, ci, vp, ci, vp, vp]
     L.deb_evolve_background_host.argtypes = [vp, vp, ci, vp, vp, vp, ci, vp, ci]
+    L.deb_evolve_background_frozen.argtypes = [vp, vp, ci, vp, vp, vp, vp, ci, vp, ci, vp, vp]
+    L.deb_evolve_background_frozen_host.argtypes = [vp, vp, ci, vp, vp, vp, vp, ci, vp, ci, vp, ci]
     L.deb_plan_destroy.argtypes = [vp]
     L.deb_plan_destroy.restype = None
     L.deb_measure_fp64_peak.argtypes = [ctypes.POINTER(ctypes.c_double), vp]

@@ -88,6 +88,24 @@ int make_params(const deb_bg_cfg* cfg, const double* params, int nset, const dou
   return DEB_OK;
 }
 
+// produce_set of every set on nthreads host threads (<= 0: one per hardware thread)
+void host_sets(const TParams& P, int nthreads) {
+  const int nset = P.nset;
+  if (nset == 0) return;
+  int nt = nthreads > 0 ? nthreads : (int)std::thread::hardware_concurrency();
+  if (nt < 1) nt = 1;
+  if (nt > nset) nt = nset;
+  const size_t nsh = (size_t)debt::tables_smem_doubles(P.num_thermo, P.num_nu);
+  auto work = [&](int t) {
+    std::vector<double> sh(nsh);
+    for (int s = t; s < nset; s += nt) debt::produce_set(P, s, 0, 1, sh.data());
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
+}
+
 }  // namespace
 
 extern "C" {
@@ -113,19 +131,51 @@ int deb_evolve_background_host(const deb_bg_cfg* cfg, const double* params, int 
   TParams P;
   const int rc = make_params(cfg, params, nset, consts, grid, tables, blob_len, status, P);
   if (rc) return rc;
+  host_sets(P, nthreads);
+  return DEB_OK;
+}
+
+int deb_evolve_background_frozen(const deb_bg_cfg* cfg, const double* d_params, int nset, const int* d_leader,
+                                 const double* d_consts, const double* d_grid, double* d_steps, int step_cap,
+                                 double* d_tables, int blob_len, int* d_status, void* stream) {
+  TParams P;
+  const int rc = make_params(cfg, d_params, nset, d_consts, d_grid, d_tables, blob_len, d_status, P);
+  if (rc) return rc;
+  if (!d_leader || !d_steps || step_cap < 1) return DEB_ERR_INVALID;
   if (nset == 0) return DEB_OK;
-  int nt = nthreads > 0 ? nthreads : (int)std::thread::hardware_concurrency();
-  if (nt < 1) nt = 1;
-  if (nt > nset) nt = nset;
-  const size_t nsh = (size_t)debt::tables_smem_doubles(P.num_thermo, P.num_nu);
-  auto work = [&](int t) {
-    std::vector<double> sh(nsh);
-    for (int s = t; s < nset; s += nt) debt::produce_set(P, s, 0, 1, sh.data());
-  };
-  std::vector<std::thread> pool;
-  for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
-  work(0);
-  for (auto& th : pool) th.join();
+  P.leader = d_leader; P.steps = d_steps; P.step_cap = step_cap;
+  const size_t smem = (size_t)debt::tables_smem_doubles(P.num_thermo, P.num_nu) * sizeof(double);
+  if (smem > 48 * 1024) {
+    if (cudaFuncSetAttribute(tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return DEB_ERR_INVALID;
+  }
+  for (int phase = 1; phase <= 2; ++phase) {
+    P.phase = phase;
+    tables_kernel<<<nset, 32, smem, (cudaStream_t)stream>>>(P);
+    if (cudaGetLastError() != cudaSuccess) return DEB_ERR_CUDA;
+  }
+  return DEB_OK;
+}
+
+int deb_evolve_background_frozen_host(const deb_bg_cfg* cfg, const double* params, int nset, const int* leader,
+                                      const double* consts, const double* grid, double* steps, int step_cap,
+                                      double* tables, int blob_len, int* status, int nthreads) {
+  TParams P;
+  const int rc = make_params(cfg, params, nset, consts, grid, tables, blob_len, status, P);
+  if (rc) return rc;
+  if (!leader || (steps && step_cap < 1)) return DEB_ERR_INVALID;
+  if (nset == 0) return DEB_OK;
+  std::vector<double> own;
+  if (!steps) {
+    step_cap = 16 * P.num_thermo;
+    own.resize((size_t)nset * (size_t)(3 * P.num_thermo + 1 + 2 * step_cap));
+    steps = own.data();
+  }
+  P.leader = leader; P.steps = steps; P.step_cap = step_cap;
+  for (int phase = 1; phase <= 2; ++phase) {
+    P.phase = phase;
+    host_sets(P, nthreads);
+  }
   return DEB_OK;
 }
 

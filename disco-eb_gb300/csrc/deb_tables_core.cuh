@@ -180,10 +180,29 @@ HD double romberg_dtauda(const Bk& B, double a, double b, int divmax) {
 }
 
 // ---------------------------------------------------------------- RECFAST
+// The branch decisions of one RHS evaluation (nine conditions on the state
+// values, one bit each): taken freely (no Br), recorded (mode 1: bits out)
+// or replayed from a leading set's record (mode 2: bits in), so that a
+// theta +- eps set evaluates the branches the nominal values selected, as
+// jax.jacfwd differentiates a jnp.where on the nominal values.
+struct Br {
+  int mode = 0;
+  unsigned bits = 0;
+};
+enum { BR_TSIGN = 0, BR_BOLTZ, BR_HE_EDGE, BR_H_PARTIAL, BR_H_SAHA, BR_H_PEEBLES0, BR_HE_ZERO, BR_H_FULL, BR_TM_LOCK,
+       BR_NBITS };
+
+HD bool take(Br* b, int bit, bool c) {
+  if (!b) return c;
+  if (b->mode == 2) return ((b->bits >> bit) & 1u) != 0;
+  if (c) b->bits |= 1u << bit;
+  return c;
+}
+
 // d(x_H, x_He, T_m)/da (thermodynamics_recfast.py:124-281); branch
-// conditions on the values; aH = a'/a at a
+// conditions on the values (or replayed, see Br); aH = a'/a at a
 template <class S>
-HD void ion_rhs(const TC& K, const Bk& B, double a, const S* y, double aH, S* f) {
+HD void ion_rhs(const TC& K, const Bk& B, double a, const S* y, double aH, S* f, Br* br = nullptr) {
   const double z = 1.0 / a - 1.0;
   const double H = B.H0 / 100.0;
   const double HO = H * K[DEB_TC_BIG_H];
@@ -192,7 +211,7 @@ HD void ion_rhs(const TC& K, const Bk& B, double a, const S* y, double aH, S* f)
   const double Nnow = K[DEB_TC_DENS_FAC] * H * H * B.Ob / mu_H;
   const S x_H = y[0], x_He = y[1], T2 = y[2];
   const S x = x_H + fHe * x_He;
-  const S Tmat = val(T2) >= 0.0 ? T2 : -T2;
+  const S Tmat = take(br, BR_TSIGN, val(T2) >= 0.0) ? T2 : -T2;
   const double zt = 1.0 + z;
   const double n = Nnow * zt * zt * zt;
   const double n_He = fHe * n;
@@ -207,7 +226,7 @@ HD void ion_rhs(const TC& K, const Bk& B, double a, const S* y, double aH, S* f)
   const S Rdown_He = K[DEB_TC_A_VF] / (sq0 * dpow(1.0 + sq0, 1.0 - K[DEB_TC_B_VF]) * dpow(1.0 + sq1, 1.0 + K[DEB_TC_B_VF]));
   const S Rup_He = 4.0 * Rdown_He * CRT15 * dexp(-K[DEB_TC_CDB_HE] / Tmat);
   const S bt = K[DEB_TC_BFACT] / Tmat;
-  const S He_Boltz = dexp(val(bt) < 680.0 ? bt : S(680.0));
+  const S He_Boltz = dexp(take(br, BR_BOLTZ, val(bt) < 680.0) ? bt : S(680.0));
   const S Rdown_trip = K[DEB_TC_A_TRIP] / (sq0 * dpow(1.0 + sq0, 1.0 - K[DEB_TC_B_TRIP]) * dpow(1.0 + sq1, 1.0 + K[DEB_TC_B_TRIP]));
   const S Rup_trip = Rdown_trip * dexp(-K[DEB_TC_HCL_HE2ST_ION_KB] / Tmat) * CRT15 * (4.0 / 3.0);
   const double lz = log(zt);
@@ -218,7 +237,7 @@ HD void ion_rhs(const TC& K, const Bk& B, double a, const S* y, double aH, S* f)
   const S nHe1 = n_He * omxHe;
   const double Hzz = Hz * zt;
   const double xHe_r = val(x_He), xH_r = val(x_H);
-  const bool he_edge = (xHe_r < 5e-9) || (xHe_r > 0.98);
+  const bool he_edge = take(br, BR_HE_EDGE, (xHe_r < 5e-9) || (xHe_r > 0.98));
   const double c2 = K[DEB_TC_C] * K[DEB_TC_C];
   S K_He;
   if (he_edge) {
@@ -226,7 +245,7 @@ HD void ion_rhs(const TC& K, const Bk& B, double a, const S* y, double aH, S* f)
   } else {
     const S tauHe_s = K[DEB_TC_A2P_S] * K[DEB_TC_CK_HE] * 3.0 * nHe1 / Hz;
     const S pHe_s = (1.0 - dexp(-tauHe_s)) / tauHe_s;
-    if (xH_r < 0.9999999) {
+    if (take(br, BR_H_PARTIAL, xH_r < 0.9999999)) {
       const S Dop = dsqrt(2.0 * K[DEB_TC_KB] * Tmat / (K[DEB_TC_MH] * K[DEB_TC_MHE_MH] * c2));
       const S Dop_2p = K[DEB_TC_C] * K[DEB_TC_L_HE_2P] * Dop;
       const double cl = K[DEB_TC_C] * K[DEB_TC_L_HE_2P];
@@ -242,11 +261,11 @@ HD void ion_rhs(const TC& K, const Bk& B, double a, const S* y, double aH, S* f)
   const S timeTh = (1.0 / (K[DEB_TC_CT] * Trad4)) * (1.0 + x + fHe) / x;
   const double timeH = 2.0 / (3.0 * HO * pow(zt, 1.5));
   S f0, f1, f2;
-  if (xH_r > 0.99) {
+  if (take(br, BR_H_SAHA, xH_r > 0.99)) {
     f0 = 0.0 * x_H;
   } else {
     const S rate = x * x_H * n * Rdown - Rup * omxH * dexp(-K[DEB_TC_CL] / Tmat);
-    if (xH_r > 0.985) {
+    if (take(br, BR_H_PEEBLES0, xH_r > 0.985)) {
       f0 = rate / Hzz;
     } else {
       const S KLn = KK * K[DEB_TC_LAMBDA_H] * n * omxH;
@@ -254,7 +273,7 @@ HD void ion_rhs(const TC& K, const Bk& B, double a, const S* y, double aH, S* f)
       f0 = rate * (1.0 + KLn) / (Hzz * den);
     }
   }
-  if (xHe_r < 1e-8) {
+  if (take(br, BR_HE_ZERO, xHe_r < 1e-8)) {
     f1 = 0.0 * x_He;
   } else {
     const S rate_He = x * x_He * n * Rdown_He - Rup_He * omxHe * dexp(-K[DEB_TC_CL_HE] / Tmat);
@@ -267,7 +286,7 @@ HD void ion_rhs(const TC& K, const Bk& B, double a, const S* y, double aH, S* f)
       const S pHe_t = (1.0 - dexp(-tauHe_t)) / tauHe_t;
       const S ePSt = dexp(-K[DEB_TC_CL_PST] / Tmat);
       S CfHe_t;
-      if (xH_r > 0.99999) {
+      if (take(br, BR_H_FULL, xH_r > 0.99999)) {
         CfHe_t = K[DEB_TC_A2P_T] * pHe_t * ePSt;
       } else {
         const S Dop = dsqrt(2.0 * K[DEB_TC_KB] * Tmat / (K[DEB_TC_MH] * K[DEB_TC_MHE_MH] * c2));
@@ -283,7 +302,7 @@ HD void ion_rhs(const TC& K, const Bk& B, double a, const S* y, double aH, S* f)
       f1 = f1 + trip * CfHe_t / Hzz;
     }
   }
-  if (val(timeTh) < K[DEB_TC_H_FRAC] * timeH) {
+  if (take(br, BR_TM_LOCK, val(timeTh) < K[DEB_TC_H_FRAC] * timeH)) {
     f2 = Tmat / zt;
   } else {
     f2 = K[DEB_TC_CT] * Trad4 * x / (1.0 + x + fHe) * (Tmat - Trad) / Hzz + 2.0 * Tmat / zt;
@@ -320,15 +339,19 @@ HD void inv3(const double A[3][3], double X[3][3]) {
 
 // one GRK4A step, every stage at t0 (ode_integrators_stiff.py:117-223)
 HD void grk4a_step(const TC& K, const Bk& B, double t0, double dt, const double* y0, double aH, double* y1,
-                           double* err) {
+                           double* err, Br* br3 = nullptr) {
   D3 yd[3], fd[3];
   for (int i = 0; i < 3; ++i) { yd[i] = D3(y0[i]); yd[i].d[i] = 1.0; }
-  ion_rhs<D3>(K, B, t0, yd, aH, fd);
+  ion_rhs<D3>(K, B, t0, yd, aH, fd, br3);
+  int ev = 0;
   double J[3][3], A[3][3], Ai[3][3];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) { J[i][j] = fd[i].d[j] * dt; A[i][j] = (i == j ? 1.0 : 0.0) - K[DEB_TC_G] * J[i][j]; }
   inv3(A, Ai);
-  auto f = [&](const double* y, double* o) { ion_rhs<double>(K, B, t0, y, aH, o); for (int i = 0; i < 3; ++i) o[i] *= dt; };
+  auto f = [&](const double* y, double* o) {
+    ion_rhs<double>(K, B, t0, y, aH, o, br3 ? br3 + (++ev) : nullptr);
+    for (int i = 0; i < 3; ++i) o[i] *= dt;
+  };
   double f0[3] = {fd[0].v * dt, fd[1].v * dt, fd[2].v * dt};
   double k1[3], k2[3], k3[3], k4[3], Jk1[3], Jk2[3], Jk3[3], t[3], u[3], f2[3];
   matvec3(Ai, f0, k1);
@@ -352,21 +375,70 @@ HD void grk4a_step(const TC& K, const Bk& B, double t0, double dt, const double*
   }
 }
 
+// Accepted steps of one set's history: a leading set's adaptive solve
+// writes (end, branch word) pairs, steps[2 pos], steps[2 pos + 1], while
+// pos < cap (pos keeps counting past cap, so that an overflow shows) and
+// the branch word of each interval's closing RHS evaluation into *fin; the
+// sets that follow it replay them.
+struct StepLog {
+  double* steps = nullptr;
+  int* pos = nullptr;
+  int cap = 0;
+  double* fin = nullptr;
+};
+
+// the three RHS evaluations of a GRK4A step in one exact integer word
+HD double pack3(const Br* b) {
+  return (double)(b[0].bits | (b[1].bits << BR_NBITS) | (b[2].bits << (2 * BR_NBITS)));
+}
+HD void unpack3(double w, Br* b) {
+  const unsigned u = (unsigned)w, m = (1u << BR_NBITS) - 1u;
+  for (int i = 0; i < 3; ++i) { b[i].mode = 2; b[i].bits = (u >> (i * BR_NBITS)) & m; }
+}
+
 // adaptive GRK4A from astart to aend under the I-controller the reference
 // inherits (safety 0.9, factor in [0.2, 10], error order 3, RMS norm);
 // out: x_H, x_He, T_m and their d/da at aend.  Returns false when the step
-// budget ran out before aend.
+// budget ran out before aend.  With `rep` (nrep (end, branch word) pairs,
+// the last end aend, and the closing evaluation's word *rep_fin) the steps
+// end there and take those branches instead, every step accepted: the
+// nominal step sequence a theta +- eps set follows, so that its tables are a
+// smooth function of theta -- the derivative jax.jacfwd takes through the
+// reference's diffeqsolve (thermodynamics_recfast.py:283-298, forward mode
+// through the nominal steps and the branches the nominal values select).
 HD bool solve_ionization(const TC& K, const Bk& B, double astart, double aend, const double* ystart, double rtol,
-                                 double atol, int max_steps, double* out) {
+                                 double atol, int max_steps, double* out, StepLog slog = StepLog(),
+                                 const double* rep = nullptr, int nrep = 0, double rep_fin = 0.0) {
   double t0 = astart;
   double t1 = fmin(astart + fabs(astart) * 1e-3, aend);
   double y[3] = {ystart[0], ystart[1], ystart[2]};
   int steps = 0;
+  Br fin;
+  if (rep) {
+    bool ok = true;
+    for (int j = 0; j < nrep; ++j) {
+      double y1[3], e[3];
+      Br b3[3];
+      unpack3(rep[2 * j + 1], b3);
+      grk4a_step(K, B, t0, rep[2 * j] - t0, y, aprimeoa(B, t0), y1, e, b3);
+      ok = ok && !(isnan(y1[0]) || isnan(y1[1]) || isnan(y1[2]));
+      y[0] = y1[0]; y[1] = y1[1]; y[2] = y1[2];
+      t0 = rep[2 * j];
+    }
+    fin.mode = 2;
+    fin.bits = (unsigned)rep_fin;
+    double dy[3];
+    ion_rhs<double>(K, B, aend, y, aprimeoa(B, aend), dy, &fin);
+    out[0] = y[0]; out[1] = y[1]; out[2] = y[2]; out[3] = dy[0]; out[4] = dy[1]; out[5] = dy[2];
+    return ok && t0 == aend;
+  }
   while (t0 < aend && steps < max_steps) {
     const double dt = t1 - t0;
     const double aH = aprimeoa(B, t0);
     double y1[3], e[3];
-    grk4a_step(K, B, t0, dt, y, aH, y1, e);
+    Br b3[3];
+    for (int i = 0; i < 3; ++i) b3[i].mode = 1;
+    grk4a_step(K, B, t0, dt, y, aH, y1, e, slog.pos ? b3 : nullptr);
     const bool nan1 = isnan(y1[0]) || isnan(y1[1]) || isnan(y1[2]);
     double ss = 0.0;
     for (int i = 0; i < 3; ++i) {
@@ -382,15 +454,32 @@ HD bool solve_ionization(const TC& K, const Bk& B, double astart, double aend, c
     if (keep) {
       y[0] = y1[0]; y[1] = y1[1]; y[2] = y1[2];
       t0 = t1;
+      if (slog.pos) {
+        if (*slog.pos < slog.cap) { slog.steps[2 * *slog.pos] = t1; slog.steps[2 * *slog.pos + 1] = pack3(b3); }
+        ++*slog.pos;
+      }
     }
     t1 = t0 + dt * fac;
     if (t1 > aend - 1e-10) t1 = aend;
     ++steps;
   }
+  fin.mode = 1;
   double dy[3];
-  ion_rhs<double>(K, B, aend, y, aprimeoa(B, aend), dy);
+  ion_rhs<double>(K, B, aend, y, aprimeoa(B, aend), dy, slog.fin ? &fin : nullptr);
+  if (slog.fin) *slog.fin = (double)fin.bits;
   out[0] = y[0]; out[1] = y[1]; out[2] = y[2]; out[3] = dy[0]; out[4] = dy[1]; out[5] = dy[2];
   return t0 >= aend;
+}
+
+// The positive root of x^2 + b x - c = 0 (c >= 0), (sqrt(b^2 + 4c) - b) / 2,
+// the form of the Saha fractions (thermodynamics_recfast.py:302-321,
+// 362-452); written as 2c / (sqrt(b^2 + 4c) + b) when b > 0, the same number
+// without the cancellation that costs the direct form ~b * 1e-16 absolute
+// (1e-7 for the hydrogen fraction near z = 2000), noise that a difference
+// quotient over parameter sets would divide by 2 eps.
+HD double quad_root(double b, double c) {
+  const double s = sqrt(b * b + 4.0 * c);
+  return b > 0.0 ? 2.0 * c / (s + b) : 0.5 * (s - b);
 }
 
 HD double saha_heii(const TC& K, const Bk& B, double a) {
@@ -406,7 +495,7 @@ HD double saha_heii(const TC& K, const Bk& B, double a) {
   const double R = pow(2.0 * K[DEB_TC_PI] * K[DEB_TC_ME] * K[DEB_TC_KB] / (K[DEB_TC_H_PLANCK] * K[DEB_TC_H_PLANCK]) * T, 1.5) / NH *
                    exp(-betaE);
   if (R > 1e5) return fHe * (1.0 - Bq / R + (1.0 + 5.0 * fHe + 6.0 * fHe * fHe) / (R * R));
-  return -(R - A) / 2.0 + sqrt((R - A) * (R - A) / 4.0 + R * Bq) - A;
+  return quad_root(R - A, R * Bq) - A;
 }
 
 struct TParams {
@@ -423,8 +512,17 @@ struct TParams {
   double amin, rtol, atol;
   double* tables;          // [nset, blob_len]
   int blob_len;
-  int* status;             // [nset] 0 ok, 1 step budget ran out in an interval
+  int* status;             // [nset] DEB_BG_* bits, 0 = ok
+  // frozen step sequences (all null/0: every set adaptive, one pass):
+  const int* leader = nullptr;   // [nset] -1: adaptive, recorded; j >= 0: follows set j
+  double* steps = nullptr;       // [nset, step_stride]: first step of each interval [num_thermo + 1],
+                                 // case of each interval and the branch word of its closing RHS
+                                 // evaluation [2 num_thermo], (end, branch word) of each step [2 step_cap]
+  int step_cap = 0;
+  int phase = 0;                 // 1: the adaptive sets, 2: the sets that follow one
 };
+
+HD long step_stride(const TParams& P) { return 3L * P.num_thermo + 1 + 2L * P.step_cap; }
 
 HD void put_derived(double* blob, long& p, const double* x, const double* y, const double* S, int n, int lane, int G) {
   double* c = blob + p;
@@ -455,7 +553,18 @@ HD long tables_smem_doubles(int N, int NN) {
 // of a group of G share the sampled work; sh: tables_smem_doubles() doubles.
 HD void produce_set(const TParams& P, int set, int lane, int G, double* sh) {
   if (set >= P.nset) return;
-  if (set >= P.nset) return;
+  // the set's role with frozen step sequences: leaders in phase 1, the sets
+  // that follow one in phase 2 (a leader index out of range or itself a
+  // follower is refused with DEB_BG_BAD_LEADER and the set runs adaptive)
+  int lead = -1, bad_leader = 0;
+  if (P.leader) {
+    lead = P.leader[set];
+    if ((lead >= 0) != (P.phase == 2)) return;
+    if (lead >= 0 && (lead >= P.nset || P.leader[lead] >= 0)) {
+      lead = -1;
+      bad_leader = DEB_BG_BAD_LEADER;
+    }
+  }
   const int N = P.num_thermo, NN = P.num_nu;
   double* th = sh;                 // [6][N]: x_H, x_He, T_m, dx_H/da, dx_He/da, dT_m/da
   double* xe = sh + 6 * N;         // [N]
@@ -521,35 +630,67 @@ HD void produce_set(const TParams& P, int set, int lane, int G, double* sh) {
     const double Tc = B.Tcmb;
     int bad = 0;
     double prev[6];
+    // step record of this set (a leader) or of the set it follows
+    double* rec = (P.leader && P.steps && lead < 0 && !bad_leader) ? P.steps + (long)set * step_stride(P) : nullptr;
+    const double* rep = (P.leader && P.steps && lead >= 0) ? P.steps + (long)lead * step_stride(P) : nullptr;
+    int pos = 0;
+    StepLog slog;
+    if (rec) { slog.steps = rec + 3 * N + 1; slog.pos = &pos; slog.cap = P.step_cap; }
+    // interval i: the leader's steps when it recorded all of them, adaptive
+    // otherwise (the leader did not integrate it, or its record overflowed)
+    auto solve = [&](int i, double astart, double aend, double* nw) {
+      if (rep) {
+        const int o0 = (int)rep[i], o1 = (int)rep[i + 1];
+        if (o1 > o0 && o1 <= P.step_cap)
+          return solve_ionization(K, B, astart, aend, prev, P.rtol, P.atol, P.max_steps, nw, StepLog(),
+                                  rep + 3 * N + 1 + 2 * o0, o1 - o0, rep[2 * N + 1 + i]) ? 0 : (int)DEB_BG_STEPS;
+        if (o1 > P.step_cap) bad |= DEB_BG_UNRECORDED;
+      }
+      StepLog lg = slog;
+      if (rec) lg.fin = rec + 2 * N + 1 + i;
+      return solve_ionization(K, B, astart, aend, prev, P.rtol, P.atol, P.max_steps, nw, lg) ? 0
+                                                                                               : (int)DEB_BG_STEPS;
+    };
     for (int i = 0; i < N; ++i) {
       const double astart = P.a_th[i], aend = P.a_th[i + 1];
+      if (rec) rec[i] = pos;
       const double zstart = 1.0 / astart - 1.0, zend = 1.0 / aend - 1.0;
       if (i == 0) {
         prev[0] = 1.0; prev[1] = 1.0; prev[2] = Tc * (1.0 + zstart); prev[3] = 0.0; prev[4] = 0.0;
         prev[5] = -Tc * (1.0 + zstart);
       }
       double nw[6];
-      if (zend > 3500.0) {
+      // the case of the thermal history (thermodynamics_recfast.py:362-452); a
+      // follower takes its leader's, as jax.jacfwd differentiates the branch
+      // the nominal values select
+      int br = zend > 3500.0 ? 0 : (i > 0 && prev[1] > 0.99) ? 1 : (i > 0 && prev[0] > 0.99) ? 2 : 3;
+      if (rep && br != 0) br = (int)rep[N + 1 + i];
+      if (rec) rec[N + 1 + i] = br;
+      if (br == 0) {
         nw[0] = 1.0; nw[1] = 1.0; nw[2] = Tc * (1.0 + zend); nw[3] = 0.0; nw[4] = 0.0; nw[5] = -Tc * (1.0 + zend);
-      } else if (i > 0 && prev[1] > 0.99) {
+      } else if (br == 1) {
         const double rhs = exp(1.5 * log(K[DEB_TC_CR] * Tc / (1.0 + zend)) -
                                K[DEB_TC_H_PLANCK] * K[DEB_TC_C] * K[DEB_TC_L_HE1_ION] / K[DEB_TC_KB] / (Tc * (1.0 + zend))) /
                            Nnow * 4.0;
-        const double xHe0 = 0.5 * (sqrt((rhs - 1.0) * (rhs - 1.0) + 4.0 * (1.0 + B.fHe) * rhs) - (rhs - 1.0));
+        const double xHe0 = quad_root(rhs - 1.0, (1.0 + B.fHe) * rhs);
         nw[0] = 1.0; nw[1] = (xHe0 - 1.0) / B.fHe; nw[2] = Tc * (1.0 + zend); nw[3] = 0.0; nw[4] = 0.0;
         nw[5] = -Tc * (1.0 + zend);
-      } else if (i > 0 && prev[0] > 0.99) {
+      } else if (br == 2) {
         const double rhs = exp(1.5 * log(K[DEB_TC_CR] * Tc / (1.0 + zend)) - K[DEB_TC_CB1] / (Tc * (1.0 + zend))) / Nnow;
-        const double xH0 = 0.5 * (sqrt(rhs * rhs + 4.0 * rhs) - rhs);
-        bad |= !solve_ionization(K, B, astart, aend, prev, P.rtol, P.atol, P.max_steps, nw);
+        const double xH0 = quad_root(rhs, rhs);
+        bad |= solve(i, astart, aend, nw);
         nw[0] = xH0;
         nw[3] = 0.0;
       } else {
-        bad |= !solve_ionization(K, B, astart, aend, prev, P.rtol, P.atol, P.max_steps, nw);
+        bad |= solve(i, astart, aend, nw);
       }
       for (int j = 0; j < 6; ++j) { th[j * N + i] = nw[j]; prev[j] = nw[j]; }
     }
-    if (P.status) P.status[set] = bad ? 1 : 0;
+    if (rec) {
+      rec[N] = pos;
+      if (pos > P.step_cap) bad |= DEB_BG_UNRECORDED;
+    }
+    if (P.status) P.status[set] = bad | bad_leader;
   }
   lane_sync(G);
   // per sample: x_e, c_s^2 a and the Romberg increment of tau

@@ -69,14 +69,22 @@ def evolve_backgrounds(params, processes=None, producer: str = "python"):
         return pool.map(_evolve, params)
 
 
+# Parameters whose values cross zero take eps relative to this scale at least
+# (w_a is drawn from [-0.3, 0.3]: eps = 1e-4 |w_a| would be 1e-7 at w_a = 1e-3,
+# where the quotient of the solve divides its rounding by 2e-7)
+EPS_SCALE = {"w_DE_a": 0.1}
+
+
 def perturbed_params(cosmo, theta=THETA, rel_step=1e-4):
-    """[(name, eps, param_plus, param_minus)] for the ODE parameters of theta."""
+    """[(name, eps, param_plus, param_minus)] for the ODE parameters of theta:
+    eps = rel_step * max(|theta|, EPS_SCALE[name])."""
     out = []
     for name in theta:
         if name in ANALYTIC:
             continue
         v = float(_get(cosmo, name))
-        eps = rel_step * abs(v) if v != 0.0 else rel_step
+        sc = max(abs(v), EPS_SCALE.get(name, 0.0))
+        eps = rel_step * sc if sc != 0.0 else rel_step
         out.append((name, eps, _with(cosmo, name, v + eps), _with(cosmo, name, v - eps)))
     return out
 
@@ -101,7 +109,8 @@ def _host_inputs(plist, backgrounds, pert, kmodes, aexp_out, nqmax):
         from . import tables_gpu
 
         sets = [q for pp in pert for (_, _, a, b) in pp for q in (a, b)]
-        tabs_all, _ = tables_gpu.evolve_background_tables_host(list(plist) + sets, nqmax)
+        tabs_all, _ = tables_gpu.evolve_background_tables_host(
+            list(plist) + sets, nqmax, leader=tables_gpu.follow_nominal(nc, len(sets) // nc))
         h.update(tab0=tabs_all[:nc], tau0=_tables.tau_of_a_blob(tabs_all[:nc], aexp_out),
                  tabs=tabs_all[nc:], taus=_tables.tau_of_a_blob(tabs_all[nc:], aexp_out))
     elif not _gpu_tables(backgrounds):
@@ -133,9 +142,10 @@ def _device_tables(plist, pert, aexp_out, nqmax, out=None):
 
     sets = [q for pp in pert for (_, _, a, b) in pp for q in (a, b)]
     o = out or (None, None)
-    tabs_all, tau_all, st = tables_gpu.evolve_background_tables(list(plist) + sets, nqmax, aexp_out=aexp_out,
-                                                                out=o[0], tau_out=o[1])
     nc = len(plist)
+    tabs_all, tau_all, st = tables_gpu.evolve_background_tables(list(plist) + sets, nqmax, aexp_out=aexp_out,
+                                                                out=o[0], tau_out=o[1],
+                                                                leader=tables_gpu.follow_nominal(nc, len(sets) // nc))
     return dict(tables_all=tabs_all, tau_all=tau_all, tab0=tabs_all[:nc], tau0=tau_all[:nc], tabs=tabs_all[nc:],
                 taus=tau_all[nc:]), st
 

@@ -328,7 +328,17 @@ def saha_heii(a, P):
     R = (2.0 * math.pi * M_E * K_B / H_PLANCK**2 * T) ** 1.5 / NH * math.exp(-betaE)
     if R > 1e5:
         return fHe * (1.0 - B / R + (1.0 + 5.0 * fHe + 6.0 * fHe**2) / R**2)
-    return -(R - A) / 2.0 + math.sqrt((R - A) ** 2 / 4.0 + R * B) - A
+    return quad_root(R - A, R * B) - A
+
+
+def quad_root(b: float, c: float) -> float:
+    """The positive root of x^2 + b x - c = 0 (c >= 0), (sqrt(b^2 + 4c) - b) / 2,
+    the form of the Saha fractions; as 2c / (sqrt(b^2 + 4c) + b) when b > 0,
+    the same number without the cancellation of the direct form (~b * 1e-16
+    absolute, noise that a difference quotient over parameter sets divides
+    by 2 eps)."""
+    s = math.sqrt(b * b + 4.0 * c)
+    return 2.0 * c / (s + b) if b > 0.0 else 0.5 * (s - b)
 
 
 def adaptive_sampling(a0: float, a1: float, N: int) -> np.ndarray:
@@ -371,11 +381,11 @@ def compute_thermal_history(*, a0, a1, N, param, rtol=1e-3, atol=1e-6, stage_tim
             new = np.array([1.0, 1.0, Tcmb * (1.0 + zend), 0.0, 0.0, -Tcmb * (1.0 + zend)])
         elif i > 0 and y_prev[1] > 0.99:
             rhs = math.exp(1.5 * math.log(CR * Tcmb / (1.0 + zend)) - H_PLANCK * C_LIGHT * L_HE1_ION / K_B / (Tcmb * (1.0 + zend))) / Nnow * 4.0
-            xHe0 = 0.5 * (math.sqrt((rhs - 1.0) ** 2 + 4.0 * (1.0 + fHe) * rhs) - (rhs - 1.0))
+            xHe0 = quad_root(rhs - 1.0, (1.0 + fHe) * rhs)
             new = np.array([1.0, (xHe0 - 1.0) / fHe, Tcmb * (1.0 + zend), 0.0, 0.0, -Tcmb * (1.0 + zend)])
         elif i > 0 and y_prev[0] > 0.99:
             rhs = math.exp(1.5 * math.log(CR * Tcmb / (1.0 + zend)) - CB1 / (Tcmb * (1.0 + zend))) / Nnow
-            xH0 = 0.5 * (math.sqrt(rhs**2 + 4.0 * rhs) - rhs)
+            xH0 = quad_root(rhs, rhs)
             new = solve_ionization(astart, aend, y_prev, param, aH_of, rtol, atol, stage_times=stage_times)
             new[0] = xH0
             new[3] = 0.0

@@ -83,17 +83,42 @@ def blob_len(num_thermo: int, nqmax: int) -> int:
 
 
 _static = {}
+# GRK4A step ends recorded per RECFAST sample for the frozen form (the
+# histories at rtol 1e-3 take a few per sample)
+STEP_CAP_PER_SAMPLE = 16
+
+
+def _leader_array(leader, nset):
+    """Checked leader indices (-1: adaptive; j: follow set j's steps)."""
+    ld = np.ascontiguousarray(np.asarray(leader, dtype=np.int32))
+    if ld.shape != (nset,):
+        raise ValueError(f"leader must have one entry per set ({nset}), got shape {ld.shape}")
+    fol = ld >= 0
+    if (ld < -1).any() or (ld[fol] >= nset).any() or (ld[ld[fol]] >= 0).any():
+        raise ValueError("a leader must be -1 or the index of a set whose own leader is -1")
+    return ld
+
+
+def follow_nominal(ncosmo: int, nper: int):
+    """Leader indices for the layout [ncosmo nominal sets, then nper
+    perturbed sets per cosmology]: the nominal sets adaptive, each perturbed
+    set on its cosmology's nominal step sequence."""
+    return np.concatenate([np.full(ncosmo, -1, np.int32), np.repeat(np.arange(ncosmo, dtype=np.int32), nper)])
 
 
 def evolve_background_tables(params, nqmax: int, *, num_thermo: int = 256, aexp_out=None, rtol: float = 1e-3,
-                             atol: float = 1e-6, max_steps: int = 128, stream=None, out=None, tau_out=None):
+                             atol: float = 1e-6, max_steps: int = 128, stream=None, out=None, tau_out=None,
+                             leader=None):
     """Table blobs of every parameter set on the current CUDA device.
 
     ``params``: list of dicts with the keys ``evolve_background`` reads.
     Returns ``(tables [nset, blob_len], tau [nset, nout] or None, status
     [nset])`` as torch tensors on the device (stream-ordered, no host sync);
     ``out`` / ``tau_out`` may pass preallocated buffers.  A nonzero status
-    means an interval of the ionisation history used up its step budget.
+    (``DEB_BG_*`` bits) means an interval of the ionisation history used up
+    its step budget or a frozen step record was incomplete.  ``leader`` (one
+    int per set, see :func:`follow_nominal`) puts sets on the recorded step
+    sequence of another set (``deb_evolve_background_frozen``).
     """
     import torch
 
@@ -115,8 +140,17 @@ def evolve_background_tables(params, nqmax: int, *, num_thermo: int = 256, aexp_
     cfg = DebBgCfg(num_thermo, NUM_NU, NQ_BG, nqmax, max_steps, AMIN, rtol, atol)
     c = lambda t: ctypes.c_void_p(t.data_ptr())
     with torch.cuda.stream(s):
-        _native.check(L.deb_evolve_background(ctypes.byref(cfg), c(pm), nset, c(consts), c(grd), c(tabs), bl, c(status),
-                                              ctypes.c_void_p(s.cuda_stream)), "deb_evolve_background")
+        if leader is None:
+            _native.check(L.deb_evolve_background(ctypes.byref(cfg), c(pm), nset, c(consts), c(grd), c(tabs), bl,
+                                                  c(status), ctypes.c_void_p(s.cuda_stream)), "deb_evolve_background")
+        else:
+            ld = torch.as_tensor(_leader_array(leader, nset)).to(dev, non_blocking=True)
+            cap = STEP_CAP_PER_SAMPLE * num_thermo
+            steps = torch.empty((nset, 3 * num_thermo + 1 + 2 * cap), dtype=torch.float64, device=dev)
+            _native.check(L.deb_evolve_background_frozen(ctypes.byref(cfg), c(pm), nset, c(ld), c(consts), c(grd),
+                                                         c(steps), cap, c(tabs), bl, c(status),
+                                                         ctypes.c_void_p(s.cuda_stream)),
+                          "deb_evolve_background_frozen")
         tau = None
         if aexp_out is not None:
             aexp = torch.as_tensor(np.atleast_1d(np.asarray(aexp_out, dtype=np.float64))).to(dev)
@@ -127,11 +161,16 @@ def evolve_background_tables(params, nqmax: int, *, num_thermo: int = 256, aexp_
 
 
 def evolve_background_tables_host(params, nqmax: int, *, num_thermo: int = 256, rtol: float = 1e-3,
-                                  atol: float = 1e-6, max_steps: int = 128, nthreads: int = 0, out=None):
+                                  atol: float = 1e-6, max_steps: int = 128, nthreads: int = 0, out=None,
+                                  leader=None, steps=None):
     """The same producer on the host cores (``deb_evolve_background_host``):
     ``[nset, blob_len]`` numpy blobs (written into ``out``, e.g. pinned
     memory, when given) and the status per set.  One CPU core builds a set
-    in a few milliseconds; worker threads split the sets."""
+    in a few milliseconds; worker threads split the sets.  ``leader`` as in
+    :func:`evolve_background_tables` (``deb_evolve_background_frozen_host``);
+    ``steps``, a float64 array ``[nset, 3 num_thermo + 1 + 2 cap]``,
+    receives the leaders' step records (layout of
+    ``deb_evolve_background_frozen``)."""
     L = _native.load()
     pm = np.ascontiguousarray(param_matrix(params))
     nset = pm.shape[0]
@@ -146,8 +185,20 @@ def evolve_background_tables_host(params, nqmax: int, *, num_thermo: int = 256, 
     status = np.zeros(nset, dtype=np.int32)
     cfg = DebBgCfg(num_thermo, NUM_NU, NQ_BG, nqmax, max_steps, AMIN, rtol, atol)
     p = lambda a: ctypes.c_void_p(a.ctypes.data)
-    _native.check(L.deb_evolve_background_host(ctypes.byref(cfg), p(pm), nset, p(consts), p(grd), p(tabs), bl,
-                                               p(status), int(nthreads)), "deb_evolve_background_host")
+    if leader is None:
+        _native.check(L.deb_evolve_background_host(ctypes.byref(cfg), p(pm), nset, p(consts), p(grd), p(tabs), bl,
+                                                   p(status), int(nthreads)), "deb_evolve_background_host")
+    else:
+        ld = _leader_array(leader, nset)
+        cap = 0
+        if steps is not None:
+            if steps.dtype != np.float64 or steps.ndim != 2 or steps.shape[0] != nset or not steps.flags.c_contiguous:
+                raise ValueError("steps must be a C-contiguous float64 array [nset, 3 num_thermo + 1 + 2 cap]")
+            cap = (steps.shape[1] - 3 * num_thermo - 1) // 2
+        _native.check(L.deb_evolve_background_frozen_host(ctypes.byref(cfg), p(pm), nset, p(ld), p(consts), p(grd),
+                                                          p(steps) if steps is not None else None, cap, p(tabs),
+                                                          bl, p(status), int(nthreads)),
+                      "deb_evolve_background_frozen_host")
     return tabs, status
 
 

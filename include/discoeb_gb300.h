@@ -358,8 +358,14 @@ int deb_forward_static(const deb_dims* dims, const double* d_tables, int ncosmo,
  *            q[nqmax], w[nqmax] (the perturbations' momentum bins),
  *            a_thermo[num_thermo + 1] (RECFAST sampling), log a_thermo[1:]
  *   d_tables [nset, blob_len] output blobs, blob_len = deb_tables_blob_len()
- *   d_status [nset] (may be NULL): 1 if an interval's step budget ran out
+ *   d_status [nset] (may be NULL): DEB_BG_* bits, 0 = ok
  */
+enum deb_bg_status {
+  DEB_BG_STEPS = 1,        /* an interval's step budget ran out (or a replayed step gave NaN) */
+  DEB_BG_UNRECORDED = 2,   /* frozen form: the leader's step record overflowed step_cap; the
+                              intervals past it ran adaptive */
+  DEB_BG_BAD_LEADER = 4    /* frozen form: leader index out of range or itself a follower; ran adaptive */
+};
 enum deb_bg_param {
   DEB_BG_OMEGAM = 0, DEB_BG_OMEGAB, DEB_BG_H0, DEB_BG_TCMB, DEB_BG_YHE, DEB_BG_NEFF, DEB_BG_NMNU, DEB_BG_MNU,
   DEB_BG_W0, DEB_BG_WA, DEB_BG_CS2DE, DEB_BG_AS, DEB_BG_NS, DEB_BG_KP, DEB_BG_OMEGAK, DEB_BG_NPARAM
@@ -395,6 +401,37 @@ int deb_evolve_background(const deb_bg_cfg* cfg, const double* d_params, int nse
    hundred sets this is the faster producer. */
 int deb_evolve_background_host(const deb_bg_cfg* cfg, const double* params, int nset, const double* consts,
                                const double* grid, double* tables, int blob_len, int* status, int nthreads);
+/*
+ * Frozen step sequences for difference quotients over parameter sets.  Set
+ * s with leader[s] = -1 integrates its ionisation history adaptively and
+ * records every accepted GRK4A step end, the case of the thermal history it
+ * took in each interval and the branches of every RHS evaluation; a set with
+ * leader[s] = j >= 0 (j a set with leader[j] = -1) takes set j's cases,
+ * steps and branches instead, all steps accepted,
+ * so that its tables are a smooth function of its parameters near set j's:
+ * the derivative the reference's jax.jacfwd takes through its RECFAST
+ * diffeqsolve (thermodynamics_recfast.py:283-298, forward mode through the
+ * nominal step sequence and the branches the nominal values select).  Sets
+ * with leader -1 give the same blobs as deb_evolve_background.
+ *
+ *   d_leader [nset]                                    device ints
+ *   d_steps  [nset, 3 num_thermo + 1 + 2 step_cap]     scratch: per leader
+ *            the first step of each interval, the case of each interval, the
+ *            branch word of its closing RHS evaluation, then an (end, branch
+ *            word) pair per step, all as doubles; follower rows are unused.
+ *            step_cap = 16 num_thermo is ample at rtol 1e-3
+ *            (DEB_BG_UNRECORDED reports an overflow).
+ *
+ * Two launches on `stream`: the leaders, then the followers.
+ */
+int deb_evolve_background_frozen(const deb_bg_cfg* cfg, const double* d_params, int nset, const int* d_leader,
+                                 const double* d_consts, const double* d_grid, double* d_steps, int step_cap,
+                                 double* d_tables, int blob_len, int* d_status, void* stream);
+/* The frozen form on the host cores: HOST buffers; steps may be NULL (the
+   library then keeps step_cap = 16 num_thermo per set itself). */
+int deb_evolve_background_frozen_host(const deb_bg_cfg* cfg, const double* params, int nset, const int* leader,
+                                      const double* consts, const double* grid, double* steps, int step_cap,
+                                      double* tables, int blob_len, int* status, int nthreads);
 /* tau_of_a (perturbations.py:975) of each blob at nout scale factors: d_tau [nset, nout] */
 int deb_tau_of_a(const double* d_tables, int nset, int blob_len, const double* d_aexp, int nout, double* d_tau,
                  void* stream);

@@ -36,8 +36,9 @@ def sets():
     base = fiducial_mnu_param()
     pert = perturbed_params(base)
     flat = [base] + [q for (_, _, a, b) in pert for q in (a, b)]
-    tabs3, _ = tables_gpu.evolve_background_tables_host(flat, 3)
-    tabs15, _ = tables_gpu.evolve_background_tables_host(flat, 15)
+    lead = tables_gpu.follow_nominal(1, len(flat) - 1)
+    tabs3, _ = tables_gpu.evolve_background_tables_host(flat, 3, leader=lead)
+    tabs15, _ = tables_gpu.evolve_background_tables_host(flat, 15, leader=lead)
     eps = np.array([e for (_, e, _, _) in pert])
     return tabs3, tabs15, eps
 

@@ -5,13 +5,15 @@
   solve (1e-8 of each parameter's largest |d ln P / d theta|);
 * against the GPU's own replay of the recorded steps on the theta +- eps
   tables (central differences of the same frozen-step map, the derivative
-  jax.jacfwd takes through diffrax at perturbations.py:765): 1e-6 of each
-  parameter's largest derivative against the quotients of eps = 1e-4 or
-  1e-5 theta (an output time within eps of a recorded step end puts a kink
-  in the replayed map that one quotient straddles) -- on the small hierarchy
-  at one and at eight outputs, and at nvar 323 with 128 k and 8 outputs
-  (steps landing on the outputs), the gradient workload of the fiducial
-  cosmology;
+  jax.jacfwd takes through diffrax at perturbations.py:765), each side on
+  the same tables, at eps = 1e-4 and 1e-5 theta: 1e-6 of each parameter's
+  largest derivative at either eps (an output time within eps of a recorded
+  step end puts a kink in the replayed map that one quotient straddles) --
+  on the small hierarchy at one and at eight outputs, and at nvar 323 with
+  128 k and 8 outputs (steps landing on the outputs), the gradient workload
+  of the fiducial cosmology.  The tables of the theta +- eps sets follow
+  the nominal set's RECFAST steps and branches, so the adjoints of the two
+  eps agree with each other to ~1e-8;
 * the checkpoint count does not change the result (8 vs 1024 slots);
 * PowerSpectrum.backward (one adjoint sweep with grad_P) against the
   contraction of the replay's Jacobian.
@@ -38,32 +40,34 @@ def base():
 
 
 def _both(base, k, a_out, dims, ck_cap=32, **kw):
-    """Adjoint, and the replay's quotients at eps = 1e-4 and 1e-5 theta."""
-    pert = [perturbed_params(base)]
-    ga = GradientProblem([base], "native", pert, k, a_out, method="adjoint", ck_cap=ck_cap, **kw, **dims)
-    _, Da = ga.run()
-    ga.check()
-    Dr = []
+    """[(adjoint, replay quotients)] on the tables of eps = 1e-4 and 1e-5 theta."""
+    pairs, ga0 = [], None
     for rs in (1e-4, 1e-5):
-        gr = GradientProblem([base], "native", [perturbed_params(base, rel_step=rs)], k, a_out, method="replay", **kw,
-                             **dims)
-        _, D = gr.run()
+        pert = [perturbed_params(base, rel_step=rs)]
+        ga = GradientProblem([base], "native", pert, k, a_out, method="adjoint", ck_cap=ck_cap, **kw, **dims)
+        _, Da = ga.run()
+        ga.check()
+        gr = GradientProblem([base], "native", pert, k, a_out, method="replay", **kw, **dims)
+        _, Dr = gr.run()
         gr.check()
-        Dr.append(D.cpu().numpy())
-    return ga, Da.cpu().numpy(), Dr
+        pairs.append((Da.cpu().numpy(), Dr.cpu().numpy()))
+        ga0 = ga0 or ga
+    return ga0, pairs[0][0], pairs
 
 
-def _close(Da, Dr, bar):
-    """Within bar of each parameter's largest derivative, against the replay's
-    quotients at either eps: where a recorded step end and an output time lie
-    within eps of each other the replayed map has a kink (their order flips
-    between the theta +- eps sets) and one quotient straddles it; a wrong
-    adjoint would miss both."""
-    Dr = Dr if isinstance(Dr, list) else [Dr]
+def _close(pairs, bar):
+    """Within bar of each parameter's largest derivative at either eps: where a
+    recorded step end and an output time lie within eps of each other the
+    replayed map has a kink (their order flips between the theta +- eps sets)
+    and one quotient straddles it; a wrong adjoint would miss both."""
     for j, name in enumerate(THETA):
-        scale = np.abs(Dr[0][..., j]).max()
-        err = np.min([np.abs(Da[..., j] - D[..., j]) for D in Dr], axis=0)
+        scale = np.abs(pairs[0][1][..., j]).max()
+        err = np.min([np.abs(Da[..., j] - Dr[..., j]) for Da, Dr in pairs], axis=0)
         assert err.max() <= bar * scale, (name, err.max() / scale)
+    # the adjoint itself does not depend on eps beyond the quotients of the tables
+    for j, name in enumerate(THETA if len(pairs) > 1 else ()):
+        scale = np.abs(pairs[0][0][..., j]).max()
+        assert np.abs(pairs[0][0][..., j] - pairs[1][0][..., j]).max() <= bar * scale, name
 
 
 @pytest.mark.parametrize("a_out,step_ts", [([1.0], False), (list(np.linspace(0.2, 1.0, 8)), True)])
@@ -76,8 +80,8 @@ def test_adjoint_matches_replay_differences(base, a_out, step_ts):
     agrees with the quotients of eps = 1e-5 there.  Those outputs are
     compared against the host build of the adjoint below.)"""
     k = np.geomspace(1e-3, 1.0, 6)
-    _, Da, Dr = _both(base, k, a_out, DIMS, rtol=1e-6, atol=1e-9, max_steps=20000, step_to_outputs=step_ts)
-    _close(Da, Dr, 1e-6)
+    _, _, pairs = _both(base, k, a_out, DIMS, rtol=1e-6, atol=1e-9, max_steps=20000, step_to_outputs=step_ts)
+    _close(pairs, 1e-6)
 
 
 def test_adjoint_matches_host_build_of_the_same_code(base):
@@ -88,7 +92,7 @@ def test_adjoint_matches_host_build_of_the_same_code(base):
     ga, Da, _ = _both(base, k, a_out, DIMS, **kw)
     pert = perturbed_params(base)
     sets = [base] + [q for (_, _, a, b) in pert for q in (a, b)]
-    tabs, _ = tables_gpu.evolve_background_tables_host(sets, 3)
+    tabs, _ = tables_gpu.evolve_background_tables_host(sets, 3, leader=tables_gpu.follow_nominal(1, len(sets) - 1))
     eps = np.array([e for (_, e, _, _) in pert])
     taus = tb.tau_of_a_blob(tabs, a_out)
     y0 = ga.d_y0.cpu().numpy()
@@ -115,7 +119,7 @@ def test_checkpoint_count_does_not_change_the_gradient(base):
         gp.check()
         out.append((D.cpu().numpy(), gp.d_ckstride.cpu().numpy()))
     assert out[0][1].max() > 1 and out[1][1].max() == 1
-    _close(out[0][0], out[1][0], 1e-9)
+    _close([(out[0][0], out[1][0])], 1e-9)
 
 
 def test_adjoint_at_the_fiducial_gradient_workload(base):
@@ -123,9 +127,9 @@ def test_adjoint_at_the_fiducial_gradient_workload(base):
     on the outputs, rtol 1e-5: the cosmology and sizes of the gradient
     workload, adjoint (8 seeds per mode) against the replay."""
     k = np.geomspace(1e-3, 1.0, 128)
-    ga, Da, Dr = _both(base, k, list(np.linspace(0.2, 1.0, 8)), FID, rtol=1e-5, atol=1e-5, max_steps=20000,
-                       step_to_outputs=True)
-    _close(Da, Dr, 1e-6)
+    _, _, pairs = _both(base, k, list(np.linspace(0.2, 1.0, 8)), FID, rtol=1e-5, atol=1e-5, max_steps=20000,
+                        step_to_outputs=True)
+    _close(pairs, 1e-6)
 
 
 def test_power_spectrum_backward_is_one_adjoint_sweep(base):
