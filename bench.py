@@ -1063,7 +1063,9 @@ def run_reference(args):
            "data": "synthetic (seeded cosmology sample, the same tables as the GPU arm's cosmology 0)",
            "config": (loglike_config(args, inp) if inp.get("objective") == "loglike" else
                       {"workload": args.workload, "ncosmo_per_gpu": inp["ncosmo"], "num_k": inp["num_k"]}),
-           "cpu_baseline": {"value": v, "unit": unit, "cores": threads, "kind": "port", "sample": sample},
+           "cpu_baseline": {"value": v, "unit": unit, "cores": threads, "kind": "port", "sample": sample,
+                            "extrapolated": "steps/s measured on the sample, scaled by the counted work of one "
+                                            "cosmology solve"},
            "cpu_structured": cm["structured"],
            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "note": "the reference's JAX path is not installable offline; the oracle (a CPU restatement of its "

@@ -90,7 +90,7 @@ def perturbed_params(cosmo, theta=THETA, rel_step=1e-4):
 
 
 TABLE_NAMES = ("tab0", "tau0", "tabs", "taus")
-SMALL_NAMES = ("k", "com", "eps", "inv_As", "lnk")
+SMALL_NAMES = ("k", "com", "eps", "eps_c", "inv_As", "lnk")
 
 
 def _host_inputs(plist, backgrounds, pert, kmodes, aexp_out, nqmax):
@@ -104,6 +104,7 @@ def _host_inputs(plist, backgrounds, pert, kmodes, aexp_out, nqmax):
     k = np.tile(kmodes, nc)
     h = dict(k=k, com=com,
              eps=np.ascontiguousarray(np.array([[e for (_, e, _, _) in pp] for pp in pert], dtype=np.float64)[com].T),
+             eps_c=np.array([[e for (_, e, _, _) in pp] for pp in pert], dtype=np.float64),
              inv_As=(1.0 / As)[:, None], lnk=np.log(k / kp)[:, None])
     if _native_tables(backgrounds):
         from . import tables_gpu
@@ -274,7 +275,7 @@ class GradientProblem:
             self.d_gy = torch.zeros((nsd, nm, no, 20), dtype=torch.float64, device=dev)
             self.d_gth = torch.empty((nsd, nm, self.npar), dtype=torch.float64, device=dev)
             self.d_ast = torch.empty((nsd * nm,), dtype=torch.int32, device=dev)
-            self.eps_c = torch.as_tensor(np.array([[e for (_, e, _, _) in pp] for pp in pert], dtype=np.float64)).to(dev)
+            self.eps_c = self._dev["eps_c"]     # [ncosmo, npar], reloaded by load()
             self.adj_plan = adjoint_plan(self.dims, nsd * nm, seg_cap_for(max_steps, self.ck_cap))
 
     def load(self, plist, backgrounds, pert, stream=None):

@@ -56,7 +56,7 @@ def test_every_launch_shape_gives_identical_results(two_cosmologies):
             ref = y
         else:
             np.testing.assert_array_equal(y, ref)
-    assert seen == {"shared", "global"}
+    assert seen == {"shared", "global", "all_global"}
 
 
 def test_tune_keeps_the_fastest_measured_shape(two_cosmologies):

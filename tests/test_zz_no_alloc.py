@@ -78,8 +78,15 @@ def _static_vs_planned(param, lm, k, a_out, rtol, return_full=False, step_to_out
     p = bg.evolve_background(param=param)
     blob = tb.pack_cosmology(p, lm["nqmax"])
     tau = tb.tau_of_a(p, a_out)
-    ref = pt.solve(blob[None], k, tau[None], rtol=rtol, atol=rtol, max_steps=max_steps, exec_mode="warp",
-                   return_full=return_full, step_to_outputs=step_to_outputs, **lm)
+    cfg = pt._cfg(rtol, rtol, 0.25, 0.80, 0.0, 20.0, 0.3, max_steps, step_to_outputs=step_to_outputs)
+    # the planned launch in the static entry's shape (every per-mode vector in
+    # global memory): the same instructions, so the same accept / reject
+    # decisions at any tolerance
+    prob = pt.DeviceProblem(blob[None], k, tau[None], exec_mode="warp", return_full=return_full, **lm)
+    prob.plan = pt.get_plan(prob.dims, prob.nmode, ("all_global", 8))
+    prob.launch(cfg)
+    ref = prob.y.cpu().numpy()
+    assert (prob.status.cpu().numpy() == 0).all()
     L = _native.load()
     dev = torch.device("cuda", 0)
     d_tab = torch.as_tensor(blob[None]).to(dev)
@@ -90,7 +97,6 @@ def _static_vs_planned(param, lm, k, a_out, rtol, return_full=False, step_to_out
     d_st = torch.empty(k.size, dtype=torch.int32, device=dev)
     d_steps = torch.empty((k.size, 2), dtype=torch.int32, device=dev)
     dims = pt._dims(nout=len(a_out), return_full=return_full, linear_solver="structured", **lm)
-    cfg = pt._cfg(rtol, rtol, 0.25, 0.80, 0.0, 20.0, 0.3, max_steps, step_to_outputs=step_to_outputs)
     stream = torch.cuda.current_stream()
     for _ in range(2):
         d_y.fill_(0.0)
@@ -101,7 +107,9 @@ def _static_vs_planned(param, lm, k, a_out, rtol, return_full=False, step_to_out
         torch.cuda.synchronize()
         assert (d_st.cpu().numpy() == 0).all()
         y = d_y.cpu().numpy()
-        np.testing.assert_allclose(y, ref, rtol=1e-6, atol=1e-9 * np.abs(ref).max(axis=(0, 1), keepdims=True))
+        scale = np.abs(ref).max(axis=(0, 1), keepdims=True)
+        bad = np.abs(y - ref) > 1e-6 * np.abs(ref) + 1e-9 * scale
+        assert not bad.any(), (int(bad.sum()), np.argwhere(bad)[:5].tolist())
 
 
 def test_static_entry_point_with_more_modes_than_array_slots():
