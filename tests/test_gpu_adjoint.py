@@ -72,7 +72,11 @@ def _both(base, k, a_out, dims, ck_cap=32, **kw):
         gr = GradientProblem([base], "native", pert, k, a_out, method="replay", **kw, **dims)
         _, Dr = gr.run()
         gr.check()
-        np.testing.assert_array_equal(ga.d_rec.cpu().numpy(), gr.d_rec.cpu().numpy())
+        n_a, n_r = ga.d_nrec.cpu().numpy(), gr.d_nrec.cpu().numpy()
+        np.testing.assert_array_equal(n_a, n_r)
+        ra, rr = ga.d_rec.cpu().numpy(), gr.d_rec.cpu().numpy()
+        for m, n in enumerate(n_a):
+            np.testing.assert_array_equal(ra[m, :n], rr[m, :n])
         eps = np.full(len(THETA), np.inf)
         for (name, e, _, _) in pert[0]:
             eps[THETA.index(name)] = e
@@ -100,12 +104,15 @@ def _close(pairs, bar, lnp_round=4e-12):
             assert np.abs(pairs[0][0][..., j] - pairs[1][0][..., j]).max() <= bar * scale, name
 
 
-@pytest.mark.parametrize("a_out,step_ts", [([1.0], False), (list(np.linspace(0.2, 1.0, 8)), True),
-                                           ([0.35, 0.5, 0.75, 1.0], False)])
-def test_adjoint_matches_replay_differences(base, a_out, step_ts):
+@pytest.mark.parametrize("a_out,step_ts,kmax", [([1.0], False, 1.0), (list(np.linspace(0.2, 1.0, 8)), True, 1.0),
+                                                ([0.35, 0.5, 0.75, 1.0], False, 0.03)])
+def test_adjoint_matches_replay_differences(base, a_out, step_ts, kmax):
     """Outputs at the end time, at step ends (steps land on them) and
-    interpolated inside steps (the reference's SaveAt semantics)."""
-    k = np.geomspace(1e-3, 1.0, 6)
+    interpolated inside steps (the reference's SaveAt semantics; there the
+    replay's quotient straddles a kink wherever an output time lies near a
+    step end, which above k ~ 0.1 -- steps of 3e-4 tau -- is nearly every
+    output, so that case stops at k = 0.03)."""
+    k = np.geomspace(1e-3, kmax, 6)
     pairs = _both(base, k, a_out, DIMS, rtol=1e-6, atol=1e-9, max_steps=20000, step_to_outputs=step_ts)
     _close(pairs, 1e-6)
 
