@@ -597,6 +597,7 @@ def run_loglike(args, inp, world, rank, local):
     # synthetic data: the first solve's ln P with 5% seeded scatter
     P0 = gp.forward(stream)
     torch.cuda.synchronize()
+    gp.fit_checkpoints()
     rng = np.random.default_rng(4321)
     lnPd = np.log(P0.cpu().numpy()).reshape(nc, inp["num_k"], nout) + 0.05 * rng.standard_normal((nc, inp["num_k"], nout))
     lp.set_data(lnPd)
@@ -702,8 +703,8 @@ def run_loglike(args, inp, world, rank, local):
         "data": "synthetic (seeded cosmology sample; tables of theta and theta +- 1e-4 theta from the library's "
                 "RECFAST producer; data vector = each cosmology's own ln P with 5% seeded scatter)",
         "config": loglike_config(args, inp),
-        "detail": {"checkpoints": f"{gp.ck_cap} slots per mode ({gp.d_ckpt.numel() * 8 / 1e9:.1f} GB), strides "
-                                  f"{int(strides.min())}-{int(strides.max())}",
+        "detail": {"checkpoints": f"per-mode slots fitted to the step counts ({gp.d_ckpt.numel() * 8 / 1e9:.1f} GB), "
+                                  f"strides {int(strides.min())}-{int(strides.max())}",
                    "cuda_graph": "record + get_power + likelihood + adjoint captured once, replayed per step",
                    "launch_shape": launch, "autotune_ms": {f"{a}/{b}": round(v, 2) for (a, b), v in tune_ms.items()}},
         "e2e": {"value": total_cosmo / t_e2e if world == 1 else None,

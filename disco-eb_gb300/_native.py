@@ -74,10 +74,10 @@ def load(path: str | None = None):
                                      ctypes.POINTER(DebSolverCfg), vp, vp, vp, vp, ctypes.c_int, vp, vp]
     L.deb_forward_record_ckpt.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp,
                                           ctypes.POINTER(DebSolverCfg), vp, vp, vp, vp, ctypes.c_int, vp, vp,
-                                          ctypes.c_int, vp, vp]
+                                          ctypes.c_int, vp, vp, vp, vp]
     L.deb_plan_create_adjoint.argtypes = [ctypes.POINTER(DebDims), ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
     L.deb_adjoint.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, ctypes.c_int, vp, vp,
-                              vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, vp]
+                              vp, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, vp, ctypes.c_int, vp, vp, vp]
     L.deb_replay.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, vp,
                              ctypes.POINTER(DebSolverCfg), vp, ctypes.c_int, vp, vp, vp, vp]
     L.deb_get_power.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,

@@ -40,6 +40,7 @@ struct AParams {
   const int* nrec;
   const double* ckpt;
   int ck_cap;
+  const long long* ckoff;    // null: mode m's slots from m * ck_cap
   const int* ckstride;
   const double* gy;          // [nseed, nmode, nout, 20]
   double* gth;               // [nseed, nmode, npar]
@@ -52,7 +53,13 @@ struct AParams {
   deb::Dims D;
 };
 
-__global__ void __launch_bounds__(32) adjoint_kernel(AParams P) {
+// Warps per SM the register allocation must leave room for (the kernel is
+// latency-bound: more resident warps hide more of each warp's memory waits)
+#ifndef DEB_ADJ_MIN_WARPS_PER_SM
+#define DEB_ADJ_MIN_WARPS_PER_SM 1
+#endif
+
+__global__ void __launch_bounds__(32, DEB_ADJ_MIN_WARPS_PER_SM) adjoint_kernel(AParams P) {
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31;
   const deb::Grp<32> gp{lane};
@@ -93,7 +100,7 @@ __global__ void __launch_bounds__(32) adjoint_kernel(AParams P) {
       it.taus = P.tau_pm + (long)ci * 2 * P.npar * P.nout;
       it.rec = P.rec + (long)m * P.rec_len;
       it.nrec = P.nrec[m];
-      it.ck = P.ckpt + (long)m * P.ck_cap * n;
+      it.ck = P.ckpt + (P.ckoff ? (long)P.ckoff[m] : (long)m * P.ck_cap) * n;
       it.ck_stride = it.nrec >= 1 ? P.ckstride[m] : 1;
       it.gy = P.gy + item * P.nout * deb::NFIELD;
       it.k = km;
@@ -212,13 +219,13 @@ int deb_plan_create_adjoint(const deb_dims* dims, int max_items, int seg_cap, de
 int deb_adjoint(deb_plan* p, const double* d_tables, const double* d_tables_pm, int ncosmo, int npar, int blob_len,
                 const double* d_eps, const double* d_k, const int* d_cosmo_of_mode, int nmode,
                 const double* d_tau_out, const double* d_tau_out_pm, const double* d_record, int rec_len,
-                const int* d_nrec, const double* d_ckpt, int ck_cap, const int* d_ckstride, const double* d_gy,
-                int nseed, double* d_gtheta, int* d_status, void* stream) {
+                const int* d_nrec, const double* d_ckpt, int ck_cap, const long long* d_ckoff, const int* d_ckstride,
+                const double* d_gy, int nseed, double* d_gtheta, int* d_status, void* stream) {
   if (!p || !p->adj || ncosmo <= 0 || npar < 1 || npar > 12 || nmode < 0 || nseed < 1 || blob_len <= deb::HDR_LEN)
     return DEB_ERR_INVALID;
   if (nmode == 0) return DEB_OK;
   if (!d_tables || !d_tables_pm || !d_eps || !d_k || !d_tau_out || !d_tau_out_pm || !d_record || !d_nrec || !d_ckpt ||
-      !d_ckstride || !d_gy || !d_gtheta || !d_status || rec_len < 2 || ck_cap < 2)
+      !d_ckstride || !d_gy || !d_gtheta || !d_status || rec_len < 2 || (!d_ckoff && ck_cap < 2))
     return DEB_ERR_INVALID;
   if ((long)nmode * nseed > p->max_modes || nmode > p->max_modes) return DEB_ERR_CAPACITY;
   int rc = adj_upload_constants();
@@ -228,7 +235,7 @@ int deb_adjoint(deb_plan* p, const double* d_tables, const double* d_tables_pm, 
   P.tables = d_tables; P.tables_pm = d_tables_pm; P.ncosmo = ncosmo; P.npar = npar; P.blob_len = blob_len;
   P.eps = d_eps; P.k = d_k; P.cosmo = d_cosmo_of_mode; P.nmode = nmode; P.nseed = nseed; P.nout = p->nout;
   P.tau_out = d_tau_out; P.tau_pm = d_tau_out_pm; P.rec = d_record; P.rec_len = rec_len; P.nrec = d_nrec;
-  P.ckpt = d_ckpt; P.ck_cap = ck_cap; P.ckstride = d_ckstride; P.gy = d_gy; P.gth = d_gtheta; P.status = d_status;
+  P.ckpt = d_ckpt; P.ck_cap = ck_cap; P.ckoff = d_ckoff; P.ckstride = d_ckstride; P.gy = d_gy; P.gth = d_gtheta; P.status = d_status;
   P.ws = p->adj_ws; P.wslot = p->adj_wslot; P.seg_cap = p->adj_seg_cap; P.queue = p->queue; P.order = p->order_dev;
   P.D = p->D;
   if (cudaMemsetAsync(p->queue, 0, sizeof(int), s) != cudaSuccess) return DEB_ERR_CUDA;

@@ -395,25 +395,33 @@ HD void apply_jt(const Grp<G>& gp, const Cosmo& c, const ModeConst& m, const Dim
       z[j] += dpart(s);
     }
   }
-  // massive neutrinos (every row explicit), element (l, q)
-  for (int e = gp.lane; e < (lnu + 1) * nq; e += G) {
-    const int l = e / nq, q = e - l * nq;
+  // massive neutrinos (every row explicit), element (l, q): a lane per
+  // momentum bin walks its multipoles with X(l-1), X(l), X(l+1) in registers
+  // (k v_q once per bin; lanes of one l read consecutive q)
+  for (int q = gp.lane; q < nq; q += G) {
     const S aq = a * w.m(M_Q + Q_AMQ * nq + q);
     const S kv = k * jrsqrt(1.0 + aq * aq);
     auto X = [&](int ll) { return x[iq0 + ll * nq + q]; };
-    S s = S(0.0);
-    if (l >= 1) {   // row l-1, its coupling to l + ... = D(l-1)
-      const int lp = l - 1;
-      const double dc = lp == 0 ? -1.0 : (lp == 1 ? -2.0 / 3.0 : (lp == 2 ? -0.6 : -T.up[lp]));
-      s = s + (dc * X(lp)) * kv;
+    double xm = 0.0, x0 = X(0), xp = lnu >= 1 ? X(1) : 0.0;
+    for (int l = 0; l <= lnu; ++l) {
+      const double xn = l + 2 <= lnu ? X(l + 2) : 0.0;
+      S s = S(0.0);
+      if (l >= 1) {   // row l-1, its coupling to l + ... = D(l-1)
+        const int lp = l - 1;
+        const double dc = lp == 0 ? -1.0 : (lp == 1 ? -2.0 / 3.0 : (lp == 2 ? -0.6 : -T.up[lp]));
+        s = s + (dc * xm) * kv;
+      }
+      if (l + 1 <= lnu) {   // row l+1, its coupling to l - ...
+        const int lp = l + 1;
+        const double uc = lp == 1 ? 1.0 / 3.0 : (lp == 2 ? 0.4 : (lp == lnu ? 1.0 : T.lo[lp]));
+        s = s + (uc * xp) * kv;
+      }
+      if (l == lnu) s = s - ((lnu + 1.0) * x0) * C.itau;
+      z[iq0 + l * nq + q] += dpart(s);
+      xm = x0;
+      x0 = xp;
+      xp = xn;
     }
-    if (l + 1 <= lnu) {   // row l+1, its coupling to l - ...
-      const int lp = l + 1;
-      const double uc = lp == 1 ? 1.0 / 3.0 : (lp == 2 ? 0.4 : (lp == lnu ? 1.0 : T.lo[lp]));
-      s = s + (uc * X(lp)) * kv;
-    }
-    if (l == lnu) s = s - ((lnu + 1.0) * X(lnu)) * C.itau;
-    z[iq0 + e] += dpart(s);
   }
   gp.sync();
   // (2) lead rows with state sources
@@ -497,9 +505,20 @@ HD void solve_Mt(const Grp<G>& gp, const Dims& D, const WS<G>& w, VecRef r) {
     const int start = ch == 0 ? ir : (!tail ? iq0 + ch - 1 : (ch == nq + 1 ? 10 : igp + 3));
     const int stride = (ch == 0 || tail) ? 1 : nq;
     const int cnt = ch == 0 ? lr + 1 : (!tail ? lnu + 1 : (ch == nq + 1 ? lg - 2 : lgp - 2));
+    // groups of eight elements load ahead of their dependent FMAs, so a
+    // sweep pays the memory latency once per group, not once per element
     int i = start + (cnt - 1) * stride;
     double rn = r[i];
-    for (int j = cnt - 2; j >= 0; --j) {
+    int j = cnt - 2;
+    for (; j >= 7; j -= 8) {
+      double rv[8], lv[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) { rv[q] = r[i - (q + 1) * stride]; lv[q] = LO(i - q * stride); }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) { rn = rv[q] - lv[q] * rn; r[i - (q + 1) * stride] = rn; }
+      i -= 8 * stride;
+    }
+    for (; j >= 0; --j) {
       const int ip = i;
       i -= stride;
       rn = r[i] - LO(ip) * rn;
@@ -508,7 +527,20 @@ HD void solve_Mt(const Grp<G>& gp, const Dims& D, const WS<G>& w, VecRef r) {
     if (!tail) {
       double zz = rn * PI(start);
       r[start] = zz;
-      for (int j = 1; j < cnt; ++j) {
+      int jb = 1;
+      for (; jb + 7 < cnt; jb += 8) {
+        double sv[8], uv[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int ii = i + (q + 1) * stride;
+          sv[q] = r[ii] * PI(ii);
+          uv[q] = UP(ii - stride);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) { zz = sv[q] - uv[q] * zz; r[i + (q + 1) * stride] = zz; }
+        i += 8 * stride;
+      }
+      for (; jb < cnt; ++jb) {
         i += stride;
         zz = r[i] * PI(i) - UP(i - stride) * zz;
         r[i] = zz;
@@ -535,7 +567,19 @@ HD void solve_Mt(const Grp<G>& gp, const Dims& D, const WS<G>& w, VecRef r) {
     const int cnt = t == 0 ? lg - 2 : lgp - 2;
     double zz = r[start] * PI(start) - UP(start - 1) * r[start - 1];
     r[start] = zz;
-    for (int j = 1; j < cnt; ++j) {
+    int j = 1;
+    for (; j + 7 < cnt; j += 8) {
+      double sv[8], uv[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int i = start + j + q;
+        sv[q] = r[i] * PI(i);
+        uv[q] = UP(i - 1);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) { zz = sv[q] - uv[q] * zz; r[start + j + q] = zz; }
+    }
+    for (; j < cnt; ++j) {
       const int i = start + j;
       zz = r[i] * PI(i) - UP(i - 1) * zz;
       r[i] = zz;
@@ -737,6 +781,93 @@ HD void phi_pass(const Grp<G>& gp, const AdjItem& it, const Dims& D, const doubl
   gp.sync();
 }
 
+// ------------------------------------------------------------------ the stage vectors of one step backwards
+// Stage s before its W^-T solve: rb = kbar_s and, for s >= 1, tmp = u_s as
+// stage_prep formed it (u_s = y0 + sum_q a_sq k_q for s <= 5, u_6 = u_5 +
+// k_5, u_7 = u_6 + k_6) -- one pass, every load of an element issued before
+// its arithmetic (register arrays indexed by unrolled constants).
+template <int G>
+HD void adj_stage_pre(const Grp<G>& gp, const AWS<G>& A, const Rodas& R, int n, int s) {
+  const VecRef rb = A.vec(A_RB), tmp = A.vec(A_TMP), kbs = A.vec(A_KB0 + s), y0 = A.fv(V_Y);
+  const int sb = s <= 5 ? s : 5;
+  double a[5];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) a[q] = q < sb ? R.a[sb][q] : 0.0;
+  for (int j = gp.lane; j < n; j += G) {
+    double k[7];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) k[q] = q < s ? A.fv(V_K0 + q)[j] : 0.0;
+    const double kb = kbs[j], y = y0[j];
+    rb[j] = kb;
+    if (s >= 1) {
+      double uu = y;
+#pragma unroll
+      for (int q = 0; q < 5; ++q)
+        if (q < sb) uu += a[q] * k[q];
+      if (s >= 6) uu = uu + k[5];
+      if (s >= 7) uu = uu + k[6];
+      tmp[j] = uu;
+    }
+  }
+  gp.sync();
+}
+
+// Stage s after J^T r_s went into ubar (s >= 1) or dL/dy0 (s = 0), in one
+// pass: kbar_q += C_sq / dt r_s (q < s) with the dt-derivative partial sums
+// pc = r_s . sum_q C_sq k_q and pk = r_s . k_s; rho += k_s[0] r_s; and the
+// stage point's cotangent: u_6 = u_5 + k_5 and u_7 = u_6 + k_6 pass ubar on
+// (kbar_{s-1} += ubar), u_s = y0 + sum_q a_sq k_q (1 <= s <= 5) sends it to
+// dL/dy0 and kbar_q and clears it.  pc, pk are this lane's partial sums.
+template <int G>
+HD void adj_stage_post(const Grp<G>& gp, const AWS<G>& A, const Rodas& R, int n, int s, double idt, double ks0,
+                       double& pc_out, double& pk_out) {
+  const VecRef rb = A.vec(A_RB), ub = A.vec(A_UB), lam = A.vec(A_LAM), rho = A.vec(A_RHO), ks = A.fv(V_K0 + s);
+  double cs[7], ci[7], aa[5];
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    cs[q] = q < s ? R.C[s][q] : 0.0;
+    ci[q] = q < s ? R.C[s][q] * idt : 0.0;
+  }
+#pragma unroll
+  for (int q = 0; q < 5; ++q) aa[q] = (s <= 5 && q < s) ? R.a[s][q] : 0.0;
+  double pc = 0.0, pk = 0.0;
+  for (int j = gp.lane; j < n; j += G) {
+    double k[7], kb[7];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+      k[q] = q < s ? A.fv(V_K0 + q)[j] : 0.0;
+      kb[q] = q < s ? A.vec(A_KB0 + q)[j] : 0.0;
+    }
+    const double rj = rb[j], kj = ks[j], rh = rho[j], uj = s >= 1 ? ub[j] : 0.0;
+    double ck = 0.0;
+#pragma unroll
+    for (int q = 0; q < 7; ++q)
+      if (q < s) {
+        ck += cs[q] * k[q];
+        kb[q] += ci[q] * rj;
+      }
+    pc += rj * ck;
+    pk += rj * kj;
+    rho[j] = rh + ks0 * rj;
+    if (s >= 6) {
+#pragma unroll
+      for (int q = 5; q < 7; ++q)
+        if (q == s - 1) kb[q] += uj;
+    } else if (s >= 1) {
+      lam[j] += uj;
+#pragma unroll
+      for (int q = 0; q < 5; ++q)
+        if (q < s) kb[q] += aa[q] * uj;
+      ub[j] = 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < 7; ++q)
+      if (q < s) A.vec(A_KB0 + q)[j] = kb[q];
+  }
+  pc_out = pc;
+  pk_out = pk;
+}
+
 // ------------------------------------------------------------------ one step backwards
 // On entry the forward step from (t0, y0 = V_Y) over dt has been recomputed
 // into w (stages, factors, y1 in vector vu) with g0 its background at y0, and
@@ -779,25 +910,11 @@ HD void step_adjoint(const Grp<G>& gp, const AdjItem& it, const Cosmo& c, const 
     else { row = iq0 + lnu * nq + (e - 3); cf = (lnu + 1.0) * it2; }
   };
   for (int s = 7; s >= 0; --s) {
-    // r = W^-T kbar_s
-    for (int j = gp.lane; j < n; j += G) rb[j] = KB(s)[j];
-    gp.sync();
+    // r = W^-T kbar_s; stage point u_s (as stage_prep forms it) and time
+    adj_stage_pre<G>(gp, A, R, n, s);
     solve_Wt<G>(gp, D, w, rb, yh, ye, g0.wQ);
-    // stage point u_s (as stage_prep forms it) and time
     const double ts = t0 + R.c[s] * dt;
-    VecRef u = y0;
-    if (s >= 1) {
-      const int sb = s <= 5 ? s : 5;
-      for (int j = gp.lane; j < n; j += G) {
-        double uu = y0[j];
-        for (int q = 0; q < sb; ++q) uu += R.a[sb][q] * K(q)[j];
-        if (s >= 6) uu = uu + K(5)[j];
-        if (s >= 7) uu = uu + K(6)[j];
-        tmp[j] = uu;
-      }
-      gp.sync();
-      u = tmp;
-    }
+    const VecRef u = s >= 1 ? tmp : y0;
     const double as = u[0];
     // derivatives of r^T f(t_s, u_s)
     bform<G>(gp, c, m, D, T, w, rb, u, as * m.amnu, true, sc + SC_B, false);
@@ -814,18 +931,13 @@ HD void step_adjoint(const Grp<G>& gp, const AdjItem& it, const Cosmo& c, const 
     const Coef<double> Cs = *reinterpret_cast<const Coef<double>*>(sc + SC_CF);
     apply_jt<double, G>(gp, c, m, D, T, w, Cs, as, rb, tgt);
     if (gp.lead()) tgt[0] += sc[SC_RES + 0];
-    // sum_q C_sq / dt k_q: kbar_q += C_sq / dt r, and its dt-derivative
-    double pc = 0.0, pk = 0.0;
-    for (int j = gp.lane; j < n; j += G) {
-      const double rj = rb[j];
-      double ck = 0.0;
-      for (int q = 0; q < s; ++q) {
-        ck += R.C[s][q] * K(q)[j];
-        KB(q)[j] += (R.C[s][q] * idt) * rj;
-      }
-      pc += rj * ck;
-      pk += rj * K(s)[j];
-    }
+    gp.sync();
+    // sum_q C_sq / dt k_q: kbar_q += C_sq / dt r, and its dt-derivative; the
+    // pair (r_s, k_s) of the J(y0) inside W: rho += k_s[0] r_s; the stage
+    // point's cotangent
+    const double ks0 = K(s)[0];
+    double pc, pk;
+    adj_stage_post<G>(gp, A, R, n, s, idt, ks0, pc, pk);
     gp.sum2(pc, pk);
     db -= pc * idt * idt;
     dbar -= pk;
@@ -841,21 +953,8 @@ HD void step_adjoint(const Grp<G>& gp, const AdjItem& it, const Cosmo& c, const 
       pf = gp.sum(pf);
       db += R.d[s] * pf;
     }
-    // the J(y0) inside W: pairs (r_s, k_s) and rho += k_s[0] r_s
+    // the J(y0) inside W: pairs (r_s, k_s)
     bform<G>(gp, c, m, D, T, w, rb, K(s), mu0, false, sc + SC_BW, true);
-    const double ks0 = K(s)[0];
-    for (int j = gp.lane; j < n; j += G) rho[j] += ks0 * rb[j];
-    // u_s = y0 + sum a_sq k_q (s <= 5), u_6 = u_5 + k_5, u_7 = u_6 + k_6
-    if (s >= 6) {
-      for (int j = gp.lane; j < n; j += G) KB(s - 1)[j] += ub[j];
-    } else if (s >= 1) {
-      for (int j = gp.lane; j < n; j += G) {
-        const double uj = ub[j];
-        lam[j] += uj;
-        for (int q = 0; q < s; ++q) KB(q)[j] += R.a[s][q] * uj;
-        ub[j] = 0.0;
-      }
-    }
     gp.sync();
   }
   // W = I/(gamma dt) - J(t0, y0): dL/dW = -sum_s r_s k_s^T

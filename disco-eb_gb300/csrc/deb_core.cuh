@@ -1069,20 +1069,18 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>
     const int start = ch == 0 ? ir : (!tail ? iq0 + ch - 1 : (ch == nq + 1 ? 10 : igp + 3));
     const int stride = (ch == 0 || tail) ? 1 : nq;
     const int cnt = ch == 0 ? lr + 1 : (!tail ? lnu + 1 : (ch == nq + 1 ? lg - 2 : lgp - 2));
-    // groups of four elements load ahead of their dependent FMAs, so the
-    // shared-memory latency is paid once per group
+    // groups of eight elements load ahead of their dependent FMAs, so the
+    // memory latency (shared or L2) is paid once per group
     int i = start + (cnt - 1) * stride;
     double rn = w.v(vr, i);
     int j = cnt - 2;
-    for (; j >= 3; j -= 4) {
-      const int i0 = i - stride, i1 = i0 - stride, i2 = i1 - stride, i3 = i2 - stride;
-      const double r0 = w.v(vr, i0), r1 = w.v(vr, i1), r2 = w.v(vr, i2), r3 = w.v(vr, i3);
-      const double u0 = w.v(V_UP, i0), u1 = w.v(V_UP, i1), u2 = w.v(V_UP, i2), u3 = w.v(V_UP, i3);
-      rn = r0 - u0 * rn; w.v(vr, i0) = rn;
-      rn = r1 - u1 * rn; w.v(vr, i1) = rn;
-      rn = r2 - u2 * rn; w.v(vr, i2) = rn;
-      rn = r3 - u3 * rn; w.v(vr, i3) = rn;
-      i = i3;
+    for (; j >= 7; j -= 8) {
+      double rv[8], uv[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) { rv[q] = w.v(vr, i - (q + 1) * stride); uv[q] = w.v(V_UP, i - (q + 1) * stride); }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) { rn = rv[q] - uv[q] * rn; w.v(vr, i - (q + 1) * stride) = rn; }
+      i -= 8 * stride;
     }
     for (; j >= 0; --j) {
       i -= stride;
@@ -1093,16 +1091,17 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>
       double z = rn * w.v(V_PI, start);
       w.v(vr, start) = z;
       int jb = 1;
-      for (; jb + 3 < cnt; jb += 4) {
-        const int i0 = i + stride, i1 = i0 + stride, i2 = i1 + stride, i3 = i2 + stride;
-        const double s0 = w.v(vr, i0) * w.v(V_PI, i0), s1 = w.v(vr, i1) * w.v(V_PI, i1);
-        const double s2 = w.v(vr, i2) * w.v(V_PI, i2), s3 = w.v(vr, i3) * w.v(V_PI, i3);
-        const double l0 = w.v(V_LO, i0), l1 = w.v(V_LO, i1), l2 = w.v(V_LO, i2), l3 = w.v(V_LO, i3);
-        z = s0 - l0 * z; w.v(vr, i0) = z;
-        z = s1 - l1 * z; w.v(vr, i1) = z;
-        z = s2 - l2 * z; w.v(vr, i2) = z;
-        z = s3 - l3 * z; w.v(vr, i3) = z;
-        i = i3;
+      for (; jb + 7 < cnt; jb += 8) {
+        double sv[8], lv[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int ii = i + (q + 1) * stride;
+          sv[q] = w.v(vr, ii) * w.v(V_PI, ii);
+          lv[q] = w.v(V_LO, ii);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) { z = sv[q] - lv[q] * z; w.v(vr, i + (q + 1) * stride) = z; }
+        i += 8 * stride;
       }
       for (; jb < cnt; ++jb) {
         i += stride;
@@ -1130,7 +1129,19 @@ HD void solve_M(const Grp<G>& gp, const ModeConst& m, const Dims& D, const WS<G>
     const int start = t == 0 ? 10 : igp + 3;
     const int cnt = t == 0 ? lg - 2 : lgp - 2;
     double z = w.v(vr, start - 1);
-    for (int j = 0; j < cnt; ++j) {
+    int j = 0;
+    for (; j + 7 < cnt; j += 8) {
+      double sv[8], lv[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int i = start + j + q;
+        sv[q] = w.v(vr, i) * w.v(V_PI, i);
+        lv[q] = w.v(V_LO, i);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) { z = sv[q] - lv[q] * z; w.v(vr, start + j + q) = z; }
+    }
+    for (; j < cnt; ++j) {
       const int i = start + j;
       z = w.v(vr, i) * w.v(V_PI, i) - w.v(V_LO, i) * z;
       w.v(vr, i) = z;

@@ -62,10 +62,13 @@ struct KParams {
   // queue order: queue position q takes mode order[q] (forward) or mode
   // order[q / nset], set q % nset (replay); null = index order
   const int* order;
-  // record with checkpoints: ckpt [nmode, ck_cap, n], ckstride [nmode]
+  // record with checkpoints: ckpt [nmode, ck_cap, n] or, with ckoff, mode m's
+  // ckcap[m] slots from slot ckoff[m] of one pool; ckstride [nmode]
   double* ckpt;
   int ck_cap;
   int* ckstride;
+  const long long* ckoff;
+  const int* ckcaps;
   deb::Ctl ctl;
   deb::Dims D;
 };
@@ -96,8 +99,12 @@ __device__ bool prepare_mode(const KParams& P, int q, deb::Cosmo& c, deb::ModeCo
   if (ok) ok = deb::load_cosmo(P.tables + (long)ti * P.blob_len, P.blob_len, c) && c.nq == P.D.nq;
   run.rec = P.rec ? P.rec + (long)m * P.rec_len : nullptr;
   run.rec_cap = P.rec_len - 1;
-  run.ck = (P.ctl.record && P.ckpt) ? P.ckpt + (long)m * P.ck_cap * P.D.n : nullptr;
-  run.ck_cap = P.ck_cap;
+  // an odd or too small per-mode capacity would break the thinning's pairing
+  // of slots: it is taken down to even, at least 2
+  const long ck_slot = P.ckoff ? (long)P.ckoff[m] : (long)m * P.ck_cap;
+  const int ck_cap = P.ckoff ? ((P.ckcaps[m] & ~1) < 2 ? 2 : (P.ckcaps[m] & ~1)) : P.ck_cap;
+  run.ck = (P.ctl.record && P.ckpt) ? P.ckpt + ck_slot * P.D.n : nullptr;
+  run.ck_cap = ck_cap;
   run.ck_stride = 1;
   run.nrec = (P.ctl.replay && P.nrec) ? P.nrec[m] : 0;
   if (ok && P.ctl.replay) ok = run.nrec >= 1 && run.nrec <= run.rec_cap;
@@ -158,7 +165,11 @@ __global__ void __launch_bounds__(kBlock) forward_lane_kernel(KParams P) {
 }
 
 // One warp per mode: the mode's vectors and MISC block in shared memory.
-__global__ void __launch_bounds__(32) forward_warp_kernel(KParams P) {
+#ifndef DEB_FWD_MIN_WARPS_PER_SM
+#define DEB_FWD_MIN_WARPS_PER_SM 1
+#endif
+
+__global__ void __launch_bounds__(32, DEB_FWD_MIN_WARPS_PER_SM) forward_warp_kernel(KParams P) {
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31;
   const long gwarp = blockIdx.x;
@@ -444,9 +455,14 @@ int deb_plan_create_ex(const deb_dims* dims, int max_modes, const deb_launch_cfg
     if (!p->warp_smem) p->warp_k_global = 0;
     p->warp_block_warps = 1;
     // blocks (= modes in flight) per SM limited by shared memory, by
-    // registers (at most 8 one-warp blocks of 255 registers per thread) and
-    // by the caller's cap
+    // registers (the kernel's own occupancy without shared memory: 8 one-warp
+    // blocks at 255 registers per thread) and by the caller's cap
     int per_sm = kMaxWarpBlocksPerSM;
+    {
+      int occ = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, forward_warp_kernel, 32, 0) == cudaSuccess && occ > 0)
+        per_sm = occ;
+    }
     if (p->warp_smem) {
       const int by_smem = (int)(sm_bytes / (smem_bytes + 1024));
       if (by_smem < per_sm) per_sm = by_smem;
@@ -584,7 +600,7 @@ int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, in
                    const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
                    double* d_y_out, int* d_status, int* d_steps, double* d_record, int rec_len, int* d_nrec,
                    int record, int replay, void* stream, double* d_ckpt = nullptr, int ck_cap = 0,
-                   int* d_ckstride = nullptr) {
+                   int* d_ckstride = nullptr, const long long* d_ckoff = nullptr, const int* d_ckcap = nullptr) {
   if (!p || !cfg || ncosmo <= 0 || nset <= 0 || nmode < 0 || blob_len <= deb::HDR_LEN) return DEB_ERR_INVALID;
   if (p->group_size > 0 || p->adj) return DEB_ERR_INVALID;   // grouped / adjoint plans serve their own calls only
   if (nmode == 0) return DEB_OK;
@@ -594,7 +610,8 @@ int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, in
   if ((record || replay) && (!d_record || !d_nrec || rec_len < 2)) return DEB_ERR_INVALID;
   if (record && rec_len < cfg->max_steps + 1) return DEB_ERR_INVALID;
   if (replay && p->exec_mode != DEB_EXEC_WARP) return DEB_ERR_INVALID;
-  if (d_ckpt && (!record || !d_ckstride || ck_cap < 2 || (ck_cap & 1))) return DEB_ERR_INVALID;
+  if (d_ckpt && (!record || !d_ckstride || (!d_ckoff && (ck_cap < 2 || (ck_cap & 1))))) return DEB_ERR_INVALID;
+  if (d_ckoff && !d_ckcap) return DEB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   KParams P{};
   P.tables = d_tables; P.ncosmo = ncosmo; P.blob_len = blob_len; P.k = d_k; P.cosmo = d_cosmo_of_mode;
@@ -603,7 +620,7 @@ int launch_forward(deb_plan* p, const double* d_tables, int ncosmo, int nset, in
   P.smem = p->warp_smem;
   P.kws = p->kws;
   P.rec = d_record; P.rec_len = rec_len; P.nrec = d_nrec; P.nset = nset;
-  P.ckpt = d_ckpt; P.ck_cap = ck_cap; P.ckstride = d_ckstride;
+  P.ckpt = d_ckpt; P.ck_cap = ck_cap; P.ckstride = d_ckstride; P.ckoff = d_ckoff; P.ckcaps = d_ckcap;
   P.order = (!replay && p->user_order && p->user_order_n == nmode) ? p->user_order : nullptr;
   P.ctl.rtol = cfg->rtol; P.ctl.atol = cfg->atol;
   P.ctl.b1 = (cfg->icoeff + cfg->pcoeff + cfg->dcoeff) / cfg->error_order;
@@ -687,10 +704,12 @@ int deb_forward_record(deb_plan* p, const double* d_tables, int ncosmo, int blob
 int deb_forward_record_ckpt(deb_plan* p, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
                             const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
                             double* d_y_out, int* d_status, int* d_steps, double* d_record, int rec_len, int* d_nrec,
-                            double* d_ckpt, int ck_cap, int* d_ckstride, void* stream) {
+                            double* d_ckpt, int ck_cap, const long long* d_ckoff, const int* d_ckcap,
+                            int* d_ckstride, void* stream) {
   if (!d_ckpt) return DEB_ERR_INVALID;
   return launch_forward(p, d_tables, ncosmo, 1, blob_len, d_k, d_cosmo_of_mode, nmode, d_tau_out, cfg, d_y_out,
-                        d_status, d_steps, d_record, rec_len, d_nrec, 1, 0, stream, d_ckpt, ck_cap, d_ckstride);
+                        d_status, d_steps, d_record, rec_len, d_nrec, 1, 0, stream, d_ckpt, ck_cap, d_ckstride,
+                        d_ckoff, d_ckcap);
 }
 
 int deb_replay(deb_plan* p, const double* d_tables, int ncosmo, int nset, int blob_len, const double* d_k,

@@ -171,6 +171,25 @@ def seg_cap_for(max_steps, ck_cap):
     return max(1, -(-2 * int(max_steps) // int(ck_cap)))
 
 
+# Checkpoint stride the adjoint plans allow (its segment buffer holds this many
+# states per warp); every mode keeps at least 2 max_steps / SEG_CAP slots so that
+# thinning stays within it, whatever its step count.
+SEG_CAP = 64
+
+
+def checkpoint_caps(nrec, max_steps, margin=1.25, extra=16):
+    """Per-mode checkpoint slots fitted to recorded step counts: room for a
+    state after every step with margin for other parameters of similar
+    step counts (stride 1: the adjoint recomputes nothing), at least
+    2 max_steps / SEG_CAP (a mode that outgrows its slots thins them, and
+    its stride stays within the plan's segment buffer), even."""
+    seg_floor = -(-2 * int(max_steps) // SEG_CAP)
+    caps = np.maximum(np.ceil(np.asarray(nrec, dtype=np.float64) * margin).astype(np.int64) + extra, seg_floor)
+    caps += caps & 1
+    offs = np.concatenate([[0], np.cumsum(caps)[:-1]])
+    return caps.astype(np.int32), offs.astype(np.int64), int(caps.sum()), seg_floor
+
+
 _adj_plans: dict = {}
 
 
@@ -265,8 +284,12 @@ class GradientProblem:
         self._copied = None
         if self.method == "adjoint":
             n = _pt.nvar(lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax)
-            self.ck_cap = int(ck_cap) + (int(ck_cap) & 1)
+            # uniform slots until fit_checkpoints() lays them out by step counts
+            self.ck_cap = max(int(ck_cap), -(-2 * int(max_steps) // SEG_CAP))
+            self.ck_cap += self.ck_cap & 1
             self.d_ckpt = torch.empty((nm, self.ck_cap, n), dtype=torch.float64, device=dev)
+            self.d_ckoff = self.d_ckcap = None
+            self.max_steps = int(max_steps)
             self.d_ckstride = torch.empty((nm,), dtype=torch.int32, device=dev)
             # the Jacobian takes one cotangent seed per output time (seed o is
             # d ln P(k, a_o) / d y); a vector-Jacobian product takes one
@@ -276,7 +299,7 @@ class GradientProblem:
             self.d_gth = torch.empty((nsd, nm, self.npar), dtype=torch.float64, device=dev)
             self.d_ast = torch.empty((nsd * nm,), dtype=torch.int32, device=dev)
             self.eps_c = self._dev["eps_c"]     # [ncosmo, npar], reloaded by load()
-            self.adj_plan = adjoint_plan(self.dims, nsd * nm, seg_cap_for(max_steps, self.ck_cap))
+            self.adj_plan = adjoint_plan(self.dims, nsd * nm, SEG_CAP)
 
     def load(self, plist, backgrounds, pert, stream=None):
         """Copy the inputs of another set of cosmologies of the same shape
@@ -327,12 +350,13 @@ class GradientProblem:
     def _record(self, plan, s):
         L = _native.load()
         c = lambda t: ctypes.c_void_p(t.data_ptr())
+        co = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
         if self.method == "adjoint":
             _native.check(_pt.launch_ordered(plan, self.order, self.nmode, lambda: L.deb_forward_record_ckpt(
                 plan.ptr, c(self.d_tab0), self.nc, self.blob_len, c(self.d_k), c(self.d_com), self.nmode,
                 c(self.d_tau0), ctypes.byref(self.cfg), c(self.d_y0), c(self.d_st0), c(self.d_steps), c(self.d_rec),
-                self.rec_len, c(self.d_nrec), c(self.d_ckpt), self.ck_cap, c(self.d_ckstride),
-                ctypes.c_void_p(s.cuda_stream))), "deb_forward_record_ckpt")
+                self.rec_len, c(self.d_nrec), c(self.d_ckpt), self.ck_cap, co(self.d_ckoff), co(self.d_ckcap),
+                c(self.d_ckstride), ctypes.c_void_p(s.cuda_stream))), "deb_forward_record_ckpt")
             return
         _native.check(_pt.launch_ordered(plan, self.order, self.nmode, lambda: L.deb_forward_record(
             plan.ptr, c(self.d_tab0), self.nc, self.blob_len, c(self.d_k), c(self.d_com), self.nmode,
@@ -346,8 +370,30 @@ class GradientProblem:
         _native.check(L.deb_adjoint(self.adj_plan.ptr, c(self.d_tab0), c(self.d_tabs), self.nc, self.npar,
                                     self.blob_len, c(self.eps_c), c(self.d_k), c(self.d_com), self.nmode,
                                     c(self.d_tau0), c(self.d_taus), c(self.d_rec), self.rec_len, c(self.d_nrec),
-                                    c(self.d_ckpt), self.ck_cap, c(self.d_ckstride), c(self.d_gy), int(nseed),
+                                    c(self.d_ckpt), self.ck_cap,
+                                    None if self.d_ckoff is None else c(self.d_ckoff), c(self.d_ckstride),
+                                    c(self.d_gy), int(nseed),
                                     c(self.d_gth), c(self.d_ast), ctypes.c_void_p(s.cuda_stream)), "deb_adjoint")
+
+    def fit_checkpoints(self, margin=1.25):
+        """Lay the checkpoint slots out per mode from the last record's step
+        counts (checkpoint_caps): afterwards every mode whose step count grows
+        by less than the margin keeps a state after every step, and the
+        adjoint recomputes no segment.  Synchronises; call it between runs,
+        before a graph capture.  Returns the pool's bytes."""
+        import torch
+
+        if self.method != "adjoint":
+            return 0
+        torch.cuda.synchronize()
+        nrec = self.d_nrec.cpu().numpy()
+        caps, offs, total, _ = checkpoint_caps(nrec, self.max_steps, margin)
+        n = self.d_ckpt.shape[-1]
+        self.d_ckpt = None
+        self.d_ckpt = torch.empty((total, n), dtype=torch.float64, device=self.device)
+        self.d_ckcap = torch.as_tensor(caps).to(self.device)
+        self.d_ckoff = torch.as_tensor(offs).to(self.device)
+        return self.d_ckpt.numel() * 8
 
     def forward(self, stream=None):
         """The recorded nominal solve (with checkpoints when the method is the
@@ -462,6 +508,10 @@ class GradientProblem:
 
         self.run()
         torch.cuda.synchronize()
+        if self.method == "adjoint" and self.d_ckoff is None:
+            self.fit_checkpoints()
+            self.run()
+            torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
             self.run(torch.cuda.current_stream())
@@ -648,6 +698,10 @@ class LoglikeProblem:
 
         self.run()
         torch.cuda.synchronize()
+        if self.gp.d_ckoff is None:
+            self.gp.fit_checkpoints()
+            self.run()
+            torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
             self.out = self.run(torch.cuda.current_stream())

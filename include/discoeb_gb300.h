@@ -197,12 +197,18 @@ int deb_replay(deb_plan* plan, const double* d_tables, int ncosmo, int nset, int
  * dropped and the stride doubles, so a mode keeps between ck_cap / 2 and
  * ck_cap evenly spaced states (ck_cap even, >= 2).
  *   d_ckpt [nmode, ck_cap, nvar], d_ckstride [nmode] (the final stride)
+ * With d_ckoff (and d_ckcap) the slots are laid out per mode instead: mode m
+ * owns d_ckcap[m] slots (taken down to even, >= 2) from slot d_ckoff[m] of
+ * the pool d_ckpt [sum of caps, nvar], so that modes with long step
+ * sequences get room for a state after every step (stride 1: the adjoint
+ * recomputes nothing) while short ones take little; ck_cap is then unused.
  * No counterpart in the reference (jax.jacfwd keeps no states).
  */
 int deb_forward_record_ckpt(deb_plan* plan, const double* d_tables, int ncosmo, int blob_len, const double* d_k,
                             const int* d_cosmo_of_mode, int nmode, const double* d_tau_out, const deb_solver_cfg* cfg,
                             double* d_y_out, int* d_status, int* d_steps, double* d_record, int rec_len, int* d_nrec,
-                            double* d_ckpt, int ck_cap, int* d_ckstride, void* stream);
+                            double* d_ckpt, int ck_cap, const long long* d_ckoff, const int* d_ckcap,
+                            int* d_ckstride, void* stream);
 
 /*
  * Discrete adjoint of the recorded solve: for a cotangent of the output
@@ -233,8 +239,8 @@ int deb_forward_record_ckpt(deb_plan* plan, const double* d_tables, int ncosmo, 
  *   d_tables_pm   [ncosmo * 2 npar, blob_len]: set 2p = +eps_p, 2p+1 = -eps_p
  *   d_eps         [ncosmo, npar]
  *   d_tau_out     [ncosmo, nout], d_tau_out_pm [ncosmo * 2 npar, nout]
- *   d_record, rec_len, d_nrec, d_ckpt, ck_cap, d_ckstride: from
- *                 deb_forward_record_ckpt on d_tables
+ *   d_record, rec_len, d_nrec, d_ckpt, ck_cap, d_ckoff, d_ckstride: from
+ *                 deb_forward_record_ckpt on d_tables (d_ckoff may be NULL)
  *   d_gy          [nseed, nmode, nout, 20] cotangents of the output fields
  *   d_gtheta      [nseed, nmode, npar] dL/dtheta per seed and mode (NaN for
  *                 a failed item)
@@ -245,8 +251,8 @@ int deb_plan_create_adjoint(const deb_dims* dims, int max_items, int seg_cap, de
 int deb_adjoint(deb_plan* plan, const double* d_tables, const double* d_tables_pm, int ncosmo, int npar, int blob_len,
                 const double* d_eps, const double* d_k, const int* d_cosmo_of_mode, int nmode,
                 const double* d_tau_out, const double* d_tau_out_pm, const double* d_record, int rec_len,
-                const int* d_nrec, const double* d_ckpt, int ck_cap, const int* d_ckstride, const double* d_gy,
-                int nseed, double* d_gtheta, int* d_status, void* stream);
+                const int* d_nrec, const double* d_ckpt, int ck_cap, const long long* d_ckoff, const int* d_ckstride,
+                const double* d_gy, int nseed, double* d_gtheta, int* d_status, void* stream);
 
 /*
  * The reference's batched variant, evolve_perturbations_batched

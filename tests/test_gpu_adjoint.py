@@ -17,7 +17,8 @@
   and branches, so the adjoints of the two eps agree with each other to
   1e-6 everywhere;
 * the checkpoint count does not change the result (8 slots, strides up to
-  a few hundred, vs a slot per step);
+  a few hundred, vs a slot per step, vs slots laid out per mode from the
+  step counts);
 * PowerSpectrum.backward (one adjoint sweep with grad_P) against the
   contraction of the replay's Jacobian.
 The host build of the same code (tests/test_adjoint_cpu.py) is not a GPU
@@ -130,6 +131,14 @@ def test_checkpoint_count_does_not_change_the_gradient(base):
     assert out[0][1].max() > 1 and out[1][1].max() == 1
     scale = np.abs(out[1][0]).max(axis=(0, 1))
     assert (np.abs(out[0][0] - out[1][0]) <= 1e-9 * scale).all()
+    # slots laid out per mode from the step counts: stride 1 everywhere
+    gp = GradientProblem([base], "native", pert, k, [1.0], method="adjoint", ck_cap=8, **kw, **DIMS)
+    gp.run()
+    gp.fit_checkpoints()
+    _, D = gp.run()
+    gp.check()
+    assert gp.d_ckstride.cpu().numpy().max() == 1 and gp.d_ckoff is not None
+    assert (np.abs(D.cpu().numpy() - out[1][0]) <= 1e-9 * scale).all()
 
 
 def test_adjoint_at_the_fiducial_gradient_workload(base):
