@@ -734,12 +734,23 @@ HD void phi_pass(const Grp<G>& gp, const AdjItem& it, const Dims& D, const doubl
                  double a, double t, double mu0, double* res, double* res2, Coef<double>* cf_out,
                  Coef<Jet<double>>* cj_out) {
   const int nev = 2 + 2 * it.npar;
-  for (int e = gp.lane; e < nev; e += G) {
+  // the nominal coefficients asked for (cf_out / cj_out) on a lane of their
+  // own, slot nev, beside the slots instead of after slot 0's jets
+  const bool extra = cf_out || cj_out;
+  for (int e = gp.lane; e < nev + (extra ? 1 : 0); e += G) {
     Cosmo c;
     ModeConst m;
-    const int set = e < 2 ? -1 : e - 2;
-    if (!item_cosmo(it, set, c)) { res[e] = 0.0; if (res2) res2[e] = 0.0; continue; }
+    const int set = (e < 2 || e == nev) ? -1 : e - 2;
+    if (!item_cosmo(it, set, c)) {
+      if (e < nev) { res[e] = 0.0; if (res2) res2[e] = 0.0; }
+      continue;
+    }
     mode_const(c, it.k, m);
+    if (e == nev) {
+      if (cj_out) *cj_out = coef<Jet<double>>(c, m, D, Jet<double>(a, 1.0), Jet<double>(t), mu0);
+      else *cf_out = coef<double>(c, m, D, a, t, mu0);
+      continue;
+    }
     if (e == 0) {
       if (B2) {
         // a-jet of a-jet: d phi(B) / da and d2 phi(B2) / da2
@@ -748,20 +759,9 @@ HD void phi_pass(const Grp<G>& gp, const AdjItem& it, const Dims& D, const doubl
         const Coef<J2> C = coef<J2>(c, m, D, aj, J2(t), mu0);
         res[e] = phi<J2>(C, B, m.k).v.d;
         res2[e] = d12(phi<J2>(C, B2, m.k));
-        if (cj_out) {
-          Coef<Jet<double>> Cj;
-          const Jet<double> aj1(a, 1.0);
-          Cj = coef<Jet<double>>(c, m, D, aj1, Jet<double>(t), mu0);
-          *cj_out = Cj;
-        }
       } else {
         const Coef<Jet<double>> C = coef<Jet<double>>(c, m, D, Jet<double>(a, 1.0), Jet<double>(t), mu0);
         res[e] = phi<Jet<double>>(C, B, m.k).d;
-        if (cf_out) {
-          Coef<double> Cv;
-          Cv = coef<double>(c, m, D, a, t, mu0);
-          *cf_out = Cv;
-        }
       }
     } else if (e == 1) {
       const Coef<Jet<double>> C = coef<Jet<double>>(c, m, D, Jet<double>(a), Jet<double>(t, 1.0), mu0);
