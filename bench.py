@@ -609,7 +609,7 @@ def run_loglike(args, inp, world, rank, local):
         ev[0].record(stream)
         P = gp.forward(stream)
         ev[1].record(stream)
-        lp.run(stream)
+        lp.backward(P, stream)
         ev[2].record(stream)
         split.append(ev)
     torch.cuda.synchronize()

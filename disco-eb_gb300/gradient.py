@@ -680,9 +680,16 @@ class LoglikeProblem:
     def run(self, stream=None):
         import torch
 
+        s = stream if stream is not None else torch.cuda.current_stream()
+        return self.backward(self.gp.forward(s), s)
+
+    def backward(self, P, stream=None):
+        """The likelihood of the P a :meth:`GradientProblem.forward` left and
+        its gradient by the adjoint sweep; returns (P, ln L, gradient)."""
+        import torch
+
         gp = self.gp
         s = stream if stream is not None else torch.cuda.current_stream()
-        P = gp.forward(s)
         with torch.cuda.stream(s):
             r = torch.log(P) - self.d_data
             gP = -self.d_w * r / P

@@ -92,7 +92,8 @@ def _close(pairs, bar, lnp_round=4e-12):
     that is kink-free at one eps at least (most of them, asserted); and the
     adjoints of the two eps agree everywhere."""
     mask = np.stack([p[2] for p in pairs])
-    assert mask.all(axis=0).mean() <= 0.15, mask.mean(axis=(1, 2))
+    both = mask.all(axis=0)
+    assert both.sum() <= max(1, 0.15 * both.size), mask.mean(axis=(1, 2))
     for j, name in enumerate(THETA):
         scale = np.abs(pairs[0][1][..., j]).max()
         err = np.stack([np.where(mk, np.nan, np.abs(Da[..., j] - Dr[..., j]) - lnp_round / (2 * eps[j]))
