@@ -493,6 +493,11 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+# DRAM read + write bytes per accepted step of adjoint_kernel, from an ncu capture of
+# profile_1cosmo_1216k_n1098_8a_rtol1e-6_loglike (88.3 GB for 30 893 accepted steps)
+ADJ_DRAM_BYTES_PER_STEP = 88.25e9 / 30893
+
+
 def algorithmic_flops_adjoint_step(dims, nq):
     """FP64 flops of one accepted step of the adjoint sweep: the recomputed
     forward step, and the eight stages backwards -- a transposed structured
@@ -713,10 +718,12 @@ def run_loglike(args, inp, world, rank, local):
                 "inputs": "parameter dicts (tables of all 13 sets per cosmology produced on the host cores inside "
                           "the timed call) and the data vector; P(k, a), ln L and the gradient copied back"},
         "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": "adjoint_kernel",
-                     "note": "FP64-issue bound (state in L2, DRAM traffic small); peak = FP64 FMA microkernel measured "
-                             "in this run (MEASURED_PEAKS.json has no FP64 figure); achieved = algorithmic FLOPs of the "
-                             "adjoint sweep (per accepted step + recomputed segment steps) / the adjoint launch's time"},
+                     "frac": achieved / peak, "traffic": ADJ_DRAM_BYTES_PER_STEP * acc, "kernel": "adjoint_kernel",
+                     "note": "FP64 pipe ~half busy, latency-bound (2 warps per scheduler at 255 registers, global-memory "
+                             "waits); peak = FP64 FMA microkernel measured in this run (MEASURED_PEAKS.json has no FP64 "
+                             "figure); achieved = algorithmic FLOPs of the adjoint sweep (per accepted step + "
+                             "recomputed segment steps) / the adjoint launch's time; traffic = DRAM bytes per accepted "
+                             "step of an ncu capture of the counter-capture workload x accepted steps"},
         "gpu_launches": 3 * args.steps,
         "clocks": clk.summary(),
         "forward_ms_median": statistics.median(fwd_ms), "adjoint_ms_median": statistics.median(step_ms),

@@ -189,6 +189,9 @@ int deb_plan_create_adjoint(const deb_dims* dims, int max_items, int seg_cap, de
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_kernel, 32, kAdjSmem) != cudaSuccess)
     return DEB_ERR_CUDA;
   if (per_sm < 1) return DEB_ERR_INVALID;
+#ifdef DEB_ADJ_WARPS_PER_SM_CAP
+  if (per_sm > DEB_ADJ_WARPS_PER_SM_CAP) per_sm = DEB_ADJ_WARPS_PER_SM_CAP;
+#endif
   deb_plan* p = new deb_plan();
   p->D = deb::make_dims(dims->lmaxg, dims->lmaxgp, dims->lmaxr, dims->lmaxnu, dims->nqmax);
   p->nout = dims->nout;
