@@ -189,9 +189,13 @@ int deb_plan_create_adjoint(const deb_dims* dims, int max_items, int seg_cap, de
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_kernel, 32, kAdjSmem) != cudaSuccess)
     return DEB_ERR_CUDA;
   if (per_sm < 1) return DEB_ERR_INVALID;
-#ifdef DEB_ADJ_WARPS_PER_SM_CAP
-  if (per_sm > DEB_ADJ_WARPS_PER_SM_CAP) per_sm = DEB_ADJ_WARPS_PER_SM_CAP;
-#endif
+  {
+    // the vectors a warp touches every step: its forward slot, the adjoint
+    // vectors and one segment state
+    const deb::Dims D = deb::make_dims(dims->lmaxg, dims->lmaxgp, dims->lmaxr, dims->lmaxnu, dims->nqmax);
+    const long hot = (deb::slot_len(D) + (long)(deb::NAV + 1) * D.n) * (long)sizeof(double);
+    per_sm = deb_internal::l2_warps_per_sm(dev, nsm, hot, per_sm);
+  }
   deb_plan* p = new deb_plan();
   p->D = deb::make_dims(dims->lmaxg, dims->lmaxgp, dims->lmaxr, dims->lmaxnu, dims->nqmax);
   p->nout = dims->nout;

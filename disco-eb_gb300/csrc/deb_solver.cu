@@ -467,6 +467,10 @@ int deb_plan_create_ex(const deb_dims* dims, int max_modes, const deb_launch_cfg
       const int by_smem = (int)(sm_bytes / (smem_bytes + 1024));
       if (by_smem < per_sm) per_sm = by_smem;
     }
+    // every per-mode vector in global memory and no cap given: as many
+    // modes per SM as share L2 without evicting each other
+    if (!p->warp_smem && mps_cap == 0)
+      per_sm = deb_internal::l2_warps_per_sm(dev, nsm, p->slot_len * (long)sizeof(double), per_sm);
     if (mps_cap > 0 && mps_cap < per_sm) per_sm = mps_cap;
     if (per_sm < 1) per_sm = 1;
     p->warp_per_sm = per_sm;
