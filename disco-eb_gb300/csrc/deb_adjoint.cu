@@ -51,6 +51,7 @@ struct AParams {
   int* queue;
   const int* order;          // modes, most recorded steps first
   deb::Dims D;
+  int shared_vectors;        // the NSHV hottest adjoint vectors in shared memory
 };
 
 // Warps per SM the register allocation must leave room for (the kernel is
@@ -75,6 +76,7 @@ __global__ void __launch_bounds__(32, DEB_ADJ_MIN_WARPS_PER_SM) adjoint_kernel(A
   A.seg_cap = P.seg_cap;
   A.sc = smem;
   A.n = n;
+  A.shv = P.shared_vectors ? smem + deb::SC_LEN : nullptr;
   const long items = (long)P.nmode * P.nseed;
   for (;;) {
     int q = 0;
@@ -164,6 +166,30 @@ int adj_upload_constants() {
 }
 
 constexpr size_t kAdjSmem = deb::SC_LEN * sizeof(double);
+// with the hottest adjoint vectors in shared memory as well
+size_t adj_smem_bytes(const deb::Dims& D, bool shared_vectors) {
+  return kAdjSmem + (shared_vectors ? (size_t)deb::NSHV * D.n * sizeof(double) : 0);
+}
+
+// the kernel's dynamic shared-memory limit, raised to at least bytes in the
+// current context (never lowered, so plans of other sizes keep working)
+std::mutex g_adj_smem_mu;
+unsigned long long g_adj_smem_ctx[64] = {0};
+size_t g_adj_smem_set[64] = {0};
+int adj_raise_smem(size_t bytes) {
+  if (bytes <= 48 * 1024) return DEB_OK;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DEB_ERR_CUDA;
+  const unsigned long long ctx = deb_internal::current_ctx_id();
+  std::lock_guard<std::mutex> lk(g_adj_smem_mu);
+  if (ctx != 0 && g_adj_smem_ctx[dev] == ctx && g_adj_smem_set[dev] >= bytes) return DEB_OK;
+  const size_t want = (g_adj_smem_ctx[dev] == ctx && g_adj_smem_set[dev] > bytes) ? g_adj_smem_set[dev] : bytes;
+  if (cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want) != cudaSuccess)
+    return DEB_ERR_CUDA;
+  g_adj_smem_ctx[dev] = ctx;
+  g_adj_smem_set[dev] = want;
+  return DEB_OK;
+}
 
 }  // namespace
 
@@ -196,7 +222,21 @@ int deb_plan_create_adjoint(const deb_dims* dims, int max_items, int seg_cap, de
     const long hot = (deb::slot_len(D) + (long)(deb::NAV + 1) * D.n) * (long)sizeof(double);
     per_sm = deb_internal::l2_warps_per_sm(dev, nsm, hot, per_sm);
   }
+  // the hottest adjoint vectors in shared memory when that leaves the warps
+  // per SM chosen above (the kernel's attribute is only ever raised)
+  const deb::Dims Dm = deb::make_dims(dims->lmaxg, dims->lmaxgp, dims->lmaxr, dims->lmaxnu, dims->nqmax);
+  size_t smem = kAdjSmem;
+  {
+    int optin = 0, per_sm_bytes = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&per_sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    const size_t want = adj_smem_bytes(Dm, true);
+    if (want <= (size_t)optin && (long)per_sm * (long)(want + 1024) <= (long)per_sm_bytes &&
+        adj_raise_smem(want) == DEB_OK)
+      smem = want;
+  }
   deb_plan* p = new deb_plan();
+  p->adj_smem = (long)smem;
   p->D = deb::make_dims(dims->lmaxg, dims->lmaxgp, dims->lmaxr, dims->lmaxnu, dims->nqmax);
   p->nout = dims->nout;
   p->exec_mode = DEB_EXEC_WARP;
@@ -245,11 +285,13 @@ int deb_adjoint(deb_plan* p, const double* d_tables, const double* d_tables_pm, 
   P.ckpt = d_ckpt; P.ck_cap = ck_cap; P.ckoff = d_ckoff; P.ckstride = d_ckstride; P.gy = d_gy; P.gth = d_gtheta; P.status = d_status;
   P.ws = p->adj_ws; P.wslot = p->adj_wslot; P.seg_cap = p->adj_seg_cap; P.queue = p->queue; P.order = p->order_dev;
   P.D = p->D;
+  P.shared_vectors = p->adj_smem > (long)kAdjSmem;
+  if (P.shared_vectors && adj_raise_smem((size_t)p->adj_smem) != DEB_OK) return DEB_ERR_CUDA;
   if (cudaMemsetAsync(p->queue, 0, sizeof(int), s) != cudaSuccess) return DEB_ERR_CUDA;
   rank_desc_adj_kernel<<<(nmode + 255) / 256, 256, 0, s>>>(d_nrec, nmode, p->order_dev);
   const long items = (long)nmode * nseed;
   const int blocks = (int)(items < p->adj_warps ? items : p->adj_warps);
-  adjoint_kernel<<<blocks, 32, kAdjSmem, s>>>(P);
+  adjoint_kernel<<<blocks, 32, (size_t)p->adj_smem, s>>>(P);
   return cudaGetLastError() == cudaSuccess ? DEB_OK : DEB_ERR_CUDA;
 }
 

@@ -259,6 +259,15 @@ enum { SC_B = 0, SC_BW = SC_B + NB, SC_BR = SC_BW + NB, SC_CF = SC_BR + NB,   //
        SC_TO = SC_SCAL + 16, SC_FT = SC_TO + 64, SC_OC = SC_FT + 72, SC_LEN = SC_OC + 16 };
 enum { SS_TB0 = 0, SS_DTB, SS_DBAR, SS_STS, SS_TBN, SS_CFB, SS_A0 };
 
+// The adjoint vectors read most often in a step -- r (every pass of the
+// transposed solve, the forms, J^T), Y_h and Y_e (each solve's Woodbury
+// term), ubar and the stage point -- can live in shared memory (AWS::shv,
+// NSHV vectors of n) when the launch has room; the others stay in global.
+constexpr int NSHV = 5;
+HD int shared_slot(int i) {
+  return i == A_RB ? 0 : i == A_YH ? 1 : i == A_YE ? 2 : i == A_UB ? 3 : i == A_TMP ? 4 : -1;
+}
+
 template <int G>
 struct AWS {
   WS<G> w;
@@ -267,7 +276,12 @@ struct AWS {
   int seg_cap;
   double* sc;      // scratch, SC_LEN doubles
   int n;
-  HD VecRef vec(int i) const { return VecRef{av + (long)i * n * WS<G>::S, WS<G>::S}; }
+  double* shv = nullptr;   // NSHV shared vectors (contiguous), or null
+  HD VecRef vec(int i) const {
+    const int sl = shv ? shared_slot(i) : -1;
+    if (sl >= 0) return VecRef{shv + (long)sl * n, 1};
+    return VecRef{av + (long)i * n * WS<G>::S, WS<G>::S};
+  }
   HD VecRef fv(int i) const { return VecRef{&w.v(i, 0), WS<G>::S}; }
   HD VecRef segv(int j) const { return VecRef{seg + (long)j * n * WS<G>::S, WS<G>::S}; }
 };

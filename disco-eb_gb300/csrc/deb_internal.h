@@ -33,6 +33,7 @@ struct deb_plan {
   // segment, per-warp workspace (doubles) and its array
   int adj, adj_warps, adj_seg_cap;
   long adj_wslot;
+  long adj_smem;   // dynamic shared memory of the adjoint launch (bytes)
   double* adj_ws;
 };
 
