@@ -716,7 +716,8 @@ def run_loglike(args, inp, world, rank, local):
         "detail": {"checkpoints": f"per-mode slots fitted to the step counts ({gp.d_ckpt.numel() * 8 / 1e9:.1f} GB), "
                                   f"strides {int(strides.min())}-{int(strides.max())}",
                    "cuda_graph": "record + get_power + likelihood + adjoint captured once, replayed per step",
-                   "launch_shape": launch, "autotune_ms": {f"{a}/{b}": round(v, 2) for (a, b), v in tune_ms.items()}},
+                   "launch_shape": launch, "adjoint_launch": gp.adj_plan.launch_info(),
+                   "autotune_ms": {f"{a}/{b}": round(v, 2) for (a, b), v in tune_ms.items()}},
         "e2e": {"value": total_cosmo / t_e2e if world == 1 else None,
                 "unit": "cosmology solves/s (P(k, a) + 8-parameter gradient)",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),

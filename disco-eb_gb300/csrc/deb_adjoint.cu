@@ -220,7 +220,7 @@ int deb_plan_create_adjoint(const deb_dims* dims, int max_items, int seg_cap, de
     // vectors and one segment state
     const deb::Dims D = deb::make_dims(dims->lmaxg, dims->lmaxgp, dims->lmaxr, dims->lmaxnu, dims->nqmax);
     const long hot = (deb::slot_len(D) + (long)(deb::NAV + 1) * D.n) * (long)sizeof(double);
-    per_sm = deb_internal::l2_warps_per_sm(dev, nsm, hot, per_sm);
+    per_sm = deb_internal::l2_warps_per_sm(dev, nsm, hot, per_sm, 1.6);
   }
   // the hottest adjoint vectors in shared memory when that leaves the warps
   // per SM chosen above (the kernel's attribute is only ever raised)

@@ -70,17 +70,18 @@ inline unsigned long long current_ctx_id() {
 }
 
 // Warps per SM for a kernel whose warps each work on hot_bytes of global
-// memory: about 1.6x the SM's share of L2 (measured at nvar 1098: the
-// adjoint is fastest at 4 warps per SM, 338 KB each, the record at 6-7,
-// 180 KB each; more warps in flight evict each other's vectors, fewer hide
-// less latency), at least 2, at most max_per_sm.
-inline int l2_warps_per_sm(int dev, int nsm, long hot_bytes, int max_per_sm) {
+// memory: the warps whose bytes fill `fill` times the SM's share of L2
+// (measured at nvar 1098: the adjoint, ~300 KB a warp, is fastest at 4
+// warps per SM, fill 1.6; the record, 141 KB a mode, at 6, fill 1.1; more
+// warps in flight evict each other's vectors, fewer hide less latency), at
+// least 2, at most max_per_sm.
+inline int l2_warps_per_sm(int dev, int nsm, long hot_bytes, int max_per_sm, double fill) {
   int l2 = 0;
   if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess || l2 <= 0 || nsm <= 0 ||
       hot_bytes <= 0)
     return max_per_sm;
   const double share = (double)l2 / nsm;
-  int w = (int)(1.6 * share / (double)hot_bytes + 0.5);
+  int w = (int)(fill * share / (double)hot_bytes);
   if (w < 2) w = 2;
   return w < max_per_sm ? w : max_per_sm;
 }

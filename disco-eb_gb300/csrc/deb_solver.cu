@@ -470,7 +470,7 @@ int deb_plan_create_ex(const deb_dims* dims, int max_modes, const deb_launch_cfg
     // every per-mode vector in global memory and no cap given: as many
     // modes per SM as share L2 without evicting each other
     if (!p->warp_smem && mps_cap == 0)
-      per_sm = deb_internal::l2_warps_per_sm(dev, nsm, p->slot_len * (long)sizeof(double), per_sm);
+      per_sm = deb_internal::l2_warps_per_sm(dev, nsm, p->slot_len * (long)sizeof(double), per_sm, 1.1);
     if (mps_cap > 0 && mps_cap < per_sm) per_sm = mps_cap;
     if (per_sm < 1) per_sm = 1;
     p->warp_per_sm = per_sm;
@@ -562,7 +562,13 @@ int deb_plan_create_grouped(const deb_dims* dims, int max_modes, int batch_size,
 
 int deb_plan_launch_info(const deb_plan* p, deb_launch_cfg* cfg, int* modes_in_flight) {
   if (!p || !cfg || !modes_in_flight) return DEB_ERR_INVALID;
-  if (p->group_size > 0) {
+  if (p->adj) {
+    // adjoint plan: warps (items) in flight and per SM; "shared" when its
+    // hottest vectors live in shared memory
+    cfg->stage_vectors = p->adj_smem > 48 * 1024 ? DEB_STAGE_SHARED : DEB_STAGE_ALL_GLOBAL;
+    cfg->modes_per_sm = p->nsm > 0 ? (p->adj_warps + p->nsm - 1) / p->nsm : 0;
+    *modes_in_flight = p->adj_warps;
+  } else if (p->group_size > 0) {
     cfg->stage_vectors = DEB_STAGE_GLOBAL;
     cfg->modes_per_sm = 0;
     *modes_in_flight = p->group_warps * p->group_size;
