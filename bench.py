@@ -1053,7 +1053,10 @@ def run_reference(args):
     inp = make_inputs(args.workload, 0, 1)
     threads = os.cpu_count() or 1
     cm = cpu_measure(inp, budget_s=args.cpu_seconds, threads=threads)
-    cap = cm["dense"]["cap"]
+    # each timed step: the same sample for fewer attempted steps per mode, about ref_step_seconds of work
+    # (steps/s does not depend on how many of a mode's early steps are run: the dense LU costs the same
+    # every step), so that warm-up + timed steps end within minutes
+    cap = max(4, int(cm["dense"]["cap"] * min(1.0, args.ref_step_seconds / max(cm["dense"]["seconds"], 1e-3))))
     num_k = inp["num_k"]
     ks = np.asarray(inp["kgrid"])[np.arange(0, num_k, cm["stride"])]
     tab0, tau0 = inp["tables"][0], np.asarray(inp["tau"])[0]
@@ -1104,6 +1107,8 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--max-steps", type=int, default=8192)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=4.0,
+                    help="reference arm: CPU seconds of each timed step's bounded sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--exec-mode", default="auto", choices=["auto", "lane", "warp"])
     ap.add_argument("--no-tune", dest="tune", action="store_false", help="skip the launch-shape autotuner")
