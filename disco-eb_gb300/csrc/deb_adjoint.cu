@@ -237,6 +237,7 @@ int deb_plan_create_adjoint(const deb_dims* dims, int max_items, int seg_cap, de
   }
   deb_plan* p = new deb_plan();
   p->adj_smem = (long)smem;
+  p->adj_shared = smem > kAdjSmem ? 1 : 0;
   p->D = deb::make_dims(dims->lmaxg, dims->lmaxgp, dims->lmaxr, dims->lmaxnu, dims->nqmax);
   p->nout = dims->nout;
   p->exec_mode = DEB_EXEC_WARP;

@@ -34,6 +34,7 @@ struct deb_plan {
   int adj, adj_warps, adj_seg_cap;
   long adj_wslot;
   long adj_smem;   // dynamic shared memory of the adjoint launch (bytes)
+  int adj_shared;  // its hottest vectors in shared memory
   double* adj_ws;
 };
 
@@ -72,9 +73,10 @@ inline unsigned long long current_ctx_id() {
 // Warps per SM for a kernel whose warps each work on hot_bytes of global
 // memory: the warps whose bytes fill `fill` times the SM's share of L2
 // (measured at nvar 1098: the adjoint, ~300 KB a warp, is fastest at 4
-// warps per SM, fill 1.6; the record, 141 KB a mode, at 6, fill 1.1; more
-// warps in flight evict each other's vectors, fewer hide less latency), at
-// least 2, at most max_per_sm.
+// warps per SM, fill 1.6; more warps in flight evict each other's vectors,
+// fewer hide less latency), at least 2, at most max_per_sm.  (The record,
+// 141 KB a mode, gained from 6 modes per SM on 2048 modes but lost on 4096:
+// it keeps its register-limited 8.)
 inline int l2_warps_per_sm(int dev, int nsm, long hot_bytes, int max_per_sm, double fill) {
   int l2 = 0;
   if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess || l2 <= 0 || nsm <= 0 ||

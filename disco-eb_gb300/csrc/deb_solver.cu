@@ -467,10 +467,6 @@ int deb_plan_create_ex(const deb_dims* dims, int max_modes, const deb_launch_cfg
       const int by_smem = (int)(sm_bytes / (smem_bytes + 1024));
       if (by_smem < per_sm) per_sm = by_smem;
     }
-    // every per-mode vector in global memory and no cap given: as many
-    // modes per SM as share L2 without evicting each other
-    if (!p->warp_smem && mps_cap == 0)
-      per_sm = deb_internal::l2_warps_per_sm(dev, nsm, p->slot_len * (long)sizeof(double), per_sm, 1.1);
     if (mps_cap > 0 && mps_cap < per_sm) per_sm = mps_cap;
     if (per_sm < 1) per_sm = 1;
     p->warp_per_sm = per_sm;
@@ -565,7 +561,7 @@ int deb_plan_launch_info(const deb_plan* p, deb_launch_cfg* cfg, int* modes_in_f
   if (p->adj) {
     // adjoint plan: warps (items) in flight and per SM; "shared" when its
     // hottest vectors live in shared memory
-    cfg->stage_vectors = p->adj_smem > 48 * 1024 ? DEB_STAGE_SHARED : DEB_STAGE_ALL_GLOBAL;
+    cfg->stage_vectors = p->adj_shared ? DEB_STAGE_SHARED : DEB_STAGE_ALL_GLOBAL;
     cfg->modes_per_sm = p->nsm > 0 ? (p->adj_warps + p->nsm - 1) / p->nsm : 0;
     *modes_in_flight = p->adj_warps;
   } else if (p->group_size > 0) {
