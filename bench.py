@@ -498,8 +498,8 @@ def run_ours(args):
 
 
 # DRAM read + write bytes per accepted step of adjoint_kernel, from an ncu capture of
-# profile_1cosmo_1216k_n1098_8a_rtol1e-6_loglike (88.3 GB for 30 893 accepted steps)
-ADJ_DRAM_BYTES_PER_STEP = 88.25e9 / 30893
+# profile_1cosmo_1216k_n1098_8a_rtol1e-6_loglike at 4 warps per SM (23.8 GB for 30 893 accepted steps)
+ADJ_DRAM_BYTES_PER_STEP = 23.80e9 / 30893
 
 
 def algorithmic_flops_adjoint_step(dims, nq):
