@@ -178,3 +178,18 @@ def test_checkpoint_thinning_does_not_change_the_gradient(sets):
     gb, _, infob, _ = H.adjoint(tabs, eps, 0.1, taus, DIMS, gy, ck_cap=4096, **kw)
     assert info8[2] > 1 and infob[2] == 1
     np.testing.assert_array_equal(g8, gb)
+
+
+def test_checkpoint_caps_fit_step_counts():
+    """Per-mode slots: room for a state after every recorded step with a
+    margin, even, and never below 2 max_steps / SEG_CAP, so that a mode whose
+    step count outgrows its slots thins them to a stride within the adjoint
+    plan's segment buffer; offsets lay the modes end to end."""
+    from discoeb_gb300.gradient import SEG_CAP, checkpoint_caps
+
+    nrec = np.array([0, 10, 255, 1000, 5001])
+    caps, offs, total, floor = checkpoint_caps(nrec, 8192)
+    assert floor == -(-2 * 8192 // SEG_CAP)
+    assert (caps % 2 == 0).all() and (caps >= floor).all() and (caps >= 1.25 * nrec).all()
+    assert offs[0] == 0 and (np.diff(offs) == caps[:-1]).all() and total == int(caps.sum())
+    assert (2 * 8192 / caps <= SEG_CAP).all()
