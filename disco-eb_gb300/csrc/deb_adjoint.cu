@@ -54,8 +54,10 @@ struct AParams {
   int shared_vectors;        // the NSHV hottest adjoint vectors in shared memory
 };
 
-// Warps per SM the register allocation must leave room for (the kernel is
-// latency-bound: more resident warps hide more of each warp's memory waits)
+// Warps per SM the register allocation must leave room for: a build-time
+// option, 1 by default (255 registers).  Caps for 12 or 16 warps per SM were
+// measured slower at nvar 1098 (spills), and the plan runs fewer warps than
+// the registers allow anyway (the L2 fit).
 #ifndef DEB_ADJ_MIN_WARPS_PER_SM
 #define DEB_ADJ_MIN_WARPS_PER_SM 1
 #endif

@@ -165,6 +165,9 @@ __global__ void __launch_bounds__(kBlock) forward_lane_kernel(KParams P) {
 }
 
 // One warp per mode: the mode's vectors and MISC block in shared memory.
+// Warps per SM the record kernel's registers must leave room for: a
+// build-time option, 1 by default (~245 registers, 8 warps per SM); 12 or 16
+// were measured no faster at nvar 1098.
 #ifndef DEB_FWD_MIN_WARPS_PER_SM
 #define DEB_FWD_MIN_WARPS_PER_SM 1
 #endif
