@@ -385,6 +385,9 @@ class GradientProblem:
 
         if self.method != "adjoint":
             return 0
+        if self.graph is not None or getattr(self, "_in_graph", False):
+            raise RuntimeError("fit_checkpoints: a captured graph holds the current checkpoint buffers; "
+                               "fit before capturing")
         torch.cuda.synchronize()
         nrec = self.d_nrec.cpu().numpy()
         caps, offs, total, _ = checkpoint_caps(nrec, self.max_steps, margin)
@@ -712,6 +715,7 @@ class LoglikeProblem:
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
             self.out = self.run(torch.cuda.current_stream())
+        self.gp._in_graph = True
         self.graph = g
         return g
 
