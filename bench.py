@@ -861,22 +861,36 @@ def run_gradient(args, inp, world, rank, local):
 
     peak = _native.measure_fp64_peak(stream.cuda_stream)
     att = int(gp.d_steps.sum().item())
-    rep = int(gp.d_nrec.sum().item()) * gp.nset
-    flops = algorithmic_flops_per_step(dims, dims["nqmax"]) * (att + rep)
+    acc = int(gp.d_nrec.sum().item())
+    adjoint = gp.method == "adjoint"
+    if adjoint:
+        # one adjoint sweep per (output, mode) on the recorded steps
+        rep = 0
+        flops = (algorithmic_flops_per_step(dims, dims["nqmax"]) * att
+                 + algorithmic_flops_adjoint_step(dims, dims["nqmax"]) * acc * gp.nseed)
+        how = "discrete adjoint of the recorded steps (deb_adjoint, one sweep per output and mode; jacfwd semantics)"
+    else:
+        rep = acc * gp.nset
+        flops = algorithmic_flops_per_step(dims, dims["nqmax"]) * (att + rep)
+        how = "central differences over the replayed nominal step sequence (jacfwd semantics)"
     kern_s = statistics.median(graph_ms) * 1e-3     # the graph's two solver launches + sub-ms tail work
     achieved = flops / kern_s
     out = {
-        "metric": "P(k)+dP/dtheta solves/s on 1 GB300, batched FP64 (8 parameters; structured Rodas5, tangents of the recorded step sequence)",
+        "metric": "P(k)+dP/dtheta solves/s on 1 GB300, batched FP64 (8 parameters; structured Rodas5, "
+                  + ("adjoint of" if adjoint else "tangents of") + " the recorded step sequence)",
         "value": value, "unit": "cosmology solves/s (P(k) + 8-parameter gradient)", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded cosmology sample, host RECFAST tables for theta and theta +- 1e-4 theta)",
         "config": {"workload": args.workload, "ncosmo_per_gpu": inp["ncosmo"], "num_k": inp["num_k"],
-                   "modes_per_step": gp.nmode, "replay_items_per_step": gp.nmode * gp.nset,
+                   "modes_per_step": gp.nmode,
+                   ("adjoint_items_per_step" if adjoint else "replay_items_per_step"):
+                       gp.nmode * (gp.nseed if adjoint else gp.nset),
                    "nvar": pt.nvar(dims["lmaxg"], dims["lmaxgp"], dims["lmaxr"], dims["lmaxnu"], dims["nqmax"]),
                    "rtol": inp["rtol"], "theta": list(gp.theta),
-                   "gradient": "central differences over the replayed nominal step sequence (jacfwd semantics)",
-                   "cuda_graph": "record + replay + get_power + quotients captured once, replayed per step",
+                   "gradient": how,
+                   "cuda_graph": "record + " + ("adjoint" if adjoint else "replay + quotients")
+                                 + " + get_power captured once, replayed per step",
                    "launch_shape": launch, "autotune_ms": {f"{a}/{b}": round(v, 2) for (a, b), v in tune_ms.items()},
                    "l2": "flushed before every timed step (256 MB write); tables %.1f MB read per step" % ((gp.d_tab0.numel() + gp.d_tabs.numel()) * 8 / 1e6),
                    "aexp_out": inp["aexp"], "cosmology": inp["cosmo_kind"], "step_to_outputs": inp["step_ts"],
@@ -894,13 +908,16 @@ def run_gradient(args, inp, world, rank, local):
         "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
                      "note": "FP64-pipe bound (state in shared memory / L2, DRAM idle); peak = FP64 FMA microkernel measured in this run; "
-                             "achieved = algorithmic FLOPs of the structured Rodas5 step x (attempted + replayed steps)"},
+                             + ("achieved = algorithmic FLOPs of the record (attempted steps) and of the adjoint sweeps "
+                                "(accepted steps x outputs) / the graph's time" if adjoint else
+                                "achieved = algorithmic FLOPs of the structured Rodas5 step x (attempted + replayed steps)")},
         "gpu_launches": 4 * args.steps,
         "clocks": clk.summary(),
         "forward_value": total_cosmo / (statistics.median(rec_ms) * 1e-3),
         "graph_ms_median": statistics.median(graph_ms),
-        "record_ms_eager_median": statistics.median(rec_ms), "replay_ms_eager_median": statistics.median(rep_ms),
-        "attempted_steps_per_launch": att, "replayed_steps_per_launch": rep,
+        "record_ms_eager_median": statistics.median(rec_ms),
+        ("adjoint_ms_eager_median" if adjoint else "replay_ms_eager_median"): statistics.median(rep_ms),
+        "attempted_steps_per_launch": att, "replayed_steps_per_launch": rep, "accepted_steps_per_launch": acc,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(inp, seconds=args.cpu_seconds)
