@@ -222,6 +222,13 @@ class GradientProblem:
     :meth:`replay` re-runs it; :meth:`load` copies the inputs of another
     problem of the same shape into the same device buffers (through pinned
     host memory), so one captured graph serves many calls.
+
+    With ``method="adjoint"`` the record keeps checkpoints and :meth:`run`
+    sweeps one adjoint per (output, mode) instead of the replay;
+    :meth:`fit_checkpoints` lays the checkpoint slots out per mode.  Problems
+    of one shape share the cached plans (their device workspaces and work
+    queues): run them on one stream, or give each its own ``plan`` /
+    ``adj_plan``.
     """
 
     def __init__(self, plist, backgrounds, pert, kmodes, aexp_out, *, lmaxg, lmaxgp, lmaxr, lmaxnu, nqmax, rtol, atol,
