@@ -6,7 +6,9 @@ drawn uniformly over Omegam [.25,.35], Omegab [.04,.055], h [.6,.75],
 n_s [.92,1], ln(1e10 A_s) [2.9,3.2], m_nu [.06,.3] eV, w0 [-1.2,-.8],
 wa [-.3,.3] (w(a) = -1 crossings redrawn), each with 1024 log-spaced k in
 [1e-5, 50] /Mpc, lmax 32 in every hierarchy and 30 momentum bins (nvar
-1098), rtol = atol = 1e-6, 64 output times uniform in a over [0.2, 1].  A
+1098), rtol = atol = 1e-6, 64 output times uniform in a over [0.2, 1] with
+steps landing on them (diffrax step_ts; interpolated inside steps, P(k) at
+this tolerance is off by up to 2 % at the lowest k).  A
 "step" is, for every cosmology, P(k, a) at all 1024 x 64 points, the
 Gaussian log-likelihood of a synthetic data vector (the cosmology's own
 ln P with 5% seeded scatter, diagonal covariance 2 / N_k) and its gradient
