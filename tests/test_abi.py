@@ -71,3 +71,39 @@ def test_new_entry_points_check_their_arguments_without_gpu():
     assert L.deb_evolve_background(ctypes.byref(cfg), 1, 1, 1, 1, 1, 123, None, None) == -1
     assert L.deb_evolve_background_host(ctypes.byref(cfg), 1, 1, 1, 1, 1, 123, None, 1) == -1
     assert L.deb_tau_of_a(None, 1, 100, None, 1, None, None) == -1
+
+
+def test_adjoint_and_frozen_producer_check_their_arguments_without_gpu():
+    """The adjoint entry points and the frozen producer refuse bad arguments
+    before touching the device."""
+    from discoeb_gb300 import _native, tables_gpu
+
+    L = _native.load()
+    vp = ctypes.c_void_p
+    plan = vp()
+    small = _native.DebDims(4, 12, 17, 17, 15, 1, 0, 0, 0)           # lmaxg < 5: no adjoint
+    assert L.deb_plan_create_adjoint(ctypes.byref(small), 8, 4, ctypes.byref(plan)) == -1
+    full = _native.DebDims(12, 12, 17, 17, 15, 1, 1, 0, 0)           # return_full: no adjoint
+    assert L.deb_plan_create_adjoint(ctypes.byref(full), 8, 4, ctypes.byref(plan)) == -1
+    # deb_adjoint without a plan, and with npar out of range
+    args = [None, None, None, 1, 6, 1000, None, None, None, 1, None, None, None, 10, None, None, 32, None, None,
+            None, 1, None, None, None]
+    assert L.deb_adjoint(*args) == -1
+    # the record with checkpoints needs its buffers
+    assert L.deb_forward_record_ckpt(None, None, 1, 1000, None, None, 1, None, None, None, None, None, None, 10,
+                                     None, None, 32, None, None, None, None) == -1
+    # the frozen producers need a leader array (and the device one its step buffer)
+    cfg = tables_gpu.DebBgCfg(256, 512, 8, 3, 128, 1e-9, 1e-3, 1e-6)
+    bl = tables_gpu.blob_len(256, 3)
+    import numpy as np
+
+    from discoeb_gb300.workloads import fiducial_mnu_param
+
+    pm = np.ascontiguousarray(tables_gpu.param_matrix([fiducial_mnu_param()]))
+    c = lambda a: vp(a.ctypes.data)
+    tabs = np.zeros((1, bl))
+    st = np.zeros(1, np.int32)
+    consts, grd = tables_gpu.constants(), tables_gpu.grid(256, 3)
+    assert L.deb_evolve_background_frozen_host(ctypes.byref(cfg), c(pm), 1, None, c(consts), c(grd), None, 0,
+                                               c(tabs), bl, c(st), 1) == -1
+    assert L.deb_evolve_background_frozen(ctypes.byref(cfg), 1, 1, None, 1, 1, None, 0, 1, bl, None, None) == -1
